@@ -1,0 +1,310 @@
+"""Contact-kernel microbenchmark: ACCD time of impact over 10M seeded contact pairs.
+
+Workload (one "step"): one additive-CCD pass over 10,000,000 candidate pairs
+(40% point-triangle, 40% edge-edge, 10% point-edge, 10% point-point), vertices
+uniform in the unit cube, separations log-uniform in [1e-6, 1e-2], Gaussian
+displacements with sigma = 0.5 x separation, eta = 0.1, offset xi = 1e-7,
+step fraction 1.  Inputs are ~2 GB, larger than L2, so no flush is needed
+between steps.  The headline `value` runs the mixed-precision kernel on
+device-resident inputs; `e2e` runs the same pass through the C ABI with pinned
+host buffers (copies in the timed region).  The FP64 kernel and the barrier
+(energy/gradient/PSD Hessian) pass are reported under "variants".
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl ours|reference]
+
+Multi-GPU: each rank runs its own replica with its own seed (weak scaling, no
+collective on the data path); the timing is the max over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "codim-ipc_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "CCD Mpairs/s"
+ETA, XI, TOC_IN = 0.1, 1e-7, 1.0
+DHAT2, KAPPA = 1e-4, 1.0
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic(name):
+    """DRAM bytes per launch from a committed ncu summary (profiles/<name>.txt), else None."""
+    p = os.path.join(ROOT, "profiles", name + ".txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_launch:"):
+            return float(line.split(":")[1])
+    return None
+
+
+def run_reference(args):
+    """CPU arm: the CPU restatement of the reference's ACCD, all host threads."""
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    import workloads
+    from oracle import oracle_ffi as orc
+    w = workloads.contact_pairs(args.pairs, seed=0)
+    n = w["type"].shape[0]
+    cores = orc.num_threads()
+    for _ in range(args.warmup):
+        orc.ccd_pairs(w["type"][:100000], w["idx"][:100000], w["x"], w["dx"], ETA, XI, TOC_IN)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.ccd_pairs(w["type"], w["idx"], w["x"], w["dx"], ETA, XI, TOC_IN)
+    dt = time.perf_counter() - t0
+    v = n * args.steps / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "Mpairs/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "ACCD time of impact, %d seeded contact pairs (PT/EE/PE/PP 40/40/10/10)" % n,
+                   "pairs": n, "eta": ETA, "xi": XI},
+        "cpu_baseline": {"value": round(v, 3), "unit": "Mpairs/s", "cores": cores, "kind": "port",
+                         "sample": "full %d-pair pass per step" % n},
+        "e2e": {"value": round(v, 3), "unit": "Mpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference (Eigen/CHOLMOD/Kokkos C++) cannot be built on this image; its ACCD is timed "
+                "through the CPU restatement in oracle/ (OpenMP, FP64)",
+    }
+    print(json.dumps(line))
+
+
+def _time_calls(fn, steps, stream):
+    import torch
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for e0, e1 in evs:
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    per = [e0.elapsed_time(e1) for e0, e1 in evs]
+    return start.elapsed_time(stop), per
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import cipc_ffi as F
+    import workloads
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=dev)
+    w = workloads.contact_pairs(args.pairs, seed=rank)
+    n = w["type"].shape[0]
+    d = {k: torch.from_numpy(np.ascontiguousarray(w[k])).to(dev) for k in ("type", "idx", "x", "dx")}
+    toc = torch.empty(n, dtype=torch.float64, device=dev)
+    hit = torch.empty(n, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    prec = F.MIXED if args.precision == "mixed" else F.FP64
+
+    def step(p=prec):
+        F.ccd_pairs_async(d["type"], d["idx"], d["x"], d["dx"], toc, hit, ETA, XI, TOC_IN, p, stream)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    st, ov = F.ccd_pairs(d["type"], d["idx"], d["x"], d["dx"], toc, hit, ETA, XI, TOC_IN, prec, F.MEM_DEVICE, stream)
+    assert ov == 0, "iteration-cap overflow in warm-up"
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    total_ms, per = _time_calls(step, args.steps, stream)
+    clk = clocks.stop()
+    if ws > 1:
+        dist.barrier()
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms = total_ms / args.steps
+    value = n * ws * args.steps / (total_ms / 1e3) / 1e6
+
+    # FP64 variant (same inputs) and barrier passes
+    variants = {}
+    other = F.FP64 if prec == F.MIXED else F.MIXED
+    _, per_o = _time_calls(lambda: step(other), 3, stream)
+    variants["ccd_%s_mpairs_s" % ("fp64" if other == F.FP64 else "mixed")] = round(n / (np.mean(per_o) / 1e3) / 1e6, 2)
+    nb = min(n, args.barrier_pairs)
+    E = torch.empty(nb, dtype=torch.float64, device=dev)
+    G = torch.empty((nb, 12), dtype=torch.float64, device=dev)
+    for bp, htype in ((F.MIXED, torch.float32), (F.FP64, torch.float64)):
+        H = torch.empty((nb, 78), dtype=htype, device=dev)
+        fn = lambda: F.barrier_pairs_async(d["type"][:nb], d["idx"][:nb], d["x"], d["x"], E, G, H, DHAT2, XI, KAPPA,
+                                           True, bp, stream)
+        fn()
+        _, per_b = _time_calls(fn, 2, stream)
+        key = "barrier_psd_%s_mpairs_s" % ("mixed" if bp == F.MIXED else "fp64")
+        variants[key] = round(nb / (np.mean(per_b) / 1e3) / 1e6, 3)
+        del H
+
+    # end to end through the C ABI with pinned host buffers
+    ph = {k: torch.from_numpy(np.ascontiguousarray(w[k])).pin_memory().numpy() for k in ("type", "idx", "x", "dx")}
+    toc_h = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+    hit_h = torch.empty(n, dtype=torch.uint8).pin_memory().numpy()
+    F.ccd_pairs(ph["type"], ph["idx"], ph["x"], ph["dx"], toc_h, hit_h, ETA, XI, TOC_IN, prec, F.MEM_HOST, stream)
+    e2e_steps = max(1, min(args.steps, 3))
+    if ws > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        F.ccd_pairs(ph["type"], ph["idx"], ph["x"], ph["dx"], toc_h, hit_h, ETA, XI, TOC_IN, prec, F.MEM_HOST, stream)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if ws > 1:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = sum(ph[k].nbytes for k in ph)
+    d2h = toc_h.nbytes + hit_h.nbytes + 24
+
+    # roofline of the dominant kernel (k_accd): algorithmic bytes / launch duration
+    ccd_bytes, _ = workloads.pair_bytes(w["type"])
+    launch_s = float(np.mean(per)) / 1e3
+    peak, peak_kind = _peaks()
+    achieved = ccd_bytes / launch_s / 1e9
+    traffic = _traffic("accd_%s_10M_pairs" % args.precision)
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if ws == 1 and not args.no_cpu_baseline:
+            from oracle import oracle_ffi as orc
+            m = min(n, 4_000_000)
+            t0 = time.perf_counter()
+            reps = 0
+            while True:
+                orc.ccd_pairs(w["type"][:m], w["idx"][:m], w["x"], w["dx"], ETA, XI, TOC_IN)
+                reps += 1
+                if time.perf_counter() - t0 > 8.0 or reps >= 10:
+                    break
+            cdt = time.perf_counter() - t0
+            cpu = {"value": round(m * reps / cdt / 1e6, 3), "unit": "Mpairs/s", "cores": orc.num_threads(),
+                   "kind": "port", "sample": "%d x first %d pairs of the same workload" % (reps, m)}
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": "Mpairs/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64" if prec == F.MIXED else "f64", "data": "synthetic",
+            "config": {"workload": "ACCD time of impact, %d seeded contact pairs per GPU (PT/EE/PE/PP 40/40/10/10)"
+                                   % n, "pairs_per_gpu": n, "precision": args.precision, "eta": ETA, "xi": XI,
+                       "l2": "inputs (%.2f GB) larger than L2; no flush" % (ccd_bytes / 1e9)},
+            "e2e": {"value": round(n * ws / e2e_s / 1e6, 2), "unit": "Mpairs/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "kernel": "k_accd<%sPol>" % ("Mixed" if prec == F.MIXED else "Exact"),
+                         "peak_source": peak_kind,
+                         "note": "ACCD is FP64-pipe bound on this part; bytes are the algorithmic minimum"},
+            "clocks": clk,
+            "variants": variants,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--pairs", type=int, default=10_000_000)
+    ap.add_argument("--barrier-pairs", type=int, default=2_000_000)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

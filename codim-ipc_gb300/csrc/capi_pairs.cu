@@ -1,0 +1,253 @@
+// C-ABI entry points for the per-pair contact kernels (include/cipc.h).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/cipc.h"
+#include "ccd_core.cuh"
+#include "cipc_internal.h"
+#include "cipc_util.h"
+
+using namespace cipc;
+
+namespace {
+
+// host-mode staging: copies n*bytes from host to a new device buffer
+template <typename T>
+cudaError_t stage_in(T** dptr, const T* h, size_t count, cudaStream_t s)
+{
+    *dptr = nullptr;
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMallocAsync((void**)dptr, count * sizeof(T), s);
+    if (e != cudaSuccess) return e;
+    if (h) return cudaMemcpyAsync(*dptr, h, count * sizeof(T), cudaMemcpyHostToDevice, s);
+    return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" int cipc_ccd_pairs(int64_t n, const uint8_t* type, const int32_t* idx, int64_t nv, const double* x,
+                              const double* dx, double eta, double thickness, double toc_in, int precision,
+                              int mem, double* toc_out, uint8_t* hit, int64_t* n_overflow, void* stream)
+{
+    if (n < 0 || nv < 0 || (n > 0 && (!type || !idx || !x || !dx || !toc_out || !hit)))
+        return set_error(CIPC_ERR_INVALID_ARG, "cipc_ccd_pairs: null buffer or negative size");
+    if (precision != CIPC_PRECISION_FP64 && precision != CIPC_PRECISION_MIXED)
+        return set_error(CIPC_ERR_INVALID_ARG, "cipc_ccd_pairs: unknown precision");
+    if (mem != CIPC_MEM_HOST && mem != CIPC_MEM_DEVICE)
+        return set_error(CIPC_ERR_INVALID_ARG, "cipc_ccd_pairs: unknown memory kind");
+    if (!(eta > 0 && eta < 1) || !(thickness >= 0) || !(toc_in > 0))
+        return set_error(CIPC_ERR_INVALID_ARG, "cipc_ccd_pairs: need 0 < eta < 1, thickness >= 0, toc_in > 0");
+    if (n_overflow) *n_overflow = 0;
+    if (n == 0) return CIPC_OK;
+    int rc = ensure_device();
+    if (rc != CIPC_OK) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+
+    const uint8_t* d_type = type;
+    const int32_t* d_idx = idx;
+    const double *d_x = x, *d_dx = dx;
+    double* d_toc = toc_out;
+    uint8_t* d_hit = hit;
+    uint8_t *t_type = nullptr, *t_hit = nullptr;
+    int32_t* t_idx = nullptr;
+    double *t_x = nullptr, *t_dx = nullptr, *t_toc = nullptr;
+    unsigned long long* counters = nullptr;
+    cudaError_t e = cudaSuccess;
+#define CK(call)                    \
+    do {                            \
+        e = (call);                 \
+        if (e != cudaSuccess) goto done; \
+    } while (0)
+    if (mem == CIPC_MEM_HOST) {
+        CK(stage_in(&t_type, type, (size_t)n, s));
+        CK(stage_in(&t_idx, idx, (size_t)n * 4, s));
+        CK(stage_in(&t_x, x, (size_t)nv * 3, s));
+        CK(stage_in(&t_dx, dx, (size_t)nv * 3, s));
+        CK(stage_in(&t_toc, (const double*)nullptr, (size_t)n, s));
+        CK(stage_in(&t_hit, (const uint8_t*)nullptr, (size_t)n, s));
+        d_type = t_type;
+        d_idx = t_idx;
+        d_x = t_x;
+        d_dx = t_dx;
+        d_toc = t_toc;
+        d_hit = t_hit;
+    }
+    CK(cudaMallocAsync((void**)&counters, 4 * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), s));
+    {
+        CcdArgs a;
+        a.n = n;
+        a.type = d_type;
+        a.idx = reinterpret_cast<const int4*>(d_idx);
+        a.x = d_x;
+        a.dx = d_dx;
+        a.eta = eta;
+        a.th = thickness;
+        a.toc_in = toc_in;
+        a.max_iter = 1 << 20;
+        a.nv = nv;
+        a.toc_out = d_toc;
+        a.hit = d_hit;
+        a.iters = nullptr;
+        a.counter = counters;
+        const bool exact = precision == CIPC_PRECISION_FP64;
+        const int bps = exact ? accd_exact_blocks_per_sm() : accd_mixed_blocks_per_sm();
+        int grid = num_sms() * bps;
+        const int64_t need = (n + 255) / 256;
+        if (need < grid) grid = (int)need;
+        CK(exact ? launch_accd_exact(a, grid, s) : launch_accd_mixed(a, grid, s));
+    }
+    if (mem == CIPC_MEM_HOST) {
+        CK(cudaMemcpyAsync(toc_out, d_toc, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(hit, d_hit, (size_t)n, cudaMemcpyDeviceToHost, s));
+    }
+    if (n_overflow || mem == CIPC_MEM_HOST) {
+        unsigned long long cnt[3] = {0, 0, 0};
+        CK(cudaMemcpyAsync(cnt, counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (n_overflow) *n_overflow = (int64_t)cnt[1];
+        if (cnt[2])
+            rc = set_error(CIPC_ERR_INDEX_RANGE, "cipc_ccd_pairs: %llu pairs with a bad type or vertex index", cnt[2]);
+        else if (cnt[1])
+            rc = set_error(CIPC_ERR_ITER_CAP, "cipc_ccd_pairs: %llu pairs reached the iteration cap", cnt[1]);
+    }
+done:
+    if (counters) cudaFreeAsync(counters, s);
+    if (t_type) cudaFreeAsync(t_type, s);
+    if (t_idx) cudaFreeAsync(t_idx, s);
+    if (t_x) cudaFreeAsync(t_x, s);
+    if (t_dx) cudaFreeAsync(t_dx, s);
+    if (t_toc) cudaFreeAsync(t_toc, s);
+    if (t_hit) cudaFreeAsync(t_hit, s);
+    if (mem == CIPC_MEM_HOST) cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return set_cuda_error(e, "cipc_ccd_pairs");
+    return rc;
+#undef CK
+}
+
+extern "C" int cipc_barrier_pairs(int64_t n, const uint8_t* type, const int32_t* idx, int64_t nv, const double* x,
+                                  const double* x_rest, double dhat2, double xi, double kappa, int project_pd,
+                                  int precision, int mem, double* energy, double* grad, void* hess,
+                                  int64_t* n_nonpositive, void* stream)
+{
+    if (n < 0 || nv < 0 || (n > 0 && (!type || !idx || !x || !x_rest || !energy || !grad || !hess)))
+        return set_error(CIPC_ERR_INVALID_ARG, "cipc_barrier_pairs: null buffer or negative size");
+    if (precision != CIPC_PRECISION_FP64 && precision != CIPC_PRECISION_MIXED)
+        return set_error(CIPC_ERR_INVALID_ARG, "cipc_barrier_pairs: unknown precision");
+    if (mem != CIPC_MEM_HOST && mem != CIPC_MEM_DEVICE)
+        return set_error(CIPC_ERR_INVALID_ARG, "cipc_barrier_pairs: unknown memory kind");
+    if (!(dhat2 > 0) || !(xi >= 0) || !(kappa > 0))
+        return set_error(CIPC_ERR_INVALID_ARG, "cipc_barrier_pairs: need dhat2 > 0, xi >= 0, kappa > 0");
+    if (n_nonpositive) *n_nonpositive = 0;
+    if (n == 0) return CIPC_OK;
+    int rc = ensure_device();
+    if (rc != CIPC_OK) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t hbytes = (size_t)n * 78 * (precision == CIPC_PRECISION_FP64 ? sizeof(double) : sizeof(float));
+
+    const uint8_t* d_type = type;
+    const int32_t* d_idx = idx;
+    const double *d_x = x, *d_xr = x_rest;
+    double *d_E = energy, *d_g = grad;
+    void* d_h = hess;
+    uint8_t* t_type = nullptr;
+    int32_t* t_idx = nullptr;
+    double *t_x = nullptr, *t_xr = nullptr, *t_E = nullptr, *t_g = nullptr;
+    char* t_h = nullptr;
+    unsigned long long* counters = nullptr;
+    cudaError_t e = cudaSuccess;
+#define CK(call)                    \
+    do {                            \
+        e = (call);                 \
+        if (e != cudaSuccess) goto done; \
+    } while (0)
+    if (mem == CIPC_MEM_HOST) {
+        CK(stage_in(&t_type, type, (size_t)n, s));
+        CK(stage_in(&t_idx, idx, (size_t)n * 4, s));
+        CK(stage_in(&t_x, x, (size_t)nv * 3, s));
+        CK(stage_in(&t_xr, x_rest, (size_t)nv * 3, s));
+        CK(stage_in(&t_E, (const double*)nullptr, (size_t)n, s));
+        CK(stage_in(&t_g, (const double*)nullptr, (size_t)n * 12, s));
+        CK(stage_in(&t_h, (const char*)nullptr, hbytes, s));
+        d_type = t_type;
+        d_idx = t_idx;
+        d_x = t_x;
+        d_xr = t_xr;
+        d_E = t_E;
+        d_g = t_g;
+        d_h = t_h;
+    }
+    CK(cudaMallocAsync((void**)&counters, 4 * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), s));
+    {
+        BarrierLaunch L;
+        L.n = n;
+        L.type = d_type;
+        L.idx = d_idx;
+        L.x = d_x;
+        L.x_rest = d_xr;
+        L.xi2 = xi * xi;
+        L.shat = dhat2 + 2 * std::sqrt(dhat2) * xi;
+        L.kappa = kappa;
+        L.project = project_pd ? 1 : 0;
+        L.fp64_hessian = precision == CIPC_PRECISION_FP64;
+        L.nv = nv;
+        L.E = d_E;
+        L.grad = d_g;
+        L.hess = d_h;
+        L.bad = counters;
+        CK(launch_barrier(L, s));
+    }
+    if (mem == CIPC_MEM_HOST) {
+        CK(cudaMemcpyAsync(energy, d_E, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(grad, d_g, (size_t)n * 12 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(hess, d_h, hbytes, cudaMemcpyDeviceToHost, s));
+    }
+    if (n_nonpositive || mem == CIPC_MEM_HOST) {
+        unsigned long long cnt[2] = {0, 0};
+        CK(cudaMemcpyAsync(cnt, counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (n_nonpositive) *n_nonpositive = (int64_t)cnt[0];
+        if (cnt[1])
+            rc = set_error(CIPC_ERR_INDEX_RANGE, "cipc_barrier_pairs: %llu pairs with a bad type or vertex index",
+                           cnt[1]);
+        else if (cnt[0])
+            rc = set_error(CIPC_ERR_NONPOSITIVE_DISTANCE, "cipc_barrier_pairs: %llu pairs at or below the offset",
+                           cnt[0]);
+    }
+done:
+    if (counters) cudaFreeAsync(counters, s);
+    if (t_type) cudaFreeAsync(t_type, s);
+    if (t_idx) cudaFreeAsync(t_idx, s);
+    if (t_x) cudaFreeAsync(t_x, s);
+    if (t_xr) cudaFreeAsync(t_xr, s);
+    if (t_E) cudaFreeAsync(t_E, s);
+    if (t_g) cudaFreeAsync(t_g, s);
+    if (t_h) cudaFreeAsync(t_h, s);
+    if (mem == CIPC_MEM_HOST) cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return set_cuda_error(e, "cipc_barrier_pairs");
+    return rc;
+#undef CK
+}
+
+extern "C" int cipc_encode_reference_constraint(int type, const int32_t* idx4, int mollified, int multiplicity,
+                                                int32_t* code4)
+{
+    if (!idx4 || !code4 || type < 0 || type > 3 || multiplicity < 1)
+        return set_error(CIPC_ERR_INVALID_ARG, "cipc_encode_reference_constraint: bad argument");
+    const int32_t a = idx4[0], b = idx4[1], c = idx4[2], d = idx4[3];
+    switch (type) {
+        case CIPC_PAIR_PT: code4[0] = -a - 1; code4[1] = b; code4[2] = c; code4[3] = d; break;
+        case CIPC_PAIR_PE: code4[0] = -a - 1; code4[1] = b; code4[2] = c; code4[3] = -multiplicity; break;
+        case CIPC_PAIR_PP: code4[0] = -a - 1; code4[1] = b; code4[2] = -1; code4[3] = -multiplicity; break;
+        default:
+            code4[0] = a;
+            code4[1] = b;
+            code4[2] = mollified ? -c - 1 : c;
+            code4[3] = d;
+    }
+    return CIPC_OK;
+}

@@ -1,0 +1,188 @@
+// Additive CCD (ACCD) over a list of contact pairs, one lane per pair.
+//
+// Restates the reference's Point_Triangle_CCD / Edge_Edge_CCD / Point_Edge_CCD /
+// Point_Point_CCD (Library/Math/Distance/CCD.h:279-483): remove the mean
+// displacement, bound the relative motion by maxDispMag, and advance the time of
+// impact by the conservative step (1-eta)(d^2 - xi^2) / ((d + xi) maxDispMag)
+// until the distance function falls below eta times its initial value (hit) or
+// the accumulated time passes the step fraction (no hit).
+//
+// GPU structure.  The iteration count differs per pair (one to thousands), so a
+// pair-per-thread loop would leave most lanes of a warp idle behind the slowest
+// pair.  Instead every lane runs one flat loop whose body is a single ACCD step:
+// a lane whose pair has finished writes its result and takes the next pair from a
+// global work counter (one atomicAdd per warp, ballot-aggregated).  Lanes stay
+// busy until the list is drained; warps see pairs of one type as long as the list
+// is grouped by type.  The loop is capped (max_iter steps per pair): a pair that
+// reaches the cap is reported as an overflow instead of spinning.
+#pragma once
+#include "geom.cuh"
+
+namespace cipc {
+
+struct CcdArgs {
+    int64_t n;
+    const uint8_t* type;
+    const int4* idx;
+    const double* x;
+    const double* dx;
+    double eta, th, toc_in;
+    int64_t max_iter;
+    int64_t nv;                        // vertex count, for index validation
+    double* toc_out;
+    uint8_t* hit;
+    int32_t* iters;                    // optional
+    unsigned long long* counter;       // [0] work counter, [1] overflow count, [2] invalid pairs
+};
+
+__device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }
+
+// Removes the mean displacement and returns maxDispMag (CCD.h:290-299, 320-329,
+// 395-401, 445-450); v/dv hold (p,t0,t1,t2) / (ea0,ea1,eb0,eb1) / (p,e0,e1) / (p0,p1).
+__device__ __forceinline__ double ccd_prepare(int tp, d3 (&dv)[4])
+{
+    switch (tp) {
+        case kPP: {
+            const d3 mov = scl(dv[0] + dv[1], 0.5);
+            dv[1] = dv[1] - mov;
+            dv[0] = dv[0] - mov;
+            return sqrt(n2(dv[0])) + sqrt(n2(dv[1]));
+        }
+        case kPE: {
+            const d3 mov = dvs((dv[0] + dv[1]) + dv[2], 3.0);
+            dv[1] = dv[1] - mov;
+            dv[2] = dv[2] - mov;
+            dv[0] = dv[0] - mov;
+            return sqrt(n2(dv[0])) + sqrt(dmax(n2(dv[1]), n2(dv[2])));
+        }
+        case kPT: {
+            const d3 mov = scl(((dv[1] + dv[2]) + dv[3]) + dv[0], 0.25);
+            dv[1] = dv[1] - mov;
+            dv[2] = dv[2] - mov;
+            dv[3] = dv[3] - mov;
+            dv[0] = dv[0] - mov;
+            const double m2 = dmax(dmax(n2(dv[1]), n2(dv[2])), n2(dv[3]));
+            return sqrt(n2(dv[0])) + sqrt(m2);
+        }
+        default: {
+            const d3 mov = scl(((dv[0] + dv[1]) + dv[2]) + dv[3], 0.25);
+            dv[0] = dv[0] - mov;
+            dv[1] = dv[1] - mov;
+            dv[2] = dv[2] - mov;
+            dv[3] = dv[3] - mov;
+            return sqrt(dmax(n2(dv[0]), n2(dv[1]))) + sqrt(dmax(n2(dv[2]), n2(dv[3])));
+        }
+    }
+}
+
+template <class Pol>
+__global__ void __launch_bounds__(256) k_accd(CcdArgs a)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const double th = a.th, th2 = a.th * a.th, eta = a.eta, toc_prev = a.toc_in;
+    int64_t pid = -1;
+    bool exhausted = false;
+    int tp = 0, phase = 0;
+    d3 v[4], dv[4];
+    double maxDisp = 0, gap = 0, t = 0, tlb = 0;
+    int64_t adv = 0;
+    while (true) {
+        const bool need = (pid < 0) && !exhausted;
+        const unsigned m = __ballot_sync(FULL, need);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(a.counter, (unsigned long long)__popc(m));
+            base = __shfl_sync(FULL, base, leader);
+            if (need) {
+                const unsigned long long my = base + __popc(m & ((1u << lane) - 1u));
+                if (my < (unsigned long long)a.n) {
+                    pid = (int64_t)my;
+                    phase = 0;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        const bool active = pid >= 0;
+        if (!__any_sync(FULL, active)) break;
+        if (!active) continue;
+        if (phase == 0) {
+            tp = a.type[pid];
+            const int4 id = a.idx[pid];
+            const int nv = tp == kPP ? 2 : (tp == kPE ? 3 : 4);
+            const int ids[4] = {id.x, id.y, id.z, id.w};
+            bool ok = tp <= kEE;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (k < nv) ok = ok && ids[k] >= 0 && ids[k] < a.nv;
+            if (!ok) {  // invalid pair: reported, never dereferenced
+                a.toc_out[pid] = toc_prev;
+                a.hit[pid] = 0;
+                if (a.iters) a.iters[pid] = 0;
+                atomicAdd(a.counter + 2, 1ull);
+                pid = -1;
+                continue;
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (k < nv) {
+                    v[k] = ld(a.x, ids[k]);
+                    dv[k] = ld(a.dx, ids[k]);
+                } else {
+                    v[k] = mk(0, 0, 0);
+                    dv[k] = mk(0, 0, 0);
+                }
+            }
+            maxDisp = ccd_prepare(tp, dv);
+            adv = 0;
+            if (maxDisp == 0) {
+                a.toc_out[pid] = toc_prev;
+                a.hit[pid] = 0;
+                if (a.iters) a.iters[pid] = 0;
+                pid = -1;
+                continue;
+            }
+        }
+        double d2;
+        const double f = Pol::dfunc(tp, v, th2, d2);
+        const double dist = Pol::sqrt_(d2);
+        if (phase == 0) {
+            gap = eta * f / (dist + th);
+            t = 0;
+            phase = 1;
+        } else {
+            if (t != 0 && (f / (dist + th) < gap)) {
+                a.toc_out[pid] = t;
+                a.hit[pid] = 1;
+                if (a.iters) a.iters[pid] = (int32_t)adv;
+                pid = -1;
+                continue;
+            }
+            t += tlb;
+            if (t > toc_prev) {
+                a.toc_out[pid] = toc_prev;
+                a.hit[pid] = 0;
+                if (a.iters) a.iters[pid] = (int32_t)adv;
+                pid = -1;
+                continue;
+            }
+        }
+        if (adv >= a.max_iter) {
+            a.toc_out[pid] = toc_prev;
+            a.hit[pid] = 0;
+            if (a.iters) a.iters[pid] = (int32_t)adv;
+            atomicAdd(a.counter + 1, 1ull);
+            pid = -1;
+            continue;
+        }
+        tlb = Pol::div_((1 - eta) * f, (dist + th) * maxDisp);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] = axpy(tlb, dv[k], v[k]);
+        ++adv;
+    }
+}
+
+}  // namespace cipc

@@ -1,0 +1,111 @@
+/*
+ * cipc.h — C ABI of the GB300 contact + Newton hot path for codimensional IPC.
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (CIPC_OK = 0).  Buffers are host memory when `mem` is CIPC_MEM_HOST (the call
+ * copies them to the GPU, runs, copies results back and waits) or device memory
+ * when `mem` is CIPC_MEM_DEVICE (the call only enqueues work on `stream`; scalar
+ * out-parameters such as counts are host pointers and, when non-NULL, make the
+ * call wait for the stream).  `stream` is a cudaStream_t or NULL for the legacy
+ * default stream.  A status other than CIPC_OK leaves a message for
+ * cipc_last_error() on the calling thread.
+ *
+ * Pair encoding.  A contact pair is type[i] in {0 PP, 1 PE, 2 PT, 3 EE} and four
+ * vertex indices idx[4*i .. 4*i+3]:
+ *   PP (p0, p1, -, -)   PE (p, e0, e1, -)   PT (p, t0, t1, t2)   EE (ea0, ea1, eb0, eb1)
+ * Unused slots are ignored.  Positions are n_verts x 3 doubles.  The reference
+ * packs the same four cases into sign-encoded Vector4i constraint codes
+ * (Library/FEM/IPC.h:571-661); cipc_encode_reference_constraint converts.
+ */
+#ifndef CIPC_H
+#define CIPC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CIPC_OK 0
+#define CIPC_ERR_INVALID_ARG 1
+#define CIPC_ERR_CUDA 2
+#define CIPC_ERR_ITER_CAP 3
+#define CIPC_ERR_NONPOSITIVE_DISTANCE 4
+#define CIPC_ERR_NOT_CONVERGED 5
+#define CIPC_ERR_NAN 6
+#define CIPC_ERR_NO_DEVICE 7
+#define CIPC_ERR_INDEX_RANGE 8
+
+#define CIPC_PRECISION_FP64 0  /* all-FP64, decisions bit-exact with the CPU restatement */
+#define CIPC_PRECISION_MIXED 1 /* FP32 classification / Hessians, FP64 distances and times */
+
+#define CIPC_MEM_HOST 0
+#define CIPC_MEM_DEVICE 1
+
+#define CIPC_PAIR_PP 0
+#define CIPC_PAIR_PE 1
+#define CIPC_PAIR_PT 2
+#define CIPC_PAIR_EE 3
+
+/* Library identification and error reporting. */
+const char* cipc_version(void);
+const char* cipc_last_error(void);
+const char* cipc_status_string(int status);
+int cipc_device_count(void);
+
+/*
+ * Additive CCD over candidate pairs.
+ *
+ * Replaces the narrow-phase calls Point_Triangle_CCD / Edge_Edge_CCD /
+ * Point_Edge_CCD / Point_Point_CCD (Library/Math/Distance/CCD.h:279-483) that
+ * Compute_Intersection_Free_StepSize makes per candidate
+ * (Library/FEM/IPC.h:1959-2242).  dx is the full displacement, toc_in the step
+ * fraction the reference passes as `toc` (its largest allowed step).
+ * Outputs per pair: hit[i] = 1 when a time of impact below toc_in exists, and
+ * toc_out[i] = that conservative time (eta-scaled, thickness-offset), else toc_in.
+ * *n_overflow (optional) receives the number of pairs that reached the
+ * iteration cap (2^20 steps) — they are reported as no hit; with any overflow the
+ * call returns CIPC_ERR_ITER_CAP.  Pairs with an index outside [0, n_verts) or a
+ * type above 3 are not evaluated and make the call return CIPC_ERR_INDEX_RANGE.
+ */
+int cipc_ccd_pairs(int64_t n_pairs, const uint8_t* type, const int32_t* idx, int64_t n_verts,
+                   const double* x, const double* dx, double eta, double thickness, double toc_in,
+                   int precision, int mem, double* toc_out, uint8_t* hit, int64_t* n_overflow,
+                   void* stream);
+
+/*
+ * Barrier energy, gradient and PSD-projected Hessian per contact pair.
+ *
+ * Replaces the per-constraint bodies of Compute_Barrier, Compute_Barrier_Gradient
+ * and Compute_Barrier_Hessian (Library/FEM/IPC.h:742-1731) for weight 1 and
+ * multiplicity 1, using the thickness-offset barrier of IPC.h:756-757 and
+ * Library/Math/BARRIER.h:9-62: s = d^2 - xi^2, shat = dhat2 + 2 sqrt(dhat2) xi,
+ * b(s) = -kappa (s - shat)^2 ln(s / shat).  EE pairs take the mollified form when
+ * |ea x eb|^2 < 1e-3 |ea_rest|^2 |eb_rest|^2 (EDGE_EDGE_MOLLIFIER.h:582-591).
+ * Outputs: energy[i]; grad[12*i + k] (first 3*nv used, rest zero); hess[78*i + k] =
+ * upper triangle of the (3nv x 3nv) Hessian packed row by row (first
+ * 3nv(3nv+1)/2 used), doubles for CIPC_PRECISION_FP64 and floats for
+ * CIPC_PRECISION_MIXED.  Pairs with s >= shat are inactive (all zeros).  Pairs
+ * with s <= 0 are counted in *n_nonpositive (optional) and make the call return
+ * CIPC_ERR_NONPOSITIVE_DISTANCE (the reference exits there, IPC.h:773-776).
+ */
+int cipc_barrier_pairs(int64_t n_pairs, const uint8_t* type, const int32_t* idx, int64_t n_verts,
+                       const double* x, const double* x_rest, double dhat2, double xi, double kappa,
+                       int project_pd, int precision, int mem, double* energy, double* grad, void* hess,
+                       int64_t* n_nonpositive, void* stream);
+
+/*
+ * Converts one pair to the reference's sign-encoded constraint code
+ * (Library/FEM/IPC.h:571-661 for the 3D merge, :776-930 for decoding):
+ *   PT (-p-1, t0, t1, t2)  PE (-p-1, e0, e1, -mult)  PP (-p0-1, p1, -1, -mult)
+ *   EE (ea0, ea1, eb0, eb1);  mollified EE (ea0, ea1, -eb0-1, eb1).
+ * mult is the PE/PP multiplicity (1 when not merged).  Returns CIPC_OK.
+ */
+int cipc_encode_reference_constraint(int type, const int32_t* idx4, int mollified, int multiplicity,
+                                     int32_t* code4);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CIPC_H */

@@ -1,0 +1,68 @@
+"""Generates tests/golden/reference_derivs.npz from the reference's own code.
+
+The reference's symbolic-toolbox derivative routines (g_PT/H_PT, g_EE/H_EE,
+g_PE3D/H_PE3D, g_EECN2/H_EECN2) and its barrier functions are compiled from the
+Codim-IPC sources by ``oracle/build.py:build_ref`` into
+``oracle/_ref/libcipc_ref.so``; this script evaluates them on seeded inputs and
+stores inputs and outputs, so that the oracle and the CUDA kernels can be
+checked against the reference on machines without its sources.
+
+Inputs: 48 random vertex sets per kind (standard normal coordinates) plus the
+fixed vertex set of the reference's derivTest_EECross / derivTest_e
+(EDGE_EDGE_MOLLIFIER.h:384-438), and barrier arguments spanning 1e-12..1.
+Run:  python tests/golden/make_golden.py
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+from oracle import build as ob  # noqa: E402
+
+
+def main():
+    path = ob.build_ref()
+    if path is None:
+        raise SystemExit("reference sources not available")
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    for n in ("ref_g_PT", "ref_H_PT", "ref_g_EE", "ref_H_EE", "ref_g_PE3D", "ref_H_PE3D", "ref_g_EECN2",
+              "ref_H_EECN2"):
+        getattr(L, n).argtypes = [P, P]
+    L.ref_barrier.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, P]
+    rng = np.random.default_rng(20210801)
+    fixed = np.array([0.0, 0.0, 0.0, 1.0, 0.1, 0.0, 0.0, 1.1, -0.1, 0.0, 0.1, -1.1])
+    out = {}
+    for kind, n in (("PT", 12), ("EE", 12), ("PE3D", 9), ("EECN2", 12)):
+        X = np.vstack([fixed[None, :], rng.standard_normal((48, 12))])
+        G = np.zeros((X.shape[0], n))
+        H = np.zeros((X.shape[0], n, n))
+        for i, x in enumerate(X):
+            xx = np.ascontiguousarray(x)
+            g = np.zeros(12)
+            h = np.zeros(144)
+            getattr(L, "ref_g_" + kind)(xx.ctypes.data, g.ctypes.data)
+            getattr(L, "ref_H_" + kind)(xx.ctypes.data, h.ctypes.data)
+            G[i] = g[:n]
+            H[i] = h[:n * n].reshape(n, n)
+        out["x_" + kind] = X[:, :n].copy()
+        out["g_" + kind] = G
+        out["H_" + kind] = H
+    args = []
+    for d in 10.0 ** rng.uniform(-12, 0, 64):
+        dhat = d * rng.uniform(1.01, 100.0)
+        kappa = 10.0 ** rng.uniform(-2, 11)
+        o = np.zeros(3)
+        L.ref_barrier(d, dhat, kappa, o.ctypes.data)
+        args.append([d, dhat, kappa, o[0], o[1], o[2]])
+    out["barrier"] = np.array(args)
+    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_derivs.npz")
+    np.savez_compressed(dst, **out)
+    print("wrote", dst, os.path.getsize(dst), "bytes")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,61 @@
+"""The C-ABI library loads and exports every entry point declared in include/cipc.h."""
+import ctypes
+import os
+import re
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = []
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", h)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names += re.findall(r"\b(cipc_\w+)\s*\(", src)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    import build_lib
+    import cipc_ffi
+    build_lib.build()
+    L = ctypes.CDLL(cipc_ffi.LIB_PATH)
+    declared = _declared()
+    assert len(declared) >= 6
+    for name in declared:
+        assert hasattr(L, name), name
+    # the Python binding declares a signature for every entry point
+    assert set(declared) <= set(cipc_ffi.exported_symbols())
+
+
+def test_host_only_entry_points():
+    import cipc_ffi
+    assert cipc_ffi.lib().cipc_version().startswith(b"cipc-gb300")
+    assert cipc_ffi.lib().cipc_status_string(0) == b"ok"
+    # reference constraint codes (IPC.h:571-661)
+    assert list(cipc_ffi.encode_reference_constraint(2, [5, 1, 2, 3])) == [-6, 1, 2, 3]
+    assert list(cipc_ffi.encode_reference_constraint(1, [5, 1, 2, -1], multiplicity=2)) == [-6, 1, 2, -2]
+    assert list(cipc_ffi.encode_reference_constraint(0, [5, 1, -1, -1])) == [-6, 1, -1, -1]
+    assert list(cipc_ffi.encode_reference_constraint(3, [5, 1, 2, 3], mollified=True)) == [5, 1, -3, 3]
+
+
+def test_argument_validation_without_gpu():
+    import cipc_ffi
+    t = np.zeros(1, np.uint8)
+    idx = np.zeros((1, 4), np.int32)
+    x = np.zeros((2, 3))
+    toc = np.zeros(1)
+    hit = np.zeros(1, np.uint8)
+    # invalid eta is rejected before any device work
+    try:
+        cipc_ffi.ccd_pairs(t, idx, x, x, toc, hit, eta=1.5)
+        raise AssertionError("expected an error")
+    except cipc_ffi.CipcError as e:
+        assert e.status == cipc_ffi.CIPC_ERR_INVALID_ARG
+    # empty input is a no-op
+    e0 = np.zeros(0, np.uint8)
+    st, ov = cipc_ffi.ccd_pairs(e0, np.zeros((0, 4), np.int32), x, x, np.zeros(0), np.zeros(0, np.uint8))
+    assert st == 0 and ov == 0
