@@ -206,12 +206,22 @@ def run_ours(args):
 
     # FP64 variant (same inputs) and barrier passes
     variants = {}
+    step()
+    torch.cuda.synchronize()
+    toc_a, hit_a = toc.cpu().numpy(), hit.cpu().numpy()
     other = F.FP64 if prec == F.MIXED else F.MIXED
     _, per_o = _time_calls(lambda: step(other), 3, stream)
     variants["ccd_%s_mpairs_s" % ("fp64" if other == F.FP64 else "mixed")] = round(n / (np.mean(per_o) / 1e3) / 1e6, 2)
+    toc_b, hit_b = toc.cpu().numpy(), hit.cpu().numpy()
+    both = (hit_a == 1) & (hit_b == 1)
+    rel = np.abs(toc_a[both] - toc_b[both]) / toc_b[both] if both.any() else np.zeros(1)
+    variants["ccd_mixed_vs_fp64"] = {"hit_mismatch_frac": float((hit_a != hit_b).mean()),
+                                     "toc_rel_err_p999": float(np.quantile(rel, 0.999)),
+                                     "toc_rel_err_max": float(rel.max()), "hit_frac": float(hit_b.mean())}
     nb = min(n, args.barrier_pairs)
     E = torch.empty(nb, dtype=torch.float64, device=dev)
     G = torch.empty((nb, 12), dtype=torch.float64, device=dev)
+    outs = {}
     for bp, htype in ((F.MIXED, torch.float32), (F.FP64, torch.float64)):
         H = torch.empty((nb, 78), dtype=htype, device=dev)
         fn = lambda: F.barrier_pairs_async(d["type"][:nb], d["idx"][:nb], d["x"], d["x"], E, G, H, DHAT2, XI, KAPPA,
@@ -220,7 +230,17 @@ def run_ours(args):
         _, per_b = _time_calls(fn, 2, stream)
         key = "barrier_psd_%s_mpairs_s" % ("mixed" if bp == F.MIXED else "fp64")
         variants[key] = round(nb / (np.mean(per_b) / 1e3) / 1e6, 3)
+        outs[bp] = (E.cpu().numpy(), G.cpu().numpy(), H.double().cpu().numpy())
         del H
+    (Em, Gm, Hm), (Ed, Gd, Hd) = outs[F.MIXED], outs[F.FP64]
+    hs = np.maximum(np.abs(Hd).max(1), 1e-300)
+    gs = np.maximum(np.abs(Gd).max(1), 1e-300)
+    variants["barrier_mixed_vs_fp64"] = {
+        "energy_rel_err_max": float((np.abs(Em - Ed) / np.maximum(np.abs(Ed), 1e-300)).max()),
+        "grad_rel_err_max": float((np.abs(Gm - Gd).max(1) / gs).max()),
+        "hess_rel_err_p999": float(np.quantile(np.abs(Hm - Hd).max(1) / hs, 0.999)),
+        "hess_rel_err_max": float((np.abs(Hm - Hd).max(1) / hs).max()),
+        "note": "errors per pair relative to the pair's largest FP64 entry"}
 
     # end to end through the C ABI with pinned host buffers
     ph = {k: torch.from_numpy(np.ascontiguousarray(w[k])).pin_memory().numpy() for k in ("type", "idx", "x", "dx")}

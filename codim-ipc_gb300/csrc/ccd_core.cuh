@@ -35,12 +35,12 @@ struct CcdArgs {
     unsigned long long* counter;       // [0] work counter, [1] overflow count, [2] invalid pairs
 };
 
-__device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }
-__device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }
+CIPC_HD double dmax(double a, double b) { return (a < b) ? b : a; }
+CIPC_HD double dmin(double a, double b) { return (b < a) ? b : a; }
 
 // Removes the mean displacement and returns maxDispMag (CCD.h:290-299, 320-329,
 // 395-401, 445-450); v/dv hold (p,t0,t1,t2) / (ea0,ea1,eb0,eb1) / (p,e0,e1) / (p0,p1).
-__device__ __forceinline__ double ccd_prepare(int tp, d3 (&dv)[4])
+CIPC_HD double ccd_prepare(int tp, d3 (&dv)[4])
 {
     switch (tp) {
         case kPP: {

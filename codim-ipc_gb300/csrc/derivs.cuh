@@ -22,27 +22,27 @@ struct t3 {
     T x, y, z;
 };
 template <typename T>
-__device__ __forceinline__ t3<T> tv(d3 v)
+CIPC_HD t3<T> tv(d3 v)
 {
     return t3<T>{(T)v.x, (T)v.y, (T)v.z};
 }
 template <typename T>
-__device__ __forceinline__ T tdot(t3<T> a, t3<T> b)
+CIPC_HD T tdot(t3<T> a, t3<T> b)
 {
     return a.x * b.x + a.y * b.y + a.z * b.z;
 }
 template <typename T>
-__device__ __forceinline__ t3<T> tcross(t3<T> a, t3<T> b)
+CIPC_HD t3<T> tcross(t3<T> a, t3<T> b)
 {
     return t3<T>{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 template <typename T>
-__device__ __forceinline__ t3<T> tsub(t3<T> a, t3<T> b)
+CIPC_HD t3<T> tsub(t3<T> a, t3<T> b)
 {
     return t3<T>{a.x - b.x, a.y - b.y, a.z - b.z};
 }
 template <typename T>
-__device__ __forceinline__ T comp(t3<T> a, int i)
+CIPC_HD T comp(t3<T> a, int i)
 {
     return i == 0 ? a.x : (i == 1 ? a.y : a.z);
 }
@@ -50,7 +50,7 @@ __device__ __forceinline__ T comp(t3<T> a, int i)
 // H[3bi+i][3bj+j] += s * B_ij (and the mirrored block when bi != bj), where
 // B = [v]x (kind 0), |v|^2 I - v v^T (kind 1), u v^T - (u.v) I (kind 2)
 template <typename T, int N>
-__device__ __forceinline__ void add_skew(T (&H)[N][N], int bi, int bj, t3<T> v, T s)
+CIPC_HD void add_skew(T (&H)[N][N], int bi, int bj, t3<T> v, T s)
 {
     // [v]x = [[0,-vz,vy],[vz,0,-vx],[-vy,vx,0]]
     const T B[3][3] = {{0, -v.z, v.y}, {v.z, 0, -v.x}, {-v.y, v.x, 0}};
@@ -64,11 +64,11 @@ __device__ __forceinline__ void add_skew(T (&H)[N][N], int bi, int bj, t3<T> v, 
 }
 
 // Gradient / Hessian of |e1 x e2|^2 into variable blocks k1, k2.
+// n = e1 x e2 is passed in: it is computed in FP64 by the caller because it
+// cancels for nearly parallel e1, e2.
 template <typename T, int N>
-__device__ __forceinline__ void crossn2_add(t3<T> e1, t3<T> e2, int k1, int k2, T s, T (&g)[N],
-                                            T (&H)[N][N])
+CIPC_HD void crossn2_add(t3<T> e1, t3<T> e2, t3<T> n, int k1, int k2, T s, T (&g)[N], T (&H)[N][N])
 {
-    const t3<T> n = tcross(e1, e2);
     const t3<T> g1 = tcross(e2, n), g2 = tcross(n, e1);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -91,13 +91,13 @@ __device__ __forceinline__ void crossn2_add(t3<T> e1, t3<T> e2, int k1, int k2, 
     add_skew<T, N>(H, k1, k2, n, T(-2) * s);
 }
 
-// f = u^2/w (PT, EE): reduced gradient and Hessian over (a, e1, e2).
+// f = u^2/w (PT, EE): reduced gradient and Hessian over (a, e1, e2).  n = e1 x e2
+// and r = u / w are passed in from FP64: u = a.n cancels when the separation is
+// small against the primitive size.
 template <typename T>
-__device__ __forceinline__ void u2w_derivs(t3<T> a, t3<T> e1, t3<T> e2, T (&g)[9], T (&H)[9][9])
+CIPC_HD void u2w_derivs(t3<T> a, t3<T> e1, t3<T> e2, t3<T> n, T r, T (&g)[9], T (&H)[9][9])
 {
-    const t3<T> n = tcross(e1, e2);
-    const T u = tdot(a, n), w = tdot(n, n);
-    const T r = u / w;
+    const T w = tdot(n, n);
     T gu[9], gw[9];
     T Hw[9][9];
     const t3<T> t1 = tcross(e2, a), t2 = tcross(a, e1);
@@ -120,7 +120,7 @@ __device__ __forceinline__ void u2w_derivs(t3<T> a, t3<T> e1, t3<T> e2, T (&g)[9
     add_skew<T, 9>(H, 0, 1, e2, T(-2) * r);
     add_skew<T, 9>(H, 0, 2, e1, T(2) * r);
     add_skew<T, 9>(H, 1, 2, a, T(-2) * r);
-    crossn2_add<T, 9>(e1, e2, 1, 2, T(1), gw, Hw);
+    crossn2_add<T, 9>(e1, e2, n, 1, 2, T(1), gw, Hw);
     const T c2w = T(2) / w, r2 = r * r;
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
@@ -134,26 +134,44 @@ __device__ __forceinline__ void u2w_derivs(t3<T> a, t3<T> e1, t3<T> e2, T (&g)[9
     }
 }
 
-// gradient only of u^2/w (used in FP64 for the Newton residual)
-template <typename T>
-__device__ __forceinline__ void u2w_grad(t3<T> a, t3<T> e1, t3<T> e2, T (&g)[9])
+// gradient only of u^2/w, FP64 (the Newton residual); u uses the same
+// fma-chain dot product as the squared distance itself
+CIPC_HD void u2w_grad(d3 a, d3 e1, d3 e2, double (&g)[9])
 {
-    const t3<T> n = tcross(e1, e2);
-    const T u = tdot(a, n), w = tdot(n, n);
+    using T = double;
+    const d3 n = cross(e1, e2);
+    const T u = dot(a, n), w = dot(n, n);
     const T r = u / w;
-    const t3<T> t1 = tcross(e2, a), t2 = tcross(a, e1);
-    const t3<T> w1 = tcross(e2, n), w2 = tcross(n, e1);
+    const d3 t1 = cross(e2, a), t2 = cross(a, e1);
+    const d3 w1 = cross(e2, n), w2 = cross(n, e1);
+    const double nn[3] = {n.x, n.y, n.z}, a1[3] = {t1.x, t1.y, t1.z}, a2[3] = {t2.x, t2.y, t2.z};
+    const double b1[3] = {w1.x, w1.y, w1.z}, b2[3] = {w2.x, w2.y, w2.z};
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        g[i] = r * (T(2) * comp(n, i));
-        g[3 + i] = r * (T(2) * comp(t1, i) - r * T(2) * comp(w1, i));
-        g[6 + i] = r * (T(2) * comp(t2, i) - r * T(2) * comp(w2, i));
+        g[i] = r * (T(2) * nn[i]);
+        g[3 + i] = r * (T(2) * a1[i] - r * T(2) * b1[i]);
+        g[6 + i] = r * (T(2) * a2[i] - r * T(2) * b2[i]);
     }
 }
 
-// f = |a x b|^2 / |b - a|^2 (PE) over (a, b)
+// gradient only of |a x b|^2 / |b - a|^2 (PE), FP64
+CIPC_HD void pe_grad(d3 a, d3 b, double (&g)[6])
+{
+    const d3 n = cross(a, b);
+    const d3 g1 = cross(b, n), g2 = cross(n, a);
+    const d3 ba = b - a;
+    const double N = dot(n, n), D = dot(ba, ba);
+    const double f = N / D;
+    const double gN[6] = {2 * g1.x, 2 * g1.y, 2 * g1.z, 2 * g2.x, 2 * g2.y, 2 * g2.z};
+    const double gD[6] = {-2 * ba.x, -2 * ba.y, -2 * ba.z, 2 * ba.x, 2 * ba.y, 2 * ba.z};
+#pragma unroll
+    for (int i = 0; i < 6; ++i) g[i] = (gN[i] - f * gD[i]) / D;
+}
+
+// f = |a x b|^2 / |b - a|^2 (PE) over (a, b); n = a x b and f come from FP64
+// (a x b cancels for a point close to the line).
 template <typename T>
-__device__ __forceinline__ void pe_derivs(t3<T> a, t3<T> b, T (&g)[6], T (&H)[6][6], bool want_h)
+CIPC_HD void pe_derivs(t3<T> a, t3<T> b, t3<T> n, T f, T (&g)[6], T (&H)[6][6])
 {
     T gN[6] = {0, 0, 0, 0, 0, 0};
     T HN[6][6];
@@ -161,11 +179,10 @@ __device__ __forceinline__ void pe_derivs(t3<T> a, t3<T> b, T (&g)[6], T (&H)[6]
     for (int i = 0; i < 6; ++i)
 #pragma unroll
         for (int j = 0; j < 6; ++j) HN[i][j] = 0;
-    crossn2_add<T, 6>(a, b, 0, 1, T(1), gN, HN);
+    crossn2_add<T, 6>(a, b, n, 0, 1, T(1), gN, HN);
     const t3<T> ba = tsub(b, a);
-    const t3<T> c = tcross(a, b);
-    const T N = tdot(c, c), D = tdot(ba, ba);
-    const T f = N / D, iD = T(1) / D;
+    const T D = tdot(ba, ba);
+    const T iD = T(1) / D;
     T gD[6];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -174,7 +191,6 @@ __device__ __forceinline__ void pe_derivs(t3<T> a, t3<T> b, T (&g)[6], T (&H)[6]
     }
 #pragma unroll
     for (int i = 0; i < 6; ++i) g[i] = (gN[i] - f * gD[i]) * iD;
-    if (!want_h) return;
 #pragma unroll
     for (int i = 0; i < 6; ++i)
 #pragma unroll
@@ -190,7 +206,7 @@ __device__ __forceinline__ void pe_derivs(t3<T> a, t3<T> b, T (&g)[6], T (&H)[6]
 // and left unchanged otherwise (the reference's makePD early return).
 // ---------------------------------------------------------------------------
 template <typename T, int N>
-__device__ __forceinline__ void jacobi_psd(T (&A)[N][N])
+CIPC_HD void jacobi_psd(T (&A)[N][N])
 {
     T scale = 0;
 #pragma unroll
@@ -279,7 +295,7 @@ __device__ __forceinline__ void jacobi_psd(T (&A)[N][N])
 // Log barrier b(s) = -kappa (s - shat)^2 ln(s / shat) and its first two
 // derivatives (Math/BARRIER.h:9-62, non-elastic branch).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void barrier3(double d, double dHat, double kappa, double& b, double& g, double& h)
+CIPC_HD void barrier3(double d, double dHat, double kappa, double& b, double& g, double& h)
 {
     const double t2 = d - dHat;
     const double lg = log(d / dHat);

@@ -8,7 +8,12 @@
 // include this header for exact FP64 kernels are compiled with -fmad=false so the
 // compiler adds no contractions of its own.
 #pragma once
+#include <cmath>
 #include <cstdint>
+
+#ifndef CIPC_HD
+#define CIPC_HD __host__ __device__ __forceinline__
+#endif
 
 namespace cipc {
 
@@ -16,30 +21,34 @@ struct d3 {
     double x, y, z;
 };
 
-__device__ __forceinline__ d3 mk(double a, double b, double c) { return d3{a, b, c}; }
-__device__ __forceinline__ d3 operator-(d3 a, d3 b) { return d3{a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ d3 operator+(d3 a, d3 b) { return d3{a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ d3 scl(d3 a, double s) { return d3{a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ d3 dvs(d3 a, double s) { return d3{a.x / s, a.y / s, a.z / s}; }
-__device__ __forceinline__ double dot(d3 a, d3 b) { return fma(a.z, b.z, fma(a.y, b.y, a.x * b.x)); }
-__device__ __forceinline__ double n2(d3 a) { return dot(a, a); }
-__device__ __forceinline__ d3 cross(d3 a, d3 b)
+CIPC_HD d3 mk(double a, double b, double c) { return d3{a, b, c}; }
+CIPC_HD d3 operator-(d3 a, d3 b) { return d3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+CIPC_HD d3 operator+(d3 a, d3 b) { return d3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+CIPC_HD d3 scl(d3 a, double s) { return d3{a.x * s, a.y * s, a.z * s}; }
+CIPC_HD d3 dvs(d3 a, double s) { return d3{a.x / s, a.y / s, a.z / s}; }
+CIPC_HD double dot(d3 a, d3 b) { return fma(a.z, b.z, fma(a.y, b.y, a.x * b.x)); }
+CIPC_HD double n2(d3 a) { return dot(a, a); }
+CIPC_HD d3 cross(d3 a, d3 b)
 {
     return d3{fma(a.y, b.z, -(a.z * b.y)), fma(a.z, b.x, -(a.x * b.z)), fma(a.x, b.y, -(a.y * b.x))};
 }
-__device__ __forceinline__ d3 axpy(double t, d3 d, d3 x)
+CIPC_HD d3 axpy(double t, d3 d, d3 x)
 {
     return d3{fma(t, d.x, x.x), fma(t, d.y, x.y), fma(t, d.z, x.z)};
 }
-__device__ __forceinline__ d3 ld(const double* __restrict__ p, int64_t i)
+CIPC_HD d3 ld(const double* __restrict__ p, int64_t i)
 {
+#ifdef __CUDA_ARCH__
     return d3{__ldg(p + 3 * i), __ldg(p + 3 * i + 1), __ldg(p + 3 * i + 2)};
+#else
+    return d3{p[3 * i], p[3 * i + 1], p[3 * i + 2]};
+#endif
 }
 
 // Eigen-style pivoted LDL^T solve of a symmetric 2x2 system; the pivot is the
 // larger |diagonal| (first on ties), zero pivots give zero, |D| <= DBL_MIN entries
 // are pseudo-inverted to zero.
-__device__ __forceinline__ void ldlt2(double a00, double a10, double a11, double b0, double b1,
+CIPC_HD void ldlt2(double a00, double a10, double a11, double b0, double b1,
                                       double& y0, double& y1)
 {
     const bool sw = fabs(a11) > fabs(a00);
@@ -71,14 +80,14 @@ __device__ __forceinline__ void ldlt2(double a00, double a10, double a11, double
     }
 }
 
-__device__ __forceinline__ void pt_param(d3 r0, d3 n, d3 v, double& s, double& q)
+CIPC_HD void pt_param(d3 r0, d3 n, d3 v, double& s, double& q)
 {
     const d3 r1 = cross(r0, n);
     ldlt2(dot(r0, r0), dot(r1, r0), dot(r1, r1), dot(r0, v), dot(r1, v), s, q);
 }
 
 // Point-triangle distance type: 0-2 PP(t0,t1,t2), 3-5 PE(t0t1,t1t2,t2t0), 6 PT.
-__device__ __forceinline__ int pt_type(d3 p, d3 t0, d3 t1, d3 t2)
+CIPC_HD int pt_type(d3 p, d3 t0, d3 t1, d3 t2)
 {
     const d3 n = cross(t1 - t0, t2 - t0);
     double s0, q0, s1, q1, s2, q2;
@@ -96,7 +105,7 @@ __device__ __forceinline__ int pt_type(d3 p, d3 t0, d3 t1, d3 t2)
 
 // Edge-edge distance type: 0 PP(a0,b0) 1 PP(a0,b1) 2 PE(a0,b) 3 PP(a1,b0) 4 PP(a1,b1)
 // 5 PE(a1,b) 6 PE(b0,a) 7 PE(b1,a) 8 EE; nearly parallel pairs fall back to PE.
-__device__ __forceinline__ int ee_type(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
+CIPC_HD int ee_type(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
 {
     const d3 u = ea1 - ea0, v = eb1 - eb0, w = ea0 - eb0;
     const double a = dot(u, u), b = dot(u, v), c = dot(v, v), d = dot(u, w), e = dot(v, w);
@@ -141,26 +150,26 @@ __device__ __forceinline__ int ee_type(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
     return dc;
 }
 
-__device__ __forceinline__ double pp_d2(d3 a, d3 b) { return n2(a - b); }
-__device__ __forceinline__ double pe_d2(d3 p, d3 e0, d3 e1) { return n2(cross(e0 - p, e1 - p)) / n2(e1 - e0); }
-__device__ __forceinline__ double pt_d2(d3 p, d3 t0, d3 t1, d3 t2)
+CIPC_HD double pp_d2(d3 a, d3 b) { return n2(a - b); }
+CIPC_HD double pe_d2(d3 p, d3 e0, d3 e1) { return n2(cross(e0 - p, e1 - p)) / n2(e1 - e0); }
+CIPC_HD double pt_d2(d3 p, d3 t0, d3 t1, d3 t2)
 {
     const d3 b = cross(t1 - t0, t2 - t0);
     const double aTb = dot(p - t0, b);
     return aTb * aTb / n2(b);
 }
-__device__ __forceinline__ double ee_d2(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
+CIPC_HD double ee_d2(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
 {
     const d3 b = cross(ea1 - ea0, eb1 - eb0);
     const double aTb = dot(eb0 - ea0, b);
     return aTb * aTb / n2(b);
 }
-__device__ __forceinline__ double ee_cross_n2(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
+CIPC_HD double ee_cross_n2(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
 {
     return n2(cross(ea1 - ea0, eb1 - eb0));
 }
 
-__device__ __forceinline__ double pt_d2_any(d3 p, d3 t0, d3 t1, d3 t2)
+CIPC_HD double pt_d2_any(d3 p, d3 t0, d3 t1, d3 t2)
 {
     switch (pt_type(p, t0, t1, t2)) {
         case 0: return pp_d2(p, t0);
@@ -173,7 +182,7 @@ __device__ __forceinline__ double pt_d2_any(d3 p, d3 t0, d3 t1, d3 t2)
     }
 }
 
-__device__ __forceinline__ double ee_d2_any(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
+CIPC_HD double ee_d2_any(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
 {
     switch (ee_type(ea0, ea1, eb0, eb1)) {
         case 0: return pp_d2(ea0, eb0);
@@ -189,7 +198,7 @@ __device__ __forceinline__ double ee_d2_any(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
 }
 
 // projection form used by the unclassified point-edge CCD distance
-__device__ __forceinline__ double pe_d2_any(d3 p, d3 e0, d3 e1)
+CIPC_HD double pe_d2_any(d3 p, d3 e0, d3 e1)
 {
     const d3 v = e1 - e0, w = p - e0;
     const double c1 = dot(w, v);

@@ -1,0 +1,45 @@
+// CPU ORACLE — test infrastructure only.  Shell scene, contact set and one
+// implicit-Euler step, restated from the reference (see oracle_shell.cpp).
+#pragma once
+#include <cstdint>
+#include <vector>
+
+namespace orc {
+
+// constraint kinds (mollified kinds carry the 4 vertices of the two edges)
+enum ConKind { kPP = 0, kPE = 1, kPT = 2, kEE = 3, kEEM = 4, kPEM = 5, kPPM = 6 };
+
+struct Con {
+    int k;     // ConKind
+    int v[4];  // PP (p0,p1) PE (p,e0,e1) PT (p,t0,t1,t2) EE (ea0,ea1,eb0,eb1)
+               // EEM (ea0,ea1,eb0,eb1) PEM (p,p',e0,e1) PPM (p,p',q,q'): primed = edge partner
+    int mult;  // PP/PE multiplicity after merging duplicates (1 otherwise)
+};
+
+struct Shell {
+    int nv = 0;
+    std::vector<double> X0;           // rest positions (nv*3), nodeAttr.x0
+    std::vector<int> tri;             // nt*3 (degenerate triangles removed)
+    std::vector<double> P;            // nt*3 inverse rest first fundamental form (p00,p01,p11)
+    std::vector<double> vol;          // nt area * thickness
+    double lam = 0, mu = 0;           // plane-stress Lame parameters
+    std::vector<int> hinge;           // nh*4 (x0, x1, x2, x3), hinge edge x1-x2
+    std::vector<double> hinfo;        // nh*3 (thetabar, |ebar|, hbar)
+    double kbend = 0;                 // bendingStiffMult * E t^3 / (24 (1 - nu^2))
+    std::vector<double> mass;         // nv lumped
+    std::vector<double> b;            // nv*3 body force
+    std::vector<int> bnode, bedge, btri;  // contact primitives
+    std::vector<char> dbc;            // nv mask
+    int nh_model = 1;                 // membrane: 1 Neo-Hookean (reference default), 0 StVK
+};
+
+struct StepParams {
+    double h, dHat2, xi;  // time step, dhat^2, offset (thickness)
+    double mu, epsv2;     // friction coefficient, epsv^2
+    int fricIterAmt;
+    double tol;           // Newton tolerance (velocity units: RMS step / h)
+    int withCollision;
+    int maxIter;          // safety cap on Newton iterations
+};
+
+}  // namespace orc
