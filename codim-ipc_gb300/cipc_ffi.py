@@ -153,3 +153,132 @@ def encode_reference_constraint(type_, idx4, mollified=False, multiplicity=1):
     _check(lib().cipc_encode_reference_constraint(int(type_), a.ctypes.data, int(bool(mollified)),
                                                   int(multiplicity), out.ctypes.data))
     return out
+
+
+# ---------------------------------------------------------------------------
+# shell simulation (cipc_sim_*)
+# ---------------------------------------------------------------------------
+class StepParams(ctypes.Structure):
+    _fields_ = [("h", ctypes.c_double), ("dhat2", ctypes.c_double), ("xi", ctypes.c_double), ("mu", ctypes.c_double),
+                ("epsv2", ctypes.c_double), ("fric_iters", ctypes.c_int), ("newton_tol", ctypes.c_double),
+                ("with_collision", ctypes.c_int), ("max_newton_iters", ctypes.c_int), ("precision", ctypes.c_int),
+                ("pcg_tol", ctypes.c_double), ("pcg_max_iters", ctypes.c_int), ("preconditioner", ctypes.c_int)]
+
+
+class StepStats(ctypes.Structure):
+    _fields_ = [("newton_iters", ctypes.c_int), ("pcg_iters", ctypes.c_int), ("line_search_trials", ctypes.c_int),
+                ("n_constraints", ctypes.c_int), ("status", ctypes.c_int), ("min_dist2", ctypes.c_double),
+                ("kappa", ctypes.c_double), ("ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_PP = ctypes.POINTER(ctypes.c_void_p)
+_SIGS.update({
+    "cipc_sim_create": (_c_int, [_c_int, _vp, _c_int, _vp, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _vp, _c_dbl, _c_int, _PP]),
+    "cipc_sim_destroy": (_c_int, [_vp]),
+    "cipc_sim_init_oipc": (_c_int, [_vp, _c_dbl, _c_dbl, _vp, _vp]),
+    "cipc_sim_set_kappa": (_c_int, [_vp, _c_dbl, _c_dbl]),
+    "cipc_sim_get_kappa": (_c_int, [_vp, _vp]),
+    "cipc_sim_set_state": (_c_int, [_vp, _vp, _vp]),
+    "cipc_sim_get_state": (_c_int, [_vp, _vp, _vp]),
+    "cipc_sim_set_dbc": (_c_int, [_vp, _c_int, _vp, _vp]),
+    "cipc_sim_step": (_c_int, [_vp, ctypes.POINTER(StepParams), ctypes.POINTER(StepStats)]),
+    "cipc_sim_constraints": (_c_int, [_vp, ctypes.POINTER(StepParams), _vp, _c_int, _vp, ctypes.POINTER(_c_int)]),
+    "cipc_sim_eval": (_c_int, [_vp, ctypes.POINTER(StepParams), _vp, _vp, _vp, _vp]),
+    "cipc_sim_ccd": (_c_int, [_vp, ctypes.POINTER(StepParams), _vp, _vp, _c_dbl, _vp]),
+})
+
+
+def make_params(h, dhat2, xi, mu=0.0, epsv2=1e-6, fric_iters=1, newton_tol=1e-2, with_collision=True,
+                max_newton_iters=200, precision=FP64, pcg_tol=1e-6, pcg_max_iters=10000, preconditioner=0):
+    return StepParams(h, dhat2, xi, mu, epsv2, fric_iters, newton_tol, int(bool(with_collision)), max_newton_iters,
+                      precision, pcg_tol, pcg_max_iters, preconditioner)
+
+
+class Sim:
+    """Owns one cipc_sim handle (device-resident shell scene)."""
+
+    def __init__(self, X, T, rho, E, nu, thickness, gravity=(0.0, -9.81, 0.0), bend_stiff_mult=1.0, nh=True):
+        X = np.ascontiguousarray(X, np.float64)
+        T = np.ascontiguousarray(T, np.int32)
+        g = np.ascontiguousarray(gravity, np.float64)
+        h = ctypes.c_void_p()
+        _check(lib().cipc_sim_create(X.shape[0], X.ctypes.data, T.shape[0], T.ctypes.data, rho, E, nu, thickness,
+                                     g.ctypes.data, bend_stiff_mult, 1 if nh else 0, ctypes.byref(h)))
+        self.h = h
+        self.nv = X.shape[0]
+
+    def close(self):
+        if self.h:
+            lib().cipc_sim_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init_oipc(self, dhat, stiff_mult=1.0):
+        k2 = np.zeros(2)
+        d2 = ctypes.c_double()
+        _check(lib().cipc_sim_init_oipc(self.h, dhat, stiff_mult, k2.ctypes.data, ctypes.byref(d2)))
+        return k2, d2.value
+
+    def set_kappa(self, kappa, kappa_max):
+        _check(lib().cipc_sim_set_kappa(self.h, kappa, kappa_max))
+
+    def kappa(self):
+        k2 = np.zeros(2)
+        _check(lib().cipc_sim_get_kappa(self.h, k2.ctypes.data))
+        return k2
+
+    def set_state(self, x=None, v=None):
+        xa = None if x is None else np.ascontiguousarray(x, np.float64)
+        va = None if v is None else np.ascontiguousarray(v, np.float64)
+        _check(lib().cipc_sim_set_state(self.h, None if xa is None else xa.ctypes.data,
+                                        None if va is None else va.ctypes.data))
+
+    def state(self):
+        x = np.zeros((self.nv, 3))
+        v = np.zeros((self.nv, 3))
+        _check(lib().cipc_sim_get_state(self.h, x.ctypes.data, v.ctypes.data))
+        return x, v
+
+    def set_dbc(self, idx, targets):
+        idx = np.ascontiguousarray(idx, np.int32)
+        tg = np.ascontiguousarray(targets, np.float64)
+        _check(lib().cipc_sim_set_dbc(self.h, idx.shape[0], idx.ctypes.data, tg.ctypes.data))
+
+    def step(self, params, allow=()):
+        st = StepStats()
+        rc = lib().cipc_sim_step(self.h, ctypes.byref(params), ctypes.byref(st))
+        _check(rc, allow)
+        return st
+
+    def constraints(self, params, x, cap=1 << 20):
+        out = np.zeros((cap, 6), np.int32)
+        c = ctypes.c_int()
+        xa = np.ascontiguousarray(x, np.float64)
+        _check(lib().cipc_sim_constraints(self.h, ctypes.byref(params), xa.ctypes.data, cap, out.ctypes.data,
+                                          ctypes.byref(c)))
+        return out[:min(c.value, cap)].copy()
+
+    def eval(self, params, x, xtilde):
+        g = np.zeros((self.nv, 3))
+        E = ctypes.c_double()
+        xa = np.ascontiguousarray(x, np.float64)
+        xt = np.ascontiguousarray(xtilde, np.float64)
+        _check(lib().cipc_sim_eval(self.h, ctypes.byref(params), xa.ctypes.data, xt.ctypes.data, ctypes.byref(E),
+                                   g.ctypes.data))
+        return E.value, g
+
+    def ccd(self, params, x, d, alpha=1.0):
+        out = ctypes.c_double()
+        xa = np.ascontiguousarray(x, np.float64)
+        da = np.ascontiguousarray(d, np.float64)
+        _check(lib().cipc_sim_ccd(self.h, ctypes.byref(params), xa.ctypes.data, da.ctypes.data, alpha,
+                                  ctypes.byref(out)))
+        return out.value

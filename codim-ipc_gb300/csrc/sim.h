@@ -1,0 +1,122 @@
+// Device-resident state of one shell simulation (one CUDA stream per handle) and
+// the internal entry points of the time-step kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+namespace cipc {
+
+// constraint kinds: PP, PE, PT, EE and the mollified edge-edge family whose
+// four vertices are the two edges (EEM: ea0 ea1 eb0 eb1, PEM: p p' e0 e1,
+// PPM: p p' q q', primed = the other endpoint of the point's edge)
+enum ConKind : int { cPP = 0, cPE = 1, cPT = 2, cEE = 3, cEEM = 4, cPEM = 5, cPPM = 6 };
+
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count)
+    {
+        if (count <= n && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc((void**)&p, (count ? count : 1) * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct SimParams {
+    double h = 0.04;          // time step
+    double dHat2 = 1e-6;      // dhat^2
+    double xi = 0;            // offset (thickness)
+    double mu = 0;            // friction coefficient
+    double epsv2 = 1e-6;      // friction smoothing epsv^2 (times h^2 inside)
+    int fricIterAmt = 1;      // friction basis updates per step
+    double tol = 1e-2;        // Newton tolerance on RMS(step)/h
+    int withCollision = 1;
+    int maxIter = 200;        // Newton iteration cap
+    int precision = 0;        // 0 FP64 Hessians / PCG, 1 FP32 Hessians + FP32 PCG with FP64 refinement
+    double pcg_tol = 1e-6;    // relative residual of the Newton system (FP64)
+    int pcg_maxit = 10000;
+    int precond = 0;          // 0 block-Jacobi, 1 learned correction (when a model is loaded)
+};
+
+struct StepStats {
+    int newton_iters = 0;
+    int pcg_iters = 0;        // total inner iterations
+    int line_search_trials = 0;
+    int n_constraints = 0;
+    int status = 0;
+    double min_dist2 = 0;
+    double kappa = 0;
+    double ms = 0;
+};
+
+struct Sim {
+    // sizes
+    int nv = 0, nt = 0, nh = 0, nbn = 0, nbe = 0, nbt = 0;
+    int nh_model = 1;
+    double lam = 0, mu = 0, kbend = 0;
+    double cell = 1;  // broad-phase cell size (mean rest edge length)
+    double kappa = 1, kappa_max = 100;
+    // static device data
+    DBuf<int> tri, hinge, bnode, bedge, btri;
+    DBuf<double> P, vol, hinfo, mass, b, X0;
+    DBuf<uint8_t> dbc;
+    std::vector<int> dbc_idx_h;
+    DBuf<int> dbc_idx;
+    DBuf<double> dbc_tgt;
+    // block sparsity of the elastic part (vertex blocks, 3x3)
+    int nnzb = 0;
+    DBuf<int> row_ptr, col, diag, tri_slot, hinge_slot;
+    // dynamic
+    DBuf<double> x, xn, xt, v, g, dir, xprev, rhs, disp;
+    DBuf<char> hval;  // BSR values, float or double per precision
+    // contact constraint list
+    int ncon = 0, cap_con = 0;
+    DBuf<int> ckind, cmult;
+    DBuf<int4> cverts;
+    DBuf<char> chess;  // 78 entries per constraint (float/double)
+    // previous iterate's constraint list and its distances (barrier stiffness update)
+    int npcon = 0;
+    DBuf<int> pkind;
+    DBuf<int4> pverts;
+    DBuf<double> pd2;
+    // friction (lagged)
+    int nfric = 0;
+    DBuf<int> fkind, fmult;
+    DBuf<int4> fverts;
+    DBuf<double> fw, fT, flam;  // 4 weights, 6 basis entries, normal force per friction constraint
+    DBuf<char> fhess;
+    // block-Jacobi diagonal (9 per vertex, double) and its inverse (float/double)
+    DBuf<double> pdiag;
+    DBuf<char> pinv;
+    // scratch
+    DBuf<double> red;               // reduction partials
+    DBuf<unsigned long long> cnt;   // counters
+    DBuf<char> scratch;             // broad-phase / solver work space
+    size_t scratch_bytes = 0;
+    cudaStream_t stream = nullptr;
+    SimParams prm;
+    StepStats last;
+    // learned preconditioner (optional)
+    void* learned = nullptr;
+    std::vector<double> host_mass;
+};
+
+// host-side construction (sim_setup.cpp)
+int sim_create(Sim** out, int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
+               double thickness, const double* gravity, double bendMult, int nh_model);
+void sim_destroy(Sim* s);
+
+}  // namespace cipc

@@ -1,0 +1,258 @@
+// Elastic and inertia terms of the incremental potential (INC_POTENTIAL.h:15-395):
+// membrane and hinge bending per element, 1/2 (x - xtilde)^T M (x - xtilde), and
+// the Dirichlet projection of the Hessian (CSR_MATRIX.h:130-141).
+//
+// Energies: FP64, one partial per block written to a reduction buffer and summed
+// in a fixed order (deterministic).  Gradients: FP64 atomics into g.  Hessians:
+// each element's PSD-projected blocks are added (atomically, in HT = float or
+// double) into the block-sparse matrix at slots precomputed from the mesh;
+// blocks that touch a Dirichlet vertex are skipped and Dirichlet diagonal blocks
+// are set to the identity.
+#include <cuda_runtime.h>
+
+#include "elements.cuh"
+#include "sim.h"
+#include "sim_kernels.h"
+
+namespace cipc {
+
+__device__ __forceinline__ double block_sum(double v, double* sh)
+{
+    const int t = threadIdx.x;
+    sh[t] = v;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (t < s) sh[t] += sh[t + s];
+        __syncthreads();
+    }
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_xtilde(int nv, const double* x, const double* v, const double* b, const double* m, double h,
+                         double* xt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const double mi = m[i];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double a = mi > 0 ? b[3 * i + d] / mi : 0.0;
+        xt[3 * i + d] = x[3 * i + d] + h * v[3 * i + d] + h * h * a;
+    }
+}
+
+// inertia energy partials, gradient m (x - xt) (g is overwritten: first term)
+__global__ void __launch_bounds__(256) k_inertia(int nv, const double* x, const double* xt, const double* m, double* g,
+                                                  double* red)
+{
+    __shared__ double sh[256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0;
+    if (i < nv) {
+        const double mi = m[i];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double dd = x[3 * i + d] - xt[3 * i + d];
+            e += mi * dd * dd;
+            if (g) g[3 * i + d] = mi * dd;
+        }
+    }
+    const double s = block_sum(0.5 * e, sh);
+    if (red && threadIdx.x == 0) red[blockIdx.x] = s;
+}
+
+template <typename HT>
+__device__ __forceinline__ void scatter_blocks(HT* hval, const int* slots, const uint8_t* dbc, const int* vid, int nvb,
+                                               const HT* H, int m)
+{
+    for (int a = 0; a < nvb; ++a) {
+        if (dbc[vid[a]]) continue;
+        for (int b = 0; b < nvb; ++b) {
+            if (dbc[vid[b]]) continue;
+            HT* dst = hval + 9 * (size_t)slots[nvb * a + b];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) atomicAdd(dst + 3 * i + j, H[(3 * a + i) * m + 3 * b + j]);
+        }
+    }
+}
+
+template <typename HT>
+__global__ void __launch_bounds__(128) k_membrane(ElasticArgs a, HT* hval)
+{
+    __shared__ double sh[128];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0;
+    if (t < a.nt) {
+        const int vid[3] = {a.tri[3 * t], a.tri[3 * t + 1], a.tri[3 * t + 2]};
+        if (!(a.dbc[vid[0]] && a.dbc[vid[1]] && a.dbc[vid[2]])) {
+            const d3 x[3] = {ld(a.x, vid[0]), ld(a.x, vid[1]), ld(a.x, vid[2])};
+            MembraneOut o;
+            double S[3], c;
+            const double k = a.h * a.h * a.vol[t];
+            membrane_eg(x, a.P + 3 * t, k, a.lam, a.mu, a.nh_model, o, S, c);
+            e = o.E;
+            if (a.g)
+                for (int v = 0; v < 3; ++v)
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) atomicAdd(a.g + 3 * vid[v] + d, o.g[3 * v + d]);
+            if (hval) {
+                HT H[9][9];
+                membrane_hess<HT>(x, a.P + 3 * t, k, a.lam, a.mu, a.nh_model, S, c, H);
+                project_translation_free<HT, 3>(H);
+                scatter_blocks<HT>(hval, a.tri_slot + 9 * t, a.dbc, vid, 3, &H[0][0], 9);
+            }
+        }
+    }
+    const double s = block_sum(e, sh);
+    if (a.red && threadIdx.x == 0) a.red[blockIdx.x] = s;
+}
+
+template <typename HT>
+__global__ void __launch_bounds__(128) k_bending(ElasticArgs a, HT* hval)
+{
+    __shared__ double sh[128];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0;
+    if (t < a.nh && a.kbend != 0) {
+        const int vid[4] = {a.hinge[4 * t], a.hinge[4 * t + 1], a.hinge[4 * t + 2], a.hinge[4 * t + 3]};
+        if (!(a.dbc[vid[0]] && a.dbc[vid[1]] && a.dbc[vid[2]] && a.dbc[vid[3]])) {
+            const d3 x[4] = {ld(a.x, vid[0]), ld(a.x, vid[1]), ld(a.x, vid[2]), ld(a.x, vid[3])};
+            const double thetabar = a.hinfo[3 * t], c = a.h * a.h * a.kbend * a.hinfo[3 * t + 1] / a.hinfo[3 * t + 2];
+            const double th = dihedral_angle(x);
+            const double dth = th - thetabar;
+            e = c * dth * dth;
+            double gt[12];
+            dihedral_grad(x, gt);
+            if (a.g)
+                for (int v = 0; v < 4; ++v)
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) atomicAdd(a.g + 3 * vid[v] + d, 2 * c * dth * gt[3 * v + d]);
+            if (hval) {
+                double Ht[12][12];
+                dihedral_hess(x, Ht);
+                HT H[12][12];
+#pragma unroll
+                for (int i = 0; i < 12; ++i)
+#pragma unroll
+                    for (int j = 0; j < 12; ++j) H[i][j] = (HT)(2 * c * (gt[i] * gt[j] + dth * Ht[i][j]));
+                project_translation_free<HT, 4>(H);
+                scatter_blocks<HT>(hval, a.hinge_slot + 16 * t, a.dbc, vid, 4, &H[0][0], 12);
+            }
+        }
+    }
+    const double s = block_sum(e, sh);
+    if (a.red && threadIdx.x == 0) a.red[blockIdx.x] = s;
+}
+
+// mass on free diagonal blocks, identity on Dirichlet diagonal blocks
+template <typename HT>
+__global__ void k_mass_diag(int nv, const double* m, const uint8_t* dbc, const int* diag, HT* hval)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    HT* d = hval + 9 * (size_t)diag[i];
+    const HT v = dbc[i] ? HT(1) : (HT)m[i];
+    d[0] += v;
+    d[4] += v;
+    d[8] += v;
+}
+
+__global__ void k_zero_dbc(int nv, const uint8_t* dbc, double* g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nv && dbc[i]) g[3 * i] = g[3 * i + 1] = g[3 * i + 2] = 0;
+}
+
+// sum of n partials in a fixed order (single block)
+__global__ void k_sum(const double* red, int n, double* out)
+{
+    __shared__ double sh[1024];
+    double s = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += red[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sh[0];
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static inline int nblk(int n, int bs) { return n > 0 ? (n + bs - 1) / bs : 1; }
+
+void launch_xtilde(Sim* s)
+{
+    k_xtilde<<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->x.p, s->v.p, s->b.p, s->mass.p, s->prm.h, s->xt.p);
+}
+
+ElasticArgs elastic_args(Sim* s, const double* x, double* g)
+{
+    ElasticArgs a;
+    a.nt = s->nt;
+    a.nh = s->nh;
+    a.tri = s->tri.p;
+    a.hinge = s->hinge.p;
+    a.P = s->P.p;
+    a.vol = s->vol.p;
+    a.hinfo = s->hinfo.p;
+    a.tri_slot = s->tri_slot.p;
+    a.hinge_slot = s->hinge_slot.p;
+    a.dbc = s->dbc.p;
+    a.x = x;
+    a.g = g;
+    a.h = s->prm.h;
+    a.lam = s->lam;
+    a.mu = s->mu;
+    a.kbend = s->kbend;
+    a.nh_model = s->nh_model;
+    a.red = nullptr;
+    return a;
+}
+
+// Energy partial layout: [inertia | membrane | bending]; returns the partial count.
+int elastic_energy_partials(Sim* s, const double* x, double* red)
+{
+    const int b0 = nblk(s->nv, 256), b1 = nblk(s->nt, 128), b2 = nblk(s->nh, 128);
+    k_inertia<<<b0, 256, 0, s->stream>>>(s->nv, x, s->xt.p, s->mass.p, nullptr, red);
+    ElasticArgs a = elastic_args(s, x, nullptr);
+    a.red = red + b0;
+    k_membrane<double><<<b1, 128, 0, s->stream>>>(a, nullptr);
+    a.red = red + b0 + b1;
+    k_bending<double><<<b2, 128, 0, s->stream>>>(a, nullptr);
+    return b0 + b1 + b2;
+}
+
+void elastic_grad_hess(Sim* s, const double* x, double* g, bool want_hess)
+{
+    k_inertia<<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, x, s->xt.p, s->mass.p, g, nullptr);
+    ElasticArgs a = elastic_args(s, x, g);
+    const bool f32 = s->prm.precision == 1;
+    if (want_hess) cudaMemsetAsync(s->hval.p, 0, 9 * (size_t)s->nnzb * (f32 ? 4 : 8), s->stream);
+    if (f32) {
+        float* hv = want_hess ? (float*)s->hval.p : nullptr;
+        k_membrane<float><<<nblk(s->nt, 128), 128, 0, s->stream>>>(a, hv);
+        k_bending<float><<<nblk(s->nh, 128), 128, 0, s->stream>>>(a, hv);
+        if (want_hess) k_mass_diag<float><<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->mass.p, s->dbc.p, s->diag.p, hv);
+    } else {
+        double* hv = want_hess ? (double*)s->hval.p : nullptr;
+        k_membrane<double><<<nblk(s->nt, 128), 128, 0, s->stream>>>(a, hv);
+        k_bending<double><<<nblk(s->nh, 128), 128, 0, s->stream>>>(a, hv);
+        if (want_hess) k_mass_diag<double><<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->mass.p, s->dbc.p, s->diag.p, hv);
+    }
+}
+
+void zero_dbc(Sim* s, double* g) { k_zero_dbc<<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->dbc.p, g); }
+
+void sum_partials(Sim* s, const double* red, int n, double* out)
+{
+    k_sum<<<1, 1024, 0, s->stream>>>(red, n, out);
+}
+
+}  // namespace cipc

@@ -1,0 +1,45 @@
+// Launchers of the time-step kernels (all enqueue on Sim::stream).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "sim.h"
+
+namespace cipc {
+
+struct ElasticArgs {
+    int nt, nh;
+    const int *tri, *hinge;
+    const double *P, *vol, *hinfo;
+    const int *tri_slot, *hinge_slot;
+    const uint8_t* dbc;
+    const double* x;
+    double* g;
+    double h, lam, mu, kbend;
+    int nh_model;
+    double* red;
+};
+
+// sim_elastic.cu
+void launch_xtilde(Sim* s);
+int elastic_energy_partials(Sim* s, const double* x, double* red);  // returns #partials written
+void elastic_grad_hess(Sim* s, const double* x, double* g, bool want_hess);
+void zero_dbc(Sim* s, double* g);
+void sum_partials(Sim* s, const double* red, int n, double* out);
+
+// sim_contact.cu
+int build_constraints(Sim* s, const double* x);           // fills the constraint list; status code
+int contact_energy_partials(Sim* s, const double* x, double* red, double* flag);  // #partials; flag: s <= 0 seen
+void contact_grad_hess(Sim* s, const double* x, double* g, bool want_hess);
+void min_dist2_partials(Sim* s, const double* x, double* out_min);  // device scalar
+int friction_basis(Sim* s, const double* x);               // lagged basis from the current constraint list
+int friction_energy_partials(Sim* s, const double* x, double* red);
+void friction_grad_hess(Sim* s, const double* x, double* g, bool want_hess);
+int ccd_step_size(Sim* s, const double* x, const double* p, double alpha_in, double* alpha_out);
+void kappa_check(Sim* s, const double* x, int* update_flag_dev);  // uses the previous constraint list
+
+// sim_solve.cu
+int linear_solve(Sim* s, const double* rhs, double* sol, int* iters);
+
+}  // namespace cipc

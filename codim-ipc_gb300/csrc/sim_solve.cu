@@ -1,0 +1,389 @@
+// Newton-system solve: preconditioned conjugate gradients on the assembled
+// Hessian (replaces the reference's per-iteration CHOLMOD factorization,
+// Library/Math/DIRECT_SOLVER.h:13-88).
+//
+// Operator: y = H x with H = (elastic + mass, 3x3 block CSR) + sum over contact
+// constraints of their stored PSD blocks + sum over friction constraints of
+// w_a w_b T M T^T (applied matrix-free from the 2x2 inner matrix).  Dirichlet
+// rows/columns were removed at assembly (identity diagonal), so Dirichlet
+// entries of every PCG vector stay zero.
+//
+// Precision modes:
+//   FP64:  matrix, vectors and reductions in FP64 (block-Jacobi PCG).
+//   mixed: matrix values FP32; inner PCG in FP32 vectors with FP32 block
+//          partials; outer iterative refinement in FP64 (r = b - H x with FP64
+//          vectors), so the Newton increment meets the same FP64 residual bound.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+
+#include "../../include/cipc.h"
+#include "cipc_util.h"
+#include "constraint_eval.cuh"
+#include "sim.h"
+#include "sim_kernels.h"
+
+namespace cipc {
+
+static inline int nblk(long long n, int bs) { return n > 0 ? (int)((n + bs - 1) / bs) : 1; }
+
+template <typename VT, typename XT>
+__global__ void __launch_bounds__(256) k_bsr_spmv(int nv, const int* __restrict__ row_ptr, const int* __restrict__ col,
+                                                  const VT* __restrict__ val, const XT* __restrict__ x,
+                                                  XT* __restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    XT a0 = 0, a1 = 0, a2 = 0;
+    for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+        const int j = col[k];
+        const VT* B = val + 9 * (size_t)k;
+        const XT x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
+        a0 += (XT)B[0] * x0 + (XT)B[1] * x1 + (XT)B[2] * x2;
+        a1 += (XT)B[3] * x0 + (XT)B[4] * x1 + (XT)B[5] * x2;
+        a2 += (XT)B[6] * x0 + (XT)B[7] * x1 + (XT)B[8] * x2;
+    }
+    y[3 * i] = a0;
+    y[3 * i + 1] = a1;
+    y[3 * i + 2] = a2;
+}
+
+// contact blocks: packed upper triangle (row by row) of the (3nv x 3nv) constraint Hessian
+template <typename VT, typename XT>
+__global__ void __launch_bounds__(128) k_con_spmv(int n, const int* __restrict__ kind, const int4* __restrict__ verts,
+                                                  const VT* __restrict__ hess, const XT* __restrict__ x,
+                                                  XT* __restrict__ y)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const int nv = con_nv(kind[c]);
+    const int m = 3 * nv;
+    const int4 iv = verts[c];
+    const int id[4] = {iv.x, iv.y, iv.z, iv.w};
+    XT xs[12], ys[12];
+    for (int q = 0; q < nv; ++q)
+        for (int d = 0; d < 3; ++d) {
+            xs[3 * q + d] = x[3 * id[q] + d];
+            ys[3 * q + d] = 0;
+        }
+    const VT* H = hess + 78 * (size_t)c;
+    int w = 0;
+    for (int p = 0; p < m; ++p) {
+        ys[p] += (XT)H[w] * xs[p];
+        ++w;
+        for (int q = p + 1; q < m; ++q, ++w) {
+            const XT h = (XT)H[w];
+            ys[p] += h * xs[q];
+            ys[q] += h * xs[p];
+        }
+    }
+    for (int q = 0; q < nv; ++q)
+        for (int d = 0; d < 3; ++d)
+            if (ys[3 * q + d] != XT(0)) atomicAdd(y + 3 * id[q] + d, ys[3 * q + d]);
+}
+
+// friction: y_a += w_a T M T^T sum_b w_b x_b
+template <typename XT>
+__global__ void k_fric_spmv(int n, const int* __restrict__ kind, const int4* __restrict__ verts,
+                            const double* __restrict__ fw, const double* __restrict__ fT, const double* __restrict__ M,
+                            const uint8_t* __restrict__ dbc, const XT* __restrict__ x, XT* __restrict__ y)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n || kind[c] >= kc_EEM) return;
+    const int nv = con_nv(kind[c]);
+    const int4 iv = verts[c];
+    const int id[4] = {iv.x, iv.y, iv.z, iv.w};
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int q = 0; q < nv; ++q) {
+        if (dbc[id[q]]) continue;
+        const double w = fw[4 * c + q];
+        s0 += w * (double)x[3 * id[q]];
+        s1 += w * (double)x[3 * id[q] + 1];
+        s2 += w * (double)x[3 * id[q] + 2];
+    }
+    const double* T = fT + 6 * (size_t)c;
+    const double t0 = T[0] * s0 + T[1] * s1 + T[2] * s2, t1 = T[3] * s0 + T[4] * s1 + T[5] * s2;
+    const double m00 = M[3 * c], m01 = M[3 * c + 1], m11 = M[3 * c + 2];
+    const double u0 = m00 * t0 + m01 * t1, u1 = m01 * t0 + m11 * t1;
+    const double o0 = T[0] * u0 + T[3] * u1, o1 = T[1] * u0 + T[4] * u1, o2 = T[2] * u0 + T[5] * u1;
+    for (int q = 0; q < nv; ++q) {
+        if (dbc[id[q]]) continue;
+        const double w = fw[4 * c + q];
+        atomicAdd(y + 3 * id[q], (XT)(w * o0));
+        atomicAdd(y + 3 * id[q] + 1, (XT)(w * o1));
+        atomicAdd(y + 3 * id[q] + 2, (XT)(w * o2));
+    }
+}
+
+// block-Jacobi: pdiag (already holding contact / friction diagonal blocks) += BSR
+// diagonal blocks, then inverted (3x3, FP64)
+template <typename VT, typename PT>
+__global__ void k_precond(int nv, const int* diag, const VT* val, const double* pdiag, PT* pinv)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    double A[9];
+    const VT* B = val + 9 * (size_t)diag[i];
+    for (int k = 0; k < 9; ++k) A[k] = (double)B[k] + pdiag[9 * (size_t)i + k];
+    const double c00 = A[4] * A[8] - A[5] * A[7], c01 = A[5] * A[6] - A[3] * A[8], c02 = A[3] * A[7] - A[4] * A[6];
+    const double det = A[0] * c00 + A[1] * c01 + A[2] * c02;
+    double inv[9];
+    if (!(fabs(det) > 0)) {
+        for (int k = 0; k < 9; ++k) inv[k] = (k % 4 == 0) ? 1.0 : 0.0;
+    } else {
+        const double id = 1.0 / det;
+        inv[0] = c00 * id;
+        inv[3] = c01 * id;
+        inv[6] = c02 * id;
+        inv[1] = (A[2] * A[7] - A[1] * A[8]) * id;
+        inv[4] = (A[0] * A[8] - A[2] * A[6]) * id;
+        inv[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+        inv[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+        inv[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+        inv[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+    }
+    for (int k = 0; k < 9; ++k) pinv[9 * (size_t)i + k] = (PT)inv[k];
+}
+
+// dot product partials (block sums in XT, written as double)
+template <typename XT>
+__global__ void k_dot(int n, const XT* __restrict__ a, const XT* __restrict__ b, double* part)
+{
+    __shared__ XT sh[256];
+    XT s = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += a[i] * b[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = (double)sh[0];
+}
+__global__ void k_dot_final(const double* part, int n, double* out)
+{
+    __shared__ double sh[256];
+    double s = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sh[0];
+}
+
+// z = Pinv r  (per vertex 3x3)
+template <typename XT, typename PT>
+__global__ void k_apply_precond(int nv, const PT* __restrict__ pinv, const XT* __restrict__ r, XT* __restrict__ z)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const PT* P = pinv + 9 * (size_t)i;
+    const XT r0 = r[3 * i], r1 = r[3 * i + 1], r2 = r[3 * i + 2];
+    z[3 * i] = (XT)P[0] * r0 + (XT)P[1] * r1 + (XT)P[2] * r2;
+    z[3 * i + 1] = (XT)P[3] * r0 + (XT)P[4] * r1 + (XT)P[5] * r2;
+    z[3 * i + 2] = (XT)P[6] * r0 + (XT)P[7] * r1 + (XT)P[8] * r2;
+}
+
+// x += alpha p ; r -= alpha q with alpha = sc[rz] / sc[pq]
+template <typename XT>
+__global__ void k_update_xr(int n, const double* sc, int irz, int ipq, const XT* p, const XT* q, XT* x, XT* r)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double den = sc[ipq];
+    const XT alpha = (XT)(den != 0 ? sc[irz] / den : 0.0);
+    x[i] += alpha * p[i];
+    r[i] -= alpha * q[i];
+}
+// p = z + beta p with beta = sc[rz_new] / sc[rz_old]
+template <typename XT>
+__global__ void k_update_p(int n, const double* sc, int inew, int iold, const XT* z, XT* p)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double den = sc[iold];
+    const XT beta = (XT)(den != 0 ? sc[inew] / den : 0.0);
+    p[i] = z[i] + beta * p[i];
+}
+template <typename A, typename B>
+__global__ void k_convert(int n, const A* a, B* b)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (B)a[i];
+}
+// r = b - y (FP64)
+__global__ void k_residual(int n, const double* b, const double* y, double* r)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) r[i] = b[i] - y[i];
+}
+template <typename XT>
+__global__ void k_axpy_into(int n, const XT* d, double* x)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] += (double)d[i];
+}
+
+struct SolveCtx {
+    Sim* s;
+    cudaStream_t st;
+    int n3;
+    double* part;   // dot partials
+    double* sc;     // device scalars
+    int nparts;
+};
+
+template <typename XT>
+static void dot(SolveCtx& C, const XT* a, const XT* b, double* out)
+{
+    k_dot<XT><<<C.nparts, 256, 0, C.st>>>(C.n3, a, b, C.part);
+    k_dot_final<<<1, 256, 0, C.st>>>(C.part, C.nparts, out);
+}
+
+template <typename VT, typename XT>
+static void apply_H(SolveCtx& C, const XT* x, XT* y)
+{
+    Sim* s = C.s;
+    k_bsr_spmv<VT, XT><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, s->row_ptr.p, s->col.p, (const VT*)s->hval.p, x, y);
+    if (s->ncon > 0)
+        k_con_spmv<VT, XT><<<nblk(s->ncon, 128), 128, 0, C.st>>>(s->ncon, s->ckind.p, s->cverts.p,
+                                                                  (const VT*)s->chess.p, x, y);
+    if (s->nfric > 0 && s->prm.mu > 0)
+        k_fric_spmv<XT><<<nblk(s->nfric, 128), 128, 0, C.st>>>(s->nfric, s->fkind.p, s->fverts.p, s->fw.p, s->fT.p,
+                                                                (const double*)s->fhess.p, s->dbc.p, x, y);
+}
+
+// PCG on H x = b (x starts at 0).  Returns iterations; *rel = final |r|/|b| (read every `every` iterations).
+template <typename VT, typename XT>
+static int pcg(SolveCtx& C, const XT* b, XT* x, XT* r, XT* z, XT* p, XT* q, double tol, int maxit, double* rel)
+{
+    const int n = C.n3;
+    const int nb = nblk(n, 256);
+    Sim* s = C.s;
+    cudaMemsetAsync(x, 0, sizeof(XT) * n, C.st);
+    cudaMemcpyAsync(r, b, sizeof(XT) * n, cudaMemcpyDeviceToDevice, C.st);
+    double* sc = C.sc;  // [0] bb, [1] rz_a, [2] rz_b, [3] pq, [4] rr
+    dot<XT>(C, b, b, sc + 0);
+    if (s->prm.precision == 1)
+        k_apply_precond<XT, float><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, (const float*)s->pinv.p, r, z);
+    else
+        k_apply_precond<XT, double><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, (const double*)s->pinv.p, r, z);
+    cudaMemcpyAsync(p, z, sizeof(XT) * n, cudaMemcpyDeviceToDevice, C.st);
+    dot<XT>(C, r, z, sc + 1);
+    double bb = 0;
+    cudaMemcpyAsync(&bb, sc, sizeof(double), cudaMemcpyDeviceToHost, C.st);
+    cudaStreamSynchronize(C.st);
+    *rel = 0;
+    if (!(bb > 0)) return 0;
+    const double thr = tol * tol * bb;
+    int it = 0;
+    int cur = 1;
+    const int every = 8;
+    while (it < maxit) {
+        apply_H<VT, XT>(C, p, q);
+        dot<XT>(C, p, q, sc + 3);
+        k_update_xr<XT><<<nb, 256, 0, C.st>>>(n, sc, cur, 3, p, q, x, r);
+        ++it;
+        if (it % every == 0 || it == maxit) {
+            dot<XT>(C, r, r, sc + 4);
+            double rr = 0;
+            cudaMemcpyAsync(&rr, sc + 4, sizeof(double), cudaMemcpyDeviceToHost, C.st);
+            cudaStreamSynchronize(C.st);
+            *rel = std::sqrt(rr / bb);
+            if (rr <= thr || !(rr == rr)) break;
+        }
+        if (s->prm.precision == 1)
+            k_apply_precond<XT, float><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, (const float*)s->pinv.p, r, z);
+        else
+            k_apply_precond<XT, double><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, (const double*)s->pinv.p, r, z);
+        const int nxt = 3 - cur;
+        dot<XT>(C, r, z, sc + nxt);
+        k_update_p<XT><<<nb, 256, 0, C.st>>>(n, sc, nxt, cur, z, p);
+        cur = nxt;
+    }
+    return it;
+}
+
+// Finalizes the block-Jacobi preconditioner from the assembled matrix
+static void build_precond(Sim* s)
+{
+    if (s->prm.precision == 1)
+        k_precond<float, float><<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->diag.p, (const float*)s->hval.p,
+                                                                          s->pdiag.p, (float*)s->pinv.p);
+    else
+        k_precond<double, double><<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->diag.p, (const double*)s->hval.p,
+                                                                            s->pdiag.p, (double*)s->pinv.p);
+}
+
+int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
+{
+    const int n3 = 3 * s->nv;
+    const size_t need = (size_t)n3 * (6 * sizeof(double) + 6 * sizeof(float)) + 4096 * sizeof(double) + (1 << 16);
+    if (s->scratch.n < need) {
+        cudaStreamSynchronize(s->stream);
+        if (s->scratch.alloc(need) != cudaSuccess) return set_error(CIPC_ERR_CUDA, "solver scratch");
+    }
+    char* base = s->scratch.p;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        off = (off + 255) & ~(size_t)255;
+        char* p = base + off;
+        off += bytes;
+        return p;
+    };
+    SolveCtx C;
+    C.s = s;
+    C.st = s->stream;
+    C.n3 = n3;
+    C.nparts = std::min(nblk(n3, 256), 1024);
+    C.part = (double*)take(1024 * sizeof(double));
+    C.sc = (double*)take(64 * sizeof(double));
+    build_precond(s);
+    int total = 0;
+    double rel = 0;
+    if (s->prm.precision != 1) {
+        double *r = (double*)take(n3 * 8), *z = (double*)take(n3 * 8), *p = (double*)take(n3 * 8),
+               *q = (double*)take(n3 * 8);
+        total = pcg<double, double>(C, rhs, sol, r, z, p, q, s->prm.pcg_tol, s->prm.pcg_maxit, &rel);
+    } else {
+        // mixed: FP32 inner PCG, FP64 iterative refinement of the residual
+        double* r64 = (double*)take(n3 * 8);
+        double* y64 = (double*)take(n3 * 8);
+        float *b32 = (float*)take(n3 * 4), *d32 = (float*)take(n3 * 4), *r = (float*)take(n3 * 4),
+              *z = (float*)take(n3 * 4), *p = (float*)take(n3 * 4), *q = (float*)take(n3 * 4);
+        cudaMemsetAsync(sol, 0, sizeof(double) * n3, s->stream);
+        cudaMemcpyAsync(r64, rhs, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s->stream);
+        double* sc = C.sc;
+        dot<double>(C, rhs, rhs, sc + 10);
+        double bb = 0;
+        cudaMemcpyAsync(&bb, sc + 10, sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+        cudaStreamSynchronize(s->stream);
+        const double inner_tol = 1e-3;
+        for (int outer = 0; outer < 20 && bb > 0; ++outer) {
+            k_convert<double, float><<<nblk(n3, 256), 256, 0, s->stream>>>(n3, r64, b32);
+            double relin = 0;
+            total += pcg<float, float>(C, b32, d32, r, z, p, q, inner_tol, s->prm.pcg_maxit - total, &relin);
+            k_axpy_into<float><<<nblk(n3, 256), 256, 0, s->stream>>>(n3, d32, sol);
+            apply_H<float, double>(C, sol, y64);
+            k_residual<<<nblk(n3, 256), 256, 0, s->stream>>>(n3, rhs, y64, r64);
+            dot<double>(C, r64, r64, sc + 11);
+            double rr = 0;
+            cudaMemcpyAsync(&rr, sc + 11, sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+            cudaStreamSynchronize(s->stream);
+            rel = std::sqrt(rr / bb);
+            if (rel <= s->prm.pcg_tol || total >= s->prm.pcg_maxit) break;
+        }
+    }
+    if (iters) *iters = total;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return set_cuda_error(e, "linear solve");
+    if (!(rel == rel)) return set_error(CIPC_ERR_NAN, "linear solve produced NaN");
+    if (rel > s->prm.pcg_tol) return set_error(CIPC_ERR_NOT_CONVERGED, "PCG stopped at relative residual %g", rel);
+    return CIPC_OK;
+}
+
+}  // namespace cipc

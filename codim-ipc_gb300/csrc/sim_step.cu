@@ -1,0 +1,567 @@
+// One implicit-Euler time step on the GPU and the simulation C ABI.
+//
+// Restates Advance_One_Step_IE_Discrete_Shell (Library/FEM/Shell/IMPLICIT_EULER.h:
+// 151-902) and Line_Search (:9-149): x~ = x + h v + h^2 M^-1 b; Dirichlet targets
+// applied when the Dirichlet step is intersection free; constraint set and lagged
+// friction basis; Newton iterations with an intersection-free (CCD) step bound and
+// backtracking on the incremental potential, the min-distance safeguard, the
+// barrier-stiffness doubling when a tiny distance keeps shrinking, the
+// max-of-last-three RMS(step)/h stopping rule (at least three iterations) and the
+// gradient-descent fallback; finally v = (x - x^n) / h.  All per-element and
+// per-constraint work runs in kernels; the host only reads back scalars
+// (energies, step sizes, residual norms) to drive the loop.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+
+#include "../../include/cipc.h"
+#include "cipc_util.h"
+#include "constraint_eval.cuh"
+#include "sim.h"
+#include "sim_host.h"
+#include "sim_kernels.h"
+
+namespace cipc {
+
+static inline int nblk(long long n, int bs) { return n > 0 ? (int)((n + bs - 1) / bs) : 1; }
+
+__global__ void k_axpby(int n, const double* a, double alpha, const double* d, double* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a[i] + alpha * d[i];
+}
+__global__ void k_neg(int n, const double* a, double* b)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = -a[i];
+}
+__global__ void k_velocity(int n, const double* x, const double* xn, double h, double* v)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (x[i] - xn[i]) / h;
+}
+__global__ void k_dbc_disp(int nd, const int* idx, const double* tgt, const double* x, double* disp)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nd) return;
+    const int v = idx[k];
+    for (int d = 0; d < 3; ++d) disp[3 * v + d] = tgt[3 * k + d] - x[3 * v + d];
+}
+__global__ void k_dbc_apply(int nd, const int* idx, const double* tgt, double* x)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nd) return;
+    const int v = idx[k];
+    for (int d = 0; d < 3; ++d) x[3 * v + d] = tgt[3 * k + d];
+}
+__global__ void k_sumsq(int n, const double* a, double* part)
+{
+    __shared__ double sh[256];
+    double s = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += a[i] * a[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+// d^2 - xi^2 for a constraint list
+__global__ void k_con_d2(int n, const int* kind, const int4* verts, const double* x, double xi2, double* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int4 iv = verts[i];
+    const int id[4] = {iv.x, iv.y, iv.z < 0 ? iv.x : iv.z, iv.w < 0 ? iv.x : iv.w};
+    d3 v[4];
+    for (int q = 0; q < 4; ++q) v[q] = ld(x, id[q]);
+    out[i] = con_d2(kind[i], v) - xi2;
+}
+// flag = 1 if some previous constraint had d2 < 1e-18 and shrank (IMPLICIT_EULER.h:566-580)
+__global__ void k_kappa_flag(int n, const int* kind, const int4* verts, const double* prev, const double* x, double xi2,
+                             unsigned long long* flag)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int4 iv = verts[i];
+    const int id[4] = {iv.x, iv.y, iv.z < 0 ? iv.x : iv.z, iv.w < 0 ? iv.x : iv.w};
+    d3 v[4];
+    for (int q = 0; q < 4; ++q) v[q] = ld(x, id[q]);
+    const double cur = con_d2(kind[i], v) - xi2;
+    if (prev[i] < 1e-18 && cur < prev[i]) *flag = 1;
+}
+
+// energy of the incremental potential at x (FP64).  *ok = false when some
+// constraint distance is at or below the offset.
+static int eval_energy(Sim* s, const double* x, double* E, bool* ok)
+{
+    const int worst = nblk(s->nv, 256) + nblk(s->nt, 128) + nblk(s->nh, 128) +
+                      (s->prm.withCollision ? nblk(s->ncon, 128) + nblk(s->nfric, 128) : 0) + 16;
+    if ((int)s->red.n < worst + 16) {
+        cudaStreamSynchronize(s->stream);
+        if (s->red.alloc(2 * worst + 64) != cudaSuccess) return set_error(CIPC_ERR_CUDA, "reduction buffer");
+    }
+    double* red = s->red.p;
+    double* out = red + s->red.n - 2;  // [E, flag]
+    cudaMemsetAsync(out, 0, 2 * sizeof(double), s->stream);
+    int n = elastic_energy_partials(s, x, red);
+    if (s->prm.withCollision) {
+        n += contact_energy_partials(s, x, red + n, out + 1);
+        if (s->prm.mu > 0) n += friction_energy_partials(s, x, red + n);
+    }
+    sum_partials(s, red, n, out);
+    double h[2];
+    cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, s->stream);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return set_cuda_error(e, "energy");
+    *E = h[0];
+    *ok = h[1] == 0;
+    return CIPC_OK;
+}
+
+// gradient (DBC rows zeroed) and, optionally, the Hessian with its preconditioner diagonal
+static void eval_grad_hess(Sim* s, const double* x, double* g, bool want_h)
+{
+    if (want_h) cudaMemsetAsync(s->pdiag.p, 0, 9 * sizeof(double) * (size_t)s->nv, s->stream);
+    elastic_grad_hess(s, x, g, want_h);
+    if (s->prm.withCollision) {
+        contact_grad_hess(s, x, g, want_h);
+        if (s->prm.mu > 0) friction_grad_hess(s, x, g, want_h);
+    }
+    zero_dbc(s, g);
+}
+
+static double sum_sq(Sim* s, const double* a, int n)
+{
+    double* part = s->red.p;
+    k_sumsq<<<64, 256, 0, s->stream>>>(n, a, part);
+    double h[64];
+    cudaMemcpyAsync(h, part, sizeof(h), cudaMemcpyDeviceToHost, s->stream);
+    cudaStreamSynchronize(s->stream);
+    double t = 0;
+    for (double v : h) t += v;
+    return t;
+}
+
+static int min_d2(Sim* s, const double* x, double* out)
+{
+    double* dev = s->red.p + s->red.n - 3;
+    min_dist2_partials(s, x, dev);
+    cudaMemcpyAsync(out, dev, sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    return e == cudaSuccess ? CIPC_OK : set_cuda_error(e, "min distance");
+}
+
+static void save_prev(Sim* s, const double* x)
+{
+    s->npcon = s->ncon;
+    if (s->ncon == 0) return;
+    s->pkind.alloc(s->ncon);
+    s->pverts.alloc(s->ncon);
+    s->pd2.alloc(s->ncon);
+    cudaMemcpyAsync(s->pkind.p, s->ckind.p, sizeof(int) * s->ncon, cudaMemcpyDeviceToDevice, s->stream);
+    cudaMemcpyAsync(s->pverts.p, s->cverts.p, sizeof(int4) * s->ncon, cudaMemcpyDeviceToDevice, s->stream);
+    k_con_d2<<<nblk(s->ncon, 256), 256, 0, s->stream>>>(s->ncon, s->ckind.p, s->cverts.p, x,
+                                                        s->prm.xi * s->prm.xi, s->pd2.p);
+}
+
+int sim_step(Sim* s, StepStats* st)
+{
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
+    StepStats S;
+    const SimParams& P = s->prm;
+    const int nv = s->nv, n3 = 3 * nv, nd = (int)s->dbc_idx_h.size();
+    cudaStream_t str = s->stream;
+    int rc = CIPC_OK;
+    cudaMemcpyAsync(s->xn.p, s->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
+    launch_xtilde(s);
+    // Dirichlet step (IMPLICIT_EULER.h:304-401)
+    if (nd > 0) {
+        cudaMemsetAsync(s->disp.p, 0, sizeof(double) * n3, str);
+        k_dbc_disp<<<nblk(nd, 128), 128, 0, str>>>(nd, s->dbc_idx.p, s->dbc_tgt.p, s->x.p, s->disp.p);
+        double dbcAlpha = 1.0;
+        if (P.withCollision) {
+            rc = ccd_step_size(s, s->x.p, s->disp.p, 1.0, &dbcAlpha);
+            if (rc) return rc;
+        }
+        if (dbcAlpha != 1.0) {
+            S.status = -2;
+            *st = S;
+            return set_error(CIPC_ERR_NOT_CONVERGED,
+                             "Dirichlet motion blocked by contact (alpha %g); the penalty path is not supported",
+                             dbcAlpha);
+        }
+        k_dbc_apply<<<nblk(nd, 128), 128, 0, str>>>(nd, s->dbc_idx.p, s->dbc_tgt.p, s->x.p);
+    }
+    s->ncon = 0;
+    s->nfric = 0;
+    s->npcon = 0;
+    if (P.withCollision) {
+        if ((rc = build_constraints(s, s->x.p))) return rc;
+        if (P.mu > 0 && (rc = friction_basis(s, s->x.p))) return rc;
+    }
+    double Eprev;
+    bool ok;
+    if ((rc = eval_energy(s, s->x.p, &Eprev, &ok))) return rc;
+    std::deque<double> res;
+    int fricIterI = 0, it = 0;
+    bool useGD = false;
+    double L2 = 0;
+    do {
+        if (it >= P.maxIter) {
+            S.status = -1;
+            rc = set_error(CIPC_ERR_NOT_CONVERGED, "Newton iteration cap %d reached", P.maxIter);
+            break;
+        }
+        eval_grad_hess(s, s->x.p, s->g.p, !useGD);
+        k_neg<<<nblk(n3, 256), 256, 0, str>>>(n3, s->g.p, s->rhs.p);
+        if (useGD) {
+            cudaMemcpyAsync(s->dir.p, s->rhs.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
+        } else {
+            int pit = 0;
+            const int lr = linear_solve(s, s->rhs.p, s->dir.p, &pit);
+            S.pcg_iters += pit;
+            if (lr == CIPC_ERR_NAN) {
+                useGD = true;
+                cudaMemcpyAsync(s->dir.p, s->rhs.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
+            } else if (lr != CIPC_OK && lr != CIPC_ERR_NOT_CONVERGED) {
+                return lr;
+            }
+        }
+        // line search (IMPLICIT_EULER.h:9-149)
+        cudaMemcpyAsync(s->xprev.p, s->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
+        double alpha = 1.0;
+        if (P.withCollision && (rc = ccd_step_size(s, s->xprev.p, s->dir.p, 1.0, &alpha))) return rc;
+        const double feasible = alpha;
+        double E = Eprev;
+        int trials = 0;
+        do {
+            if (++trials > 200) {
+                S.status = -3;
+                return set_error(CIPC_ERR_NOT_CONVERGED, "line search did not find a decrease");
+            }
+            k_axpby<<<nblk(n3, 256), 256, 0, str>>>(n3, s->xprev.p, alpha, s->dir.p, s->x.p);
+            if (P.withCollision) {
+                if ((rc = build_constraints(s, s->x.p))) return rc;
+                if (s->ncon > 0) {
+                    double md;
+                    if ((rc = min_d2(s, s->x.p, &md))) return rc;
+                    if (md <= 0) {
+                        alpha /= 2;
+                        E = Eprev + 1;
+                        ok = true;
+                        continue;
+                    }
+                }
+            }
+            if ((rc = eval_energy(s, s->x.p, &E, &ok))) return rc;
+            alpha /= 2;
+        } while (E > Eprev || !ok);
+        S.line_search_trials += trials;
+        Eprev = E;
+        // barrier stiffness update (IMPLICIT_EULER.h:566-595)
+        if (s->npcon > 0) {
+            unsigned long long* flag = s->cnt.p + 32;
+            cudaMemsetAsync(flag, 0, sizeof(unsigned long long), str);
+            k_kappa_flag<<<nblk(s->npcon, 256), 256, 0, str>>>(s->npcon, s->pkind.p, s->pverts.p, s->pd2.p, s->x.p,
+                                                               P.xi * P.xi, flag);
+            unsigned long long hf = 0;
+            cudaMemcpyAsync(&hf, flag, sizeof(hf), cudaMemcpyDeviceToHost, str);
+            cudaStreamSynchronize(str);
+            if (hf && s->kappa < s->kappa_max) {
+                s->kappa *= 2;
+                if ((rc = eval_energy(s, s->x.p, &Eprev, &ok))) return rc;
+            }
+        }
+        save_prev(s, s->x.p);
+        // convergence (IMPLICIT_EULER.h:647-710)
+        L2 = std::sqrt(sum_sq(s, s->dir.p, n3) / (nv - nd)) / P.h;
+        ++it;
+        res.push_back(L2);
+        if (res.size() > 3) res.pop_front();
+        const double cur = L2;
+        L2 = *std::max_element(res.begin(), res.end());
+        if (useGD) L2 = P.tol * 10;
+        if (alpha * 2 < 1e-8 && feasible > 1e-8) {
+            if (!useGD) {
+                if (cur < P.tol) res.assign(3, cur);
+                else useGD = true;
+            }
+        } else {
+            useGD = false;
+        }
+        if (res.size() == 3 && L2 <= P.tol) {
+            ++fricIterI;
+            if ((fricIterI < P.fricIterAmt || P.fricIterAmt <= 0) && P.withCollision && P.mu > 0) {
+                if ((rc = friction_basis(s, s->x.p))) return rc;
+                eval_grad_hess(s, s->x.p, s->g.p, true);
+                k_neg<<<nblk(n3, 256), 256, 0, str>>>(n3, s->g.p, s->rhs.p);
+                int pit = 0;
+                const int lr = linear_solve(s, s->rhs.p, s->dir.p, &pit);
+                S.pcg_iters += pit;
+                if (lr != CIPC_OK && lr != CIPC_ERR_NOT_CONVERGED) return lr;
+                L2 = std::sqrt(sum_sq(s, s->dir.p, n3) / (nv - nd)) / P.h;
+                if (L2 > P.tol && (rc = eval_energy(s, s->x.p, &Eprev, &ok))) return rc;
+            }
+        }
+    } while (res.size() < 3 || L2 > P.tol);
+    k_velocity<<<nblk(n3, 256), 256, 0, str>>>(n3, s->x.p, s->xn.p, P.h, s->v.p);
+    S.newton_iters = it;
+    S.n_constraints = s->ncon;
+    if (s->ncon > 0) min_d2(s, s->x.p, &S.min_dist2);
+    S.kappa = s->kappa;
+    cudaError_t e = cudaStreamSynchronize(str);
+    if (e != cudaSuccess) return set_cuda_error(e, "step");
+    S.ms = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+    *st = S;
+    return rc;
+}
+
+void sim_destroy(Sim* s)
+{
+    if (!s) return;
+    cudaStreamSynchronize(s->stream);
+    for (DBuf<int>* b : {&s->tri, &s->hinge, &s->bnode, &s->bedge, &s->btri, &s->dbc_idx, &s->row_ptr, &s->col,
+                         &s->diag, &s->tri_slot, &s->hinge_slot, &s->ckind, &s->cmult, &s->fkind, &s->fmult,
+                         &s->pkind})
+        b->release();
+    for (DBuf<double>* b : {&s->P, &s->vol, &s->hinfo, &s->mass, &s->b, &s->X0, &s->dbc_tgt, &s->x, &s->xn, &s->xt,
+                            &s->v, &s->g, &s->dir, &s->xprev, &s->rhs, &s->disp, &s->fw, &s->fT, &s->flam, &s->pdiag,
+                            &s->red, &s->pd2})
+        b->release();
+    s->dbc.release();
+    s->hval.release();
+    s->chess.release();
+    s->fhess.release();
+    s->pinv.release();
+    s->scratch.release();
+    s->cnt.release();
+    s->cverts.release();
+    s->fverts.release();
+    s->pverts.release();
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+}  // namespace cipc
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+using namespace cipc;
+
+struct cipc_sim {
+    Sim* s;
+};
+
+static int check_sim(cipc_sim* h)
+{
+    if (!h || !h->s) return set_error(CIPC_ERR_INVALID_ARG, "null simulation handle");
+    return CIPC_OK;
+}
+
+extern "C" int cipc_sim_create(int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
+                               double thickness, const double* gravity, double bend_stiff_mult, int membrane_model,
+                               cipc_sim** out)
+{
+    if (!out || !gravity) return set_error(CIPC_ERR_INVALID_ARG, "cipc_sim_create: null output or gravity");
+    if (nv >= (1 << 21) - 1) return set_error(CIPC_ERR_INVALID_ARG, "cipc_sim_create: at most 2^21-2 vertices");
+    Sim* s = nullptr;
+    int rc = sim_create(&s, nv, X, nt, tri, rho, E, nu, thickness, gravity, bend_stiff_mult, membrane_model);
+    if (rc) return rc;
+    *out = new cipc_sim{s};
+    return CIPC_OK;
+}
+
+extern "C" int cipc_sim_destroy(cipc_sim* h)
+{
+    if (!h) return CIPC_OK;
+    sim_destroy(h->s);
+    delete h;
+    return CIPC_OK;
+}
+
+extern "C" int cipc_sim_init_oipc(cipc_sim* h, double dhat, double stiff_mult, double* kappa2, double* dhat2)
+{
+    if (int rc = check_sim(h)) return rc;
+    double k2[2];
+    const double d2 = oipc_kappa(h->s->host_mass, dhat, stiff_mult, k2);
+    h->s->kappa = k2[0];
+    h->s->kappa_max = k2[1];
+    if (kappa2) {
+        kappa2[0] = k2[0];
+        kappa2[1] = k2[1];
+    }
+    if (dhat2) *dhat2 = d2;
+    return CIPC_OK;
+}
+
+extern "C" int cipc_sim_set_kappa(cipc_sim* h, double kappa, double kappa_max)
+{
+    if (int rc = check_sim(h)) return rc;
+    h->s->kappa = kappa;
+    h->s->kappa_max = kappa_max;
+    return CIPC_OK;
+}
+
+extern "C" int cipc_sim_get_kappa(cipc_sim* h, double* kappa2)
+{
+    if (int rc = check_sim(h)) return rc;
+    kappa2[0] = h->s->kappa;
+    kappa2[1] = h->s->kappa_max;
+    return CIPC_OK;
+}
+
+extern "C" int cipc_sim_set_state(cipc_sim* h, const double* x, const double* v)
+{
+    if (int rc = check_sim(h)) return rc;
+    Sim* s = h->s;
+    const size_t b = sizeof(double) * 3 * s->nv;
+    if (x) cudaMemcpyAsync(s->x.p, x, b, cudaMemcpyHostToDevice, s->stream);
+    if (v) cudaMemcpyAsync(s->v.p, v, b, cudaMemcpyHostToDevice, s->stream);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    return e == cudaSuccess ? CIPC_OK : set_cuda_error(e, "cipc_sim_set_state");
+}
+
+extern "C" int cipc_sim_get_state(cipc_sim* h, double* x, double* v)
+{
+    if (int rc = check_sim(h)) return rc;
+    Sim* s = h->s;
+    const size_t b = sizeof(double) * 3 * s->nv;
+    if (x) cudaMemcpyAsync(x, s->x.p, b, cudaMemcpyDeviceToHost, s->stream);
+    if (v) cudaMemcpyAsync(v, s->v.p, b, cudaMemcpyDeviceToHost, s->stream);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    return e == cudaSuccess ? CIPC_OK : set_cuda_error(e, "cipc_sim_get_state");
+}
+
+extern "C" int cipc_sim_set_dbc(cipc_sim* h, int n, const int* idx, const double* targets)
+{
+    if (int rc = check_sim(h)) return rc;
+    Sim* s = h->s;
+    if (n < 0 || (n > 0 && (!idx || !targets))) return set_error(CIPC_ERR_INVALID_ARG, "cipc_sim_set_dbc: bad arrays");
+    for (int k = 0; k < n; ++k)
+        if (idx[k] < 0 || idx[k] >= s->nv) return set_error(CIPC_ERR_INDEX_RANGE, "cipc_sim_set_dbc: vertex index");
+    s->dbc_idx_h.assign(idx, idx + n);
+    std::vector<uint8_t> mask(s->nv, 0);
+    for (int k = 0; k < n; ++k) mask[idx[k]] = 1;
+    cudaError_t e = cudaMemcpyAsync(s->dbc.p, mask.data(), s->nv, cudaMemcpyHostToDevice, s->stream);
+    if (n > 0) {
+        if (s->dbc_idx.alloc(n) || s->dbc_tgt.alloc(3 * (size_t)n)) return set_error(CIPC_ERR_CUDA, "dbc buffers");
+        cudaMemcpyAsync(s->dbc_idx.p, idx, sizeof(int) * n, cudaMemcpyHostToDevice, s->stream);
+        cudaMemcpyAsync(s->dbc_tgt.p, targets, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    return e == cudaSuccess ? CIPC_OK : set_cuda_error(e, "cipc_sim_set_dbc");
+}
+
+static void to_params(const cipc_step_params* p, SimParams& q)
+{
+    q.h = p->h;
+    q.dHat2 = p->dhat2;
+    q.xi = p->xi;
+    q.mu = p->mu;
+    q.epsv2 = p->epsv2;
+    q.fricIterAmt = p->fric_iters;
+    q.tol = p->newton_tol;
+    q.withCollision = p->with_collision;
+    q.maxIter = p->max_newton_iters > 0 ? p->max_newton_iters : 200;
+    q.precision = p->precision;
+    q.pcg_tol = p->pcg_tol > 0 ? p->pcg_tol : 1e-6;
+    q.pcg_maxit = p->pcg_max_iters > 0 ? p->pcg_max_iters : 10000;
+    q.precond = p->preconditioner;
+}
+
+extern "C" int cipc_sim_step(cipc_sim* h, const cipc_step_params* p, cipc_step_stats* stats)
+{
+    if (int rc = check_sim(h)) return rc;
+    if (!p || !(p->h > 0) || !(p->dhat2 > 0) || !(p->xi >= 0) || !(p->newton_tol > 0) ||
+        (p->precision != CIPC_PRECISION_FP64 && p->precision != CIPC_PRECISION_MIXED))
+        return set_error(CIPC_ERR_INVALID_ARG, "cipc_sim_step: bad parameters");
+    Sim* s = h->s;
+    const int old_prec = s->prm.precision;
+    to_params(p, s->prm);
+    if (old_prec != s->prm.precision) s->hval.alloc(9 * sizeof(double) * (size_t)s->nnzb);
+    StepStats S;
+    const int rc = sim_step(s, &S);
+    if (stats) {
+        stats->newton_iters = S.newton_iters;
+        stats->pcg_iters = S.pcg_iters;
+        stats->line_search_trials = S.line_search_trials;
+        stats->n_constraints = S.n_constraints;
+        stats->status = S.status;
+        stats->min_dist2 = S.min_dist2;
+        stats->kappa = S.kappa;
+        stats->ms = S.ms;
+    }
+    return rc;
+}
+
+extern "C" int cipc_sim_constraints(cipc_sim* h, const cipc_step_params* p, const double* x, int cap, int* out6,
+                                    int* count)
+{
+    if (int rc = check_sim(h)) return rc;
+    Sim* s = h->s;
+    to_params(p, s->prm);
+    cudaMemcpyAsync(s->xprev.p, x, sizeof(double) * 3 * s->nv, cudaMemcpyHostToDevice, s->stream);
+    int rc = build_constraints(s, s->xprev.p);
+    if (rc) return rc;
+    *count = s->ncon;
+    const int n = std::min(cap, s->ncon);
+    std::vector<int> k(n), m(n);
+    std::vector<int4> v(n);
+    if (n > 0) {
+        cudaMemcpy(k.data(), s->ckind.p, sizeof(int) * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(m.data(), s->cmult.p, sizeof(int) * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(v.data(), s->cverts.p, sizeof(int4) * n, cudaMemcpyDeviceToHost);
+    }
+    for (int i = 0; i < n; ++i) {
+        out6[6 * i] = k[i];
+        out6[6 * i + 1] = v[i].x;
+        out6[6 * i + 2] = v[i].y;
+        out6[6 * i + 3] = v[i].z;
+        out6[6 * i + 4] = v[i].w;
+        out6[6 * i + 5] = m[i];
+    }
+    return CIPC_OK;
+}
+
+extern "C" int cipc_sim_eval(cipc_sim* h, const cipc_step_params* p, const double* x, const double* xtilde,
+                             double* energy, double* grad)
+{
+    if (int rc = check_sim(h)) return rc;
+    Sim* s = h->s;
+    to_params(p, s->prm);
+    const size_t b = sizeof(double) * 3 * s->nv;
+    cudaMemcpyAsync(s->xprev.p, x, b, cudaMemcpyHostToDevice, s->stream);
+    cudaMemcpyAsync(s->xt.p, xtilde, b, cudaMemcpyHostToDevice, s->stream);
+    s->nfric = 0;
+    int rc = CIPC_OK;
+    if (p->with_collision && (rc = build_constraints(s, s->xprev.p))) return rc;
+    bool ok = true;
+    if ((rc = eval_energy(s, s->xprev.p, energy, &ok))) return rc;
+    if (!ok) *energy = NAN;
+    if (grad) {
+        eval_grad_hess(s, s->xprev.p, s->g.p, false);
+        cudaMemcpyAsync(grad, s->g.p, b, cudaMemcpyDeviceToHost, s->stream);
+    }
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    return e == cudaSuccess ? CIPC_OK : set_cuda_error(e, "cipc_sim_eval");
+}
+
+extern "C" int cipc_sim_ccd(cipc_sim* h, const cipc_step_params* p, const double* x, const double* dir, double alpha,
+                            double* alpha_out)
+{
+    if (int rc = check_sim(h)) return rc;
+    Sim* s = h->s;
+    to_params(p, s->prm);
+    const size_t b = sizeof(double) * 3 * s->nv;
+    cudaMemcpyAsync(s->xprev.p, x, b, cudaMemcpyHostToDevice, s->stream);
+    cudaMemcpyAsync(s->disp.p, dir, b, cudaMemcpyHostToDevice, s->stream);
+    return ccd_step_size(s, s->xprev.p, s->disp.p, alpha, alpha_out);
+}

@@ -113,3 +113,101 @@ def pair_bytes(types, fp64_hessian=False):
     hb = 8 if fp64_hessian else 4
     bar = (17 + nv * 24 + np.where(types == EE, 96, 0) + 8 + nv * 24 + m * (m + 1) // 2 * hb).sum()
     return int(ccd), int(bar)
+
+
+# ---------------------------------------------------------------------------
+# Shell scenes
+# ---------------------------------------------------------------------------
+def cloth_grid(n, m, size_x, size_z, y=0.0, origin=(0.0, 0.0)):
+    """n x m vertex grid in the plane y = const with the connectivity of the
+    reference's mat_gen.py: quad (i, j) -> triangles (i,j)(i+1,j)(i,j+1) and
+    (i+1,j+1)(i,j+1)(i+1,j), vertex index i*m + j."""
+    i, j = np.meshgrid(np.arange(n), np.arange(m), indexing="ij")
+    X = np.stack([origin[0] + i.ravel() * size_x / (n - 1), np.full(n * m, float(y)),
+                  origin[1] + j.ravel() * size_z / (m - 1)], 1)
+    idx = lambda r, c: r * m + c
+    ii, jj = np.meshgrid(np.arange(n - 1), np.arange(m - 1), indexing="ij")
+    ii, jj = ii.ravel(), jj.ravel()
+    t1 = np.stack([idx(ii, jj), idx(ii + 1, jj), idx(ii, jj + 1)], 1)
+    t2 = np.stack([idx(ii + 1, jj + 1), idx(ii, jj + 1), idx(ii + 1, jj)], 1)
+    T = np.stack([t1, t2], 1).reshape(-1, 3)
+    return X, T.astype(np.int32)
+
+
+def box_shell(size, center, nsub=2):
+    """Closed box surface (edge length `size`) with each face split into
+    nsub x nsub quads, two triangles each, outward normals."""
+    c = np.asarray(center, float)
+    h = size / 2.0
+    verts = {}
+    tris = []
+
+    def vid(p):
+        key = tuple(np.round(p, 12))
+        if key not in verts:
+            verts[key] = len(verts)
+        return verts[key]
+
+    for axis in range(3):
+        for sgn in (-1.0, 1.0):
+            u_ax, v_ax = [a for a in range(3) if a != axis]
+            for a in range(nsub):
+                for b in range(nsub):
+                    q = []
+                    for (da, db) in ((0, 0), (1, 0), (1, 1), (0, 1)):
+                        p = np.zeros(3)
+                        p[axis] = sgn * h
+                        p[u_ax] = -h + (a + da) * size / nsub
+                        p[v_ax] = -h + (b + db) * size / nsub
+                        q.append(vid(p + c))
+                    # orientation so that the normal points outward
+                    flip = (sgn > 0) == ((axis + 1) % 3 == u_ax)
+                    if flip:
+                        tris += [[q[0], q[1], q[2]], [q[0], q[2], q[3]]]
+                    else:
+                        tris += [[q[0], q[2], q[1]], [q[0], q[3], q[2]]]
+    X = np.zeros((len(verts), 3))
+    for k, i in verts.items():
+        X[i] = k
+    return X, np.array(tris, np.int32)
+
+
+def icosphere(radius, center, subdiv=3):
+    """Geodesic sphere from a subdivided icosahedron (outward normals)."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    V = [[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+         [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]]
+    V = [np.array(v, float) / np.linalg.norm(v) for v in V]
+    F = [[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4], [11, 10, 2],
+         [10, 7, 6], [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9], [4, 9, 5], [2, 4, 11],
+         [6, 2, 10], [8, 6, 7], [9, 8, 1]]
+    for _ in range(subdiv):
+        mid = {}
+
+        def m(a, b):
+            k = (min(a, b), max(a, b))
+            if k not in mid:
+                p = V[a] + V[b]
+                V.append(p / np.linalg.norm(p))
+                mid[k] = len(V) - 1
+            return mid[k]
+
+        nf = []
+        for a, b, c in F:
+            ab, bc, ca = m(a, b), m(b, c), m(c, a)
+            nf += [[a, ab, ca], [b, bc, ab], [c, ca, bc], [ab, bc, ca]]
+        F = nf
+    X = np.array(V) * radius + np.asarray(center, float)
+    return X, np.array(F, np.int32)
+
+
+def merge_meshes(*meshes):
+    """Concatenates (X, T) meshes; returns X, T and the vertex offset of each."""
+    Xs, Ts, offs = [], [], []
+    o = 0
+    for X, T in meshes:
+        Xs.append(X)
+        Ts.append(T + o)
+        offs.append(o)
+        o += X.shape[0]
+    return np.concatenate(Xs), np.concatenate(Ts).astype(np.int32), offs

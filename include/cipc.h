@@ -104,6 +104,78 @@ int cipc_barrier_pairs(int64_t n_pairs, const uint8_t* type, const int32_t* idx,
 int cipc_encode_reference_constraint(int type, const int32_t* idx4, int mollified, int multiplicity,
                                      int32_t* code4);
 
+/* ------------------------------------------------------------------------
+ * Shell simulation: one implicit-Euler time step of codimensional shells with
+ * offset IPC contact and lagged friction, on one GPU.
+ * ------------------------------------------------------------------------ */
+
+/* Step parameters; the fields mirror the arguments of the reference's
+ * FEM.DiscreteShell.Advance_One_Step_IE_Hinge (Library/FEM/Shell/DISCRETE_SHELL.h:1108,
+ * IMPLICIT_EULER.h:151-187) that this path uses. */
+typedef struct cipc_step_params {
+    double h;              /* dt */
+    double dhat2;          /* dHat2 (dhat squared) */
+    double xi;             /* thickness offset of the barrier (the driver's `thickness`) */
+    double mu;             /* friction coefficient */
+    double epsv2;          /* friction smoothing epsv^2 (scaled by h^2 inside) */
+    int fric_iters;        /* fricIterAmt */
+    double newton_tol;     /* PNTol: RMS(Newton step) / h */
+    int with_collision;    /* withCollision */
+    int max_newton_iters;  /* safety cap (0 = 200) */
+    int precision;         /* CIPC_PRECISION_FP64 or CIPC_PRECISION_MIXED */
+    double pcg_tol;        /* relative residual of each Newton system (0 = 1e-6) */
+    int pcg_max_iters;     /* 0 = 10000 */
+    int preconditioner;    /* 0 block-Jacobi, 1 learned correction when a model is set */
+} cipc_step_params;
+
+typedef struct cipc_step_stats {
+    int newton_iters;       /* the reference's return value (PNIter) */
+    int pcg_iters;
+    int line_search_trials;
+    int n_constraints;
+    int status;
+    double min_dist2;       /* min over constraints of d^2 - xi^2 at the end of the step */
+    double kappa;           /* barrier stiffness after the step (kappaVec[0]) */
+    double ms;              /* wall time of the step */
+} cipc_step_stats;
+
+typedef struct cipc_sim cipc_sim;
+
+/* Creates a simulation of the shell mesh (nv vertices, nt triangles) with the
+ * reference's shell initialization (Initialize_Shell_Hinge_EIPC ->
+ * Initialize_Discrete_Shell, DISCRETE_SHELL.h:218-357): lumped mass, body force
+ * mass*gravity, inverse rest fundamental forms, hinges, plane-stress material.
+ * membrane_model: 1 Neo-Hookean (the reference's default useNH), 0 StVK. */
+int cipc_sim_create(int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
+                    double thickness, const double* gravity, double bend_stiff_mult, int membrane_model,
+                    cipc_sim** out);
+int cipc_sim_destroy(cipc_sim* sim);
+/* Offset-IPC barrier stiffness; replaces FEM.DiscreteShell.Initialize_OIPC
+ * (DISCRETE_SHELL.h:555-577, export :1103).  Writes (kappa, kappa_max) and dhat^2. */
+int cipc_sim_init_oipc(cipc_sim* sim, double dhat, double stiff_mult, double* kappa2, double* dhat2);
+int cipc_sim_set_kappa(cipc_sim* sim, double kappa, double kappa_max);
+int cipc_sim_get_kappa(cipc_sim* sim, double* kappa2);
+/* Positions / velocities, host arrays nv x 3 (either may be NULL). */
+int cipc_sim_set_state(cipc_sim* sim, const double* x, const double* v);
+int cipc_sim_get_state(cipc_sim* sim, double* x, double* v);
+/* Dirichlet vertices and their targets for the next step (the DBC storage of the
+ * reference, moved by FEM.Step_Dirichlet on the host). */
+int cipc_sim_set_dbc(cipc_sim* sim, int n, const int* idx, const double* targets);
+/* One time step; replaces Advance_One_Step_IE_Hinge (IMPLICIT_EULER.h:151-902).
+ * Returns CIPC_OK, or CIPC_ERR_NOT_CONVERGED when the Newton cap is reached or
+ * the Dirichlet motion is blocked by contact (stats->status -1 / -2). */
+int cipc_sim_step(cipc_sim* sim, const cipc_step_params* params, cipc_step_stats* stats);
+/* Parity entry points: the constraint set at x (rows of kind, v0..v3, multiplicity;
+ * kinds 0 PP 1 PE 2 PT 3 EE 4 mollified EE 5 mollified PE 6 mollified PP), the
+ * incremental potential and its gradient at x for a given x~, and the
+ * intersection-free step size along dir (Compute_Intersection_Free_StepSize). */
+int cipc_sim_constraints(cipc_sim* sim, const cipc_step_params* params, const double* x, int cap, int* out6,
+                         int* count);
+int cipc_sim_eval(cipc_sim* sim, const cipc_step_params* params, const double* x, const double* xtilde,
+                  double* energy, double* grad);
+int cipc_sim_ccd(cipc_sim* sim, const cipc_step_params* params, const double* x, const double* dir, double alpha,
+                 double* alpha_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -120,5 +120,90 @@ def set_threads(n):
     lib().orc_set_threads(int(n))
 
 
+class Shell:
+    """The oracle's shell scene and time step (oracle_shell.cpp)."""
+
+    def __init__(self, X, T, rho, E, nu, thickness, gravity=(0.0, -9.81, 0.0), bend_mult=1.0, nh=True):
+        L = lib()
+        L.orc_shell_create.restype = _P
+        L.orc_shell_create.argtypes = [ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_double, _P, ctypes.c_double, ctypes.c_int]
+        L.orc_shell_destroy.argtypes = [_P]
+        L.orc_shell_counts.argtypes = [_P, _P]
+        L.orc_shell_arrays.argtypes = [_P] + [_P] * 10
+        L.orc_shell_oipc.restype = ctypes.c_double
+        L.orc_shell_oipc.argtypes = [_P, ctypes.c_double, ctypes.c_double, _P]
+        L.orc_shell_constraints.restype = ctypes.c_int
+        L.orc_shell_constraints.argtypes = [_P, _P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_double, _P,
+                                            ctypes.c_int]
+        L.orc_shell_eval.restype = ctypes.c_double
+        L.orc_shell_eval.argtypes = [_P, _P, _P, _P, _P, _P, ctypes.c_int, _P, _P]
+        L.orc_shell_ccd.restype = ctypes.c_double
+        L.orc_shell_ccd.argtypes = [_P, _P, _P, ctypes.c_double, ctypes.c_double, _P, ctypes.c_int]
+        L.orc_shell_step.restype = ctypes.c_int
+        L.orc_shell_step.argtypes = [_P, _P, _P, _P, _P, _P, _P, ctypes.c_int, _P]
+        self.L = L
+        self.X = _c(X, np.float64)
+        T = _c(T, np.int32)
+        g = _c(gravity, np.float64)
+        self.h = L.orc_shell_create(self.X.shape[0], _p(self.X), T.shape[0], _p(T), rho, E, nu, thickness, _p(g),
+                                    bend_mult, 1 if nh else 0)
+        self.nv = self.X.shape[0]
+        self.dbc = np.zeros(0, np.int32)
+
+    def __del__(self):
+        try:
+            self.L.orc_shell_destroy(self.h)
+        except Exception:
+            pass
+
+    def arrays(self):
+        c = np.zeros(5, np.int32)
+        self.L.orc_shell_counts(self.h, _p(c))
+        nt, nh, nbn, nbe, nbt = [int(v) for v in c]
+        out = dict(tri=np.zeros((nt, 3), np.int32), P=np.zeros((nt, 3)), vol=np.zeros(nt),
+                   hinge=np.zeros((nh, 4), np.int32), hinfo=np.zeros((nh, 3)), mass=np.zeros(self.nv),
+                   b=np.zeros((self.nv, 3)), bnode=np.zeros(nbn, np.int32), bedge=np.zeros((nbe, 2), np.int32),
+                   scal=np.zeros(3))
+        self.L.orc_shell_arrays(self.h, *[_p(out[k]) for k in ("tri", "P", "vol", "hinge", "hinfo", "mass", "b",
+                                                               "bnode", "bedge", "scal")])
+        return out
+
+    def init_oipc(self, dhat, stiff_mult=1.0):
+        k2 = np.zeros(2)
+        d2 = self.L.orc_shell_oipc(self.h, dhat, stiff_mult, _p(k2))
+        return k2, d2
+
+    def constraints(self, x, dhat2, xi, cap=1 << 20):
+        out = np.zeros((cap, 6), np.int32)
+        n = self.L.orc_shell_constraints(self.h, _p(_c(x, np.float64)), _p(self.dbc), len(self.dbc), dhat2, xi,
+                                         _p(out), cap)
+        return out[:min(n, cap)].copy()
+
+    def eval(self, x, xtilde, dhat2, xi, kappa, h, mu=0.0, epsv2=1e-6, xbasis=None, xn=None, with_collision=True):
+        g = np.zeros((self.nv, 3))
+        prm = np.array([h, dhat2, xi, kappa, mu, epsv2, 1.0 if with_collision else 0.0])
+        xb = None if xbasis is None else _c(xbasis, np.float64)
+        xnn = _c(x if xn is None else xn, np.float64)
+        E = self.L.orc_shell_eval(self.h, _p(_c(x, np.float64)), _p(_c(xtilde, np.float64)), _p(xb), _p(xnn),
+                                  _p(self.dbc), len(self.dbc), _p(prm), _p(g))
+        return E, g
+
+    def ccd(self, x, d, alpha, xi):
+        return self.L.orc_shell_ccd(self.h, _p(_c(x, np.float64)), _p(_c(d, np.float64)), alpha, xi, _p(self.dbc),
+                                    len(self.dbc))
+
+    def step(self, x, v, kappa2, dbc_idx, dbc_tgt, h, dhat2, xi, mu=0.0, epsv2=1e-6, fric_iters=1, tol=1e-2,
+             with_collision=True, max_iter=500):
+        """Advances x, v, kappa2 in place; returns (status, stats dict)."""
+        prm = np.array([h, dhat2, xi, mu, epsv2, fric_iters, tol, 1.0 if with_collision else 0.0, max_iter], float)
+        st = np.zeros(4)
+        idx = _c(dbc_idx, np.int32)
+        tg = _c(dbc_tgt, np.float64)
+        self.dbc = idx
+        rc = self.L.orc_shell_step(self.h, _p(prm), _p(x), _p(v), _p(kappa2), _p(idx), _p(tg), len(idx), _p(st))
+        return rc, dict(newton_iters=int(st[0]), n_constraints=int(st[1]), min_dist2=st[2], gd_iters=int(st[3]))
+
+
 def num_threads():
     return lib().orc_num_threads()

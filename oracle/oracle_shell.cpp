@@ -178,13 +178,14 @@ static S dihedral(T3<S> v0, T3<S> v1, T3<S> v2, T3<S> v3)
 {
     T3<S> n1 = tcross(sub(v1, v0), sub(v2, v0));
     T3<S> n2 = tcross(sub(v2, v3), sub(v1, v3));
-    // theta = angle between n1 and n2, signed by (n2 x n1).(v1 - v2)
+    // theta = angle between n1 and n2, signed by (n2 x n1).(v1 - v2).  n2 x n1 is
+    // parallel to the hinge edge, so its signed length along the unit edge is
+    // smooth through flat hinges (|n2 x n1| is not differentiable there).
     T3<S> c = tcross(n2, n1);
-    S sn = sqrt(tdot(c, c));
+    T3<S> e = sub(v1, v2);
+    S sn = tdot(c, e) / sqrt(tdot(e, e));
     S cs = tdot(n1, n2);
-    S th = atan2(sn, cs);
-    if (val(tdot(c, sub(v1, v2))) < 0) th = (-1.0) * th;
-    return th;
+    return atan2(sn, cs);
 }
 
 static double dihedral_value(V3 v0, V3 v1, V3 v2, V3 v3)
@@ -1465,3 +1466,29 @@ int orc_shell_step(void* h, const double* params, double* x, double* v, double* 
 }
 
 }  // extern "C"
+
+extern "C" {
+// single-element checks: energy, gradient, Hessian (project = 1 applies makePD)
+double orc_membrane_elem(const double* x9, const double* P, double k, double lam, double mu, int nh, int project,
+                         double* g, double* H)
+{
+    Du xd[9], gd[9];
+    for (int i = 0; i < 9; ++i) xd[i] = dc(x9[i]);
+    membrane_grad<Du>(xd, P, k, lam, mu, nh, gd);
+    for (int i = 0; i < 9; ++i) g[i] = gd[i].v;
+    auto gf = [&](const Du* xx, Du* gg) { membrane_grad<Du>(xx, P, k, lam, mu, nh, gg); };
+    hess_from_grad<9>(x9, gf, H);
+    if (project) make_pd(9, H);
+    return membrane_energy(x9, P, k, lam, mu, nh);
+}
+
+double orc_bending_elem(const double* x12, double thetabar, double c, int project, double* g, double* H)
+{
+    bending_grad_d(x12, thetabar, c, g);
+    auto gf = [&](const Du* xx, Du* gg) { bending_grad<Du>(xx, thetabar, c, gg); };
+    hess_from_grad<12>(x12, gf, H);
+    if (project) make_pd(12, H);
+    double th = dihedral_value(ld3(x12), ld3(x12 + 3), ld3(x12 + 6), ld3(x12 + 9));
+    return c * (th - thetabar) * (th - thetabar);
+}
+}

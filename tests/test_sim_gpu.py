@@ -1,0 +1,148 @@
+"""Time-step parity: the GPU shell simulation against the CPU oracle's
+restatement of Advance_One_Step_IE_Discrete_Shell, through the C ABI.
+
+Scene: a cloth grid (reference mat_gen connectivity) falling onto a fixed box
+shell, material of the small BASELINE configuration (rho 200, E 1e5, nu 0.3,
+t 1 mm), offset xi = 1 mm, dhat = 1 mm, dt = 0.04.
+
+Bars:
+  * constraint sets at identical states: equal as sets (kind, vertices, multiplicity);
+  * incremental potential and gradient at identical states: 1e-10 relative;
+  * intersection-free step size along a direction: 1e-12 relative;
+  * positions after time steps solved to a tight Newton tolerance (1e-9) and a
+    tight PCG tolerance (1e-12): within 1e-8 of the bounding-box diagonal of the
+    oracle's direct-solve Newton;
+  * every step ends intersection free (minimum d^2 - xi^2 > 0).
+"""
+import numpy as np
+import pytest
+
+import cipc_ffi as F
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+MAT = dict(rho=200.0, E=1e5, nu=0.3, thickness=1e-3)
+XI, DHAT, DT = 1e-3, 1e-3, 0.04
+
+
+def scene(n=10, y=-0.092, nh=True):
+    cl = W.cloth_grid(n, n, 0.5, 0.5, y=y, origin=(-0.25, -0.25))
+    bx = W.box_shell(0.3, (0.0, -0.25, 0.0), nsub=2)
+    X, T, offs = W.merge_meshes(cl, bx)
+    dbc = np.arange(offs[1], X.shape[0], dtype=np.int32)
+    return X, T, dbc
+
+
+@pytest.fixture(scope="module")
+def trajectory(orc):
+    """Oracle states of the cloth falling onto the box (module-scoped)."""
+    X, T, dbc = scene()
+    sh = orc.Shell(X, T, **MAT)
+    k2, dhat2 = sh.init_oipc(DHAT)
+    x = X.copy()
+    v = np.zeros_like(X)
+    states = [x.copy()]
+    for _ in range(6):
+        rc, st = sh.step(x, v, k2, dbc, X[dbc], DT, dhat2, XI, tol=1e-2)
+        assert rc == 0
+        states.append(x.copy())
+    return dict(X=X, T=T, dbc=dbc, states=states, dhat2=dhat2, kappa=k2.copy(), shell=sh)
+
+
+def _gpu_sim(X, T, dbc, nh=True):
+    s = F.Sim(X, T, MAT["rho"], MAT["E"], MAT["nu"], MAT["thickness"], nh=nh)
+    s.set_dbc(dbc, X[dbc])
+    return s
+
+
+def _rows(c):
+    return sorted(map(tuple, c.tolist()))
+
+
+def test_constraint_sets_match(cuda, trajectory):
+    t = trajectory
+    s = _gpu_sim(t["X"], t["T"], t["dbc"])
+    prm = F.make_params(DT, t["dhat2"], XI)
+    t["shell"].dbc = t["dbc"]
+    seen = 0
+    for x in t["states"]:
+        go = _rows(t["shell"].constraints(x, t["dhat2"], XI))
+        gg = _rows(s.constraints(prm, x))
+        assert gg == go
+        seen += len(go)
+    assert seen > 0
+
+
+def test_energy_gradient_match(cuda, trajectory):
+    t = trajectory
+    s = _gpu_sim(t["X"], t["T"], t["dbc"])
+    rng = np.random.default_rng(0)
+    t["shell"].dbc = t["dbc"]
+    for nh in (True,):
+        for k, x in enumerate(t["states"]):
+            xt = x + rng.standard_normal(x.shape) * 1e-4
+            kappa = t["kappa"][0]
+            s.set_kappa(kappa, t["kappa"][1])
+            prm = F.make_params(DT, t["dhat2"], XI)
+            Eg, gg = s.eval(prm, x, xt)
+            Eo, go = t["shell"].eval(x, xt, t["dhat2"], XI, kappa, DT)
+            assert abs(Eg - Eo) <= 1e-10 * abs(Eo), (k, Eg, Eo)
+            assert np.abs(gg - go).max() <= 1e-9 * np.abs(go).max(), (k, np.abs(gg - go).max())
+
+
+def test_ccd_step_size_matches(cuda, trajectory):
+    t = trajectory
+    s = _gpu_sim(t["X"], t["T"], t["dbc"])
+    prm = F.make_params(DT, t["dhat2"], XI)
+    t["shell"].dbc = t["dbc"]
+    for k in range(len(t["states"]) - 1):
+        x = t["states"][k]
+        d = 3.0 * (t["states"][k + 1] - x)
+        d[t["dbc"]] = 0
+        ag = s.ccd(prm, x, d, 1.0)
+        ao = t["shell"].ccd(x, d, 1.0, XI)
+        assert abs(ag - ao) <= 1e-12 * max(ao, 1e-300), (k, ag, ao)
+
+
+@pytest.mark.parametrize("nh", [True, False])
+def test_steps_match_direct_solve(cuda, orc, nh):
+    X, T, dbc = scene(n=8, y=-0.095)
+    sh = orc.Shell(X, T, **MAT, nh=nh)
+    k2o, dhat2 = sh.init_oipc(DHAT)
+    s = _gpu_sim(X, T, dbc, nh=nh)
+    k2g, dhat2g = s.init_oipc(DHAT)
+    assert np.allclose(k2o, k2g, rtol=1e-12) and dhat2 == dhat2g
+    xo = X.copy()
+    vo = np.zeros_like(X)
+    prm = F.make_params(DT, dhat2, XI, newton_tol=1e-7, pcg_tol=1e-12, max_newton_iters=400)
+    diag = np.linalg.norm(X.max(0) - X.min(0))
+    for step in range(4):
+        # each step starts from the oracle's state
+        s.set_state(xo, vo)
+        s.set_kappa(k2o[0], k2o[1])
+        rc, sto = sh.step(xo, vo, k2o, dbc, X[dbc], DT, dhat2, XI, tol=1e-7, max_iter=400)
+        assert rc == 0
+        stg = s.step(prm)
+        xg, vg = s.state()
+        assert stg.min_dist2 > 0 or stg.n_constraints == 0
+        err = np.abs(xg - xo).max()
+        assert err <= 1e-8 * diag, (step, err, sto, stg.as_dict())
+
+
+def test_mixed_precision_steps(cuda):
+    """FP32 Hessians + FP32 PCG with FP64 refinement track the FP64 path."""
+    X, T, dbc = scene(n=12, y=-0.09)
+    sims = []
+    for prec in (F.FP64, F.MIXED):
+        s = _gpu_sim(X, T, dbc)
+        k2, dhat2 = s.init_oipc(DHAT)
+        sims.append((s, F.make_params(DT, dhat2, XI, newton_tol=1e-2, precision=prec, pcg_tol=1e-6)))
+    diag = np.linalg.norm(X.max(0) - X.min(0))
+    for step in range(8):
+        outs = []
+        for s, prm in sims:
+            st = s.step(prm)
+            assert st.n_constraints == 0 or st.min_dist2 > 0
+            outs.append(s.state()[0])
+        assert np.abs(outs[0] - outs[1]).max() <= 1e-3 * diag
