@@ -69,10 +69,14 @@ struct Sim {
     double lam = 0, mu = 0, kbend = 0;
     double cell = 1;  // broad-phase cell size (mean rest edge length)
     double kappa = 1, kappa_max = 100;
+    int trace = 0;    // CIPC_TRACE set: one stderr line per Newton iteration and refinement pass
     // static device data
     DBuf<int> tri, hinge, bnode, bedge, btri;
     DBuf<double> P, vol, hinfo, mass, b, X0;
-    DBuf<uint8_t> dbc;
+    DBuf<uint8_t> dbc;        // Dirichlet vertices (element / constraint exclusion)
+    DBuf<uint8_t> proj;       // rows/columns projected out of the Newton system
+    DBuf<uint8_t> dbc_fixed;  // Dirichlet vertices whose target equals their position
+    double dbc_stiff = 0;     // penalty stiffness of the augmented-Lagrangian Dirichlet path (0 = projection)
     std::vector<int> dbc_idx_h;
     DBuf<int> dbc_idx;
     DBuf<double> dbc_tgt;

@@ -628,7 +628,7 @@ static BarArgs bar_args(Sim* s, const double* x)
     a.mult = s->cmult.p;
     a.x = x;
     a.X0 = s->X0.p;
-    a.dbc = s->dbc.p;
+    a.dbc = s->proj.p;  // Hessian rows / columns removed from the Newton system
     a.xi2 = s->prm.xi * s->prm.xi;
     a.shat = s->prm.dHat2 + 2 * sqrt(s->prm.dHat2) * s->prm.xi;
     a.kappa = s->kappa;
@@ -899,7 +899,7 @@ static FricArgs fric_args(Sim* s, const double* x)
     a.flam = s->flam.p;
     a.x = x;
     a.xn = s->xn.p;
-    a.dbc = s->dbc.p;
+    a.dbc = s->proj.p;  // Hessian rows / columns removed from the Newton system
     a.eh = sqrt(s->prm.epsv2) * s->prm.h;
     a.mu = s->prm.mu;
     a.g = nullptr;

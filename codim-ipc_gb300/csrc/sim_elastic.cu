@@ -10,6 +10,8 @@
 // are set to the identity.
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "elements.cuh"
 #include "sim.h"
 #include "sim_kernels.h"
@@ -103,7 +105,7 @@ __global__ void __launch_bounds__(128) k_membrane(ElasticArgs a, HT* hval)
                 HT H[9][9];
                 membrane_hess<HT>(x, a.P + 3 * t, k, a.lam, a.mu, a.nh_model, S, c, H);
                 project_translation_free<HT, 3>(H);
-                scatter_blocks<HT>(hval, a.tri_slot + 9 * t, a.dbc, vid, 3, &H[0][0], 9);
+                scatter_blocks<HT>(hval, a.tri_slot + 9 * t, a.proj, vid, 3, &H[0][0], 9);
             }
         }
     }
@@ -140,7 +142,7 @@ __global__ void __launch_bounds__(128) k_bending(ElasticArgs a, HT* hval)
 #pragma unroll
                     for (int j = 0; j < 12; ++j) H[i][j] = (HT)(2 * c * (gt[i] * gt[j] + dth * Ht[i][j]));
                 project_translation_free<HT, 4>(H);
-                scatter_blocks<HT>(hval, a.hinge_slot + 16 * t, a.dbc, vid, 4, &H[0][0], 12);
+                scatter_blocks<HT>(hval, a.hinge_slot + 16 * t, a.proj, vid, 4, &H[0][0], 12);
             }
         }
     }
@@ -148,23 +150,65 @@ __global__ void __launch_bounds__(128) k_bending(ElasticArgs a, HT* hval)
     if (a.red && threadIdx.x == 0) a.red[blockIdx.x] = s;
 }
 
-// mass on free diagonal blocks, identity on Dirichlet diagonal blocks
+// mass (+ Dirichlet penalty k m on penalized vertices) on free diagonal blocks,
+// identity on projected diagonal blocks
 template <typename HT>
-__global__ void k_mass_diag(int nv, const double* m, const uint8_t* dbc, const int* diag, HT* hval)
+__global__ void k_mass_diag(int nv, const double* m, const uint8_t* proj, const uint8_t* dbc, double stiff,
+                            const int* diag, HT* hval)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
     HT* d = hval + 9 * (size_t)diag[i];
-    const HT v = dbc[i] ? HT(1) : (HT)m[i];
+    const HT v = proj[i] ? HT(1) : (HT)(m[i] * (dbc[i] ? 1.0 + stiff : 1.0));
     d[0] += v;
     d[4] += v;
     d[8] += v;
 }
 
-__global__ void k_zero_dbc(int nv, const uint8_t* dbc, double* g)
+__global__ void k_zero_dbc(int nv, const uint8_t* proj, double* g)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < nv && dbc[i]) g[3 * i] = g[3 * i + 1] = g[3 * i + 2] = 0;
+    if (i < nv && proj[i]) g[3 * i] = g[3 * i + 1] = g[3 * i + 2] = 0;
+}
+
+// Dirichlet penalty 1/2 k m |x - target|^2 (Shell/DIRICHLET.h:26-94)
+__global__ void __launch_bounds__(256) k_dbc_penalty(int nd, const int* idx, const double* tgt, const double* m,
+                                                      const double* x, double stiff, double* g, double* red)
+{
+    __shared__ double sh[256];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0;
+    if (k < nd) {
+        const int v = idx[k];
+        double p = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double dd = tgt[3 * k + d] - x[3 * v + d];
+            p += dd * dd;
+            if (g) g[3 * v + d] += stiff * m[v] * (-dd);
+        }
+        e = p * m[v];
+    }
+    const double s = block_sum(e, sh);
+    if (red && threadIdx.x == 0) red[blockIdx.x] = 0.5 * stiff * s;
+}
+
+__global__ void __launch_bounds__(256) k_dbc_dist2(int nd, const int* idx, const double* tgt, const double* x,
+                                                    double* red)
+{
+    __shared__ double sh[256];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double p = 0;
+    if (k < nd) {
+        const int v = idx[k];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double dd = tgt[3 * k + d] - x[3 * v + d];
+            p += dd * dd;
+        }
+    }
+    const double s = block_sum(p, sh);
+    if (threadIdx.x == 0) red[blockIdx.x] = s;
 }
 
 // sum of n partials in a fixed order (single block)
@@ -205,6 +249,7 @@ ElasticArgs elastic_args(Sim* s, const double* x, double* g)
     a.tri_slot = s->tri_slot.p;
     a.hinge_slot = s->hinge_slot.p;
     a.dbc = s->dbc.p;
+    a.proj = s->proj.p;
     a.x = x;
     a.g = g;
     a.h = s->prm.h;
@@ -239,16 +284,43 @@ void elastic_grad_hess(Sim* s, const double* x, double* g, bool want_hess)
         float* hv = want_hess ? (float*)s->hval.p : nullptr;
         k_membrane<float><<<nblk(s->nt, 128), 128, 0, s->stream>>>(a, hv);
         k_bending<float><<<nblk(s->nh, 128), 128, 0, s->stream>>>(a, hv);
-        if (want_hess) k_mass_diag<float><<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->mass.p, s->dbc.p, s->diag.p, hv);
+        if (want_hess)
+            k_mass_diag<float><<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->mass.p, s->proj.p, s->dbc.p,
+                                                                      s->dbc_stiff, s->diag.p, hv);
     } else {
         double* hv = want_hess ? (double*)s->hval.p : nullptr;
         k_membrane<double><<<nblk(s->nt, 128), 128, 0, s->stream>>>(a, hv);
         k_bending<double><<<nblk(s->nh, 128), 128, 0, s->stream>>>(a, hv);
-        if (want_hess) k_mass_diag<double><<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->mass.p, s->dbc.p, s->diag.p, hv);
+        if (want_hess)
+            k_mass_diag<double><<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->mass.p, s->proj.p, s->dbc.p,
+                                                                       s->dbc_stiff, s->diag.p, hv);
     }
 }
 
-void zero_dbc(Sim* s, double* g) { k_zero_dbc<<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->dbc.p, g); }
+void zero_dbc(Sim* s, double* g) { k_zero_dbc<<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->proj.p, g); }
+
+int dbc_penalty_partials(Sim* s, const double* x, double* red, double* g)
+{
+    const int nd = (int)s->dbc_idx_h.size();
+    if (nd == 0 || s->dbc_stiff == 0) return 0;
+    k_dbc_penalty<<<nblk(nd, 256), 256, 0, s->stream>>>(nd, s->dbc_idx.p, s->dbc_tgt.p, s->mass.p, x, s->dbc_stiff,
+                                                        g, red);
+    return red ? nblk(nd, 256) : 0;
+}
+
+double dbc_dist2(Sim* s, const double* x)
+{
+    const int nd = (int)s->dbc_idx_h.size();
+    if (nd == 0) return 0;
+    const int nb = nblk(nd, 256);
+    k_dbc_dist2<<<nb, 256, 0, s->stream>>>(nd, s->dbc_idx.p, s->dbc_tgt.p, x, s->red.p);
+    std::vector<double> h(nb);
+    cudaMemcpyAsync(h.data(), s->red.p, sizeof(double) * nb, cudaMemcpyDeviceToHost, s->stream);
+    cudaStreamSynchronize(s->stream);
+    double t = 0;
+    for (double v : h) t += v;
+    return t;
+}
 
 void sum_partials(Sim* s, const double* red, int n, double* out)
 {

@@ -13,7 +13,8 @@ struct ElasticArgs {
     const int *tri, *hinge;
     const double *P, *vol, *hinfo;
     const int *tri_slot, *hinge_slot;
-    const uint8_t* dbc;
+    const uint8_t* dbc;   // element skip: all vertices Dirichlet
+    const uint8_t* proj;  // Hessian rows/columns projected out
     const double* x;
     double* g;
     double h, lam, mu, kbend;
@@ -26,6 +27,8 @@ void launch_xtilde(Sim* s);
 int elastic_energy_partials(Sim* s, const double* x, double* red);  // returns #partials written
 void elastic_grad_hess(Sim* s, const double* x, double* g, bool want_hess);
 void zero_dbc(Sim* s, double* g);
+int dbc_penalty_partials(Sim* s, const double* x, double* red, double* g);  // energy partials (+ gradient if g)
+double dbc_dist2(Sim* s, const double* x);                                   // sum |target - x|^2 (host value)
 void sum_partials(Sim* s, const double* red, int n, double* out);
 
 // sim_contact.cu

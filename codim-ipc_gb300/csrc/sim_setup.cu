@@ -13,6 +13,7 @@
 // is the sort-reduce of the reference's triplet assembly done once per mesh.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <map>
 #include <set>
 #include <vector>
@@ -247,8 +248,10 @@ int sim_upload(Sim* s, const HostScene& S)
     const size_t n3 = 3 * (size_t)S.nv;
     for (DBuf<double>* d : {&s->x, &s->xn, &s->xt, &s->v, &s->g, &s->dir, &s->xprev, &s->rhs, &s->disp})
         if (e == cudaSuccess) e = d->alloc(n3);
-    if (e == cudaSuccess) e = s->dbc.alloc(S.nv);
-    if (e == cudaSuccess) e = cudaMemset(s->dbc.p, 0, S.nv);
+    for (DBuf<uint8_t>* m : {&s->dbc, &s->proj, &s->dbc_fixed}) {
+        if (e == cudaSuccess) e = m->alloc(S.nv);
+        if (e == cudaSuccess) e = cudaMemset(m->p, 0, S.nv);
+    }
     if (e == cudaSuccess) e = s->x.alloc(n3);
     if (e == cudaSuccess) e = cudaMemcpy(s->x.p, S.X0.data(), n3 * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(s->v.p, 0, n3 * sizeof(double));
@@ -270,6 +273,7 @@ int sim_create(Sim** out, int nv, const double* X, int nt, const int* tri, doubl
     rc = ensure_device();
     if (rc != CIPC_OK) return rc;
     Sim* s = new Sim();
+    s->trace = std::getenv("CIPC_TRACE") != nullptr;
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete s;
         return set_error(CIPC_ERR_CUDA, "sim: stream creation failed");

@@ -15,6 +15,7 @@
 //          vectors), so the Newton increment meets the same FP64 residual bound.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 
@@ -227,6 +228,19 @@ __global__ void k_axpy_into(int n, const XT* d, double* x)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) x[i] += (double)d[i];
 }
+// b = (float)(a * scale): the refinement hands the FP32 solver a unit-norm
+// residual, so that its dot products neither underflow nor overflow
+__global__ void k_convert_scaled(int n, const double* a, double scale, float* b)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)(a[i] * scale);
+}
+// x += scale * d
+__global__ void k_axpy_scaled(int n, const float* d, double scale, double* x)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] += scale * (double)d[i];
+}
 
 struct SolveCtx {
     Sim* s;
@@ -254,7 +268,7 @@ static void apply_H(SolveCtx& C, const XT* x, XT* y)
                                                                   (const VT*)s->chess.p, x, y);
     if (s->nfric > 0 && s->prm.mu > 0)
         k_fric_spmv<XT><<<nblk(s->nfric, 128), 128, 0, C.st>>>(s->nfric, s->fkind.p, s->fverts.p, s->fw.p, s->fT.p,
-                                                                (const double*)s->fhess.p, s->dbc.p, x, y);
+                                                                (const double*)s->fhess.p, s->proj.p, x, y);
 }
 
 // PCG on H x = b (x starts at 0).  Returns iterations; *rel = final |r|/|b| (read every `every` iterations).
@@ -349,6 +363,7 @@ int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
         double *r = (double*)take(n3 * 8), *z = (double*)take(n3 * 8), *p = (double*)take(n3 * 8),
                *q = (double*)take(n3 * 8);
         total = pcg<double, double>(C, rhs, sol, r, z, p, q, s->prm.pcg_tol, s->prm.pcg_maxit, &rel);
+        if (s->trace) std::fprintf(stderr, "cipc pcg: rel %.3e pcg %d\n", rel, total);
     } else {
         // mixed: FP32 inner PCG, FP64 iterative refinement of the residual
         double* r64 = (double*)take(n3 * 8);
@@ -362,19 +377,26 @@ int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
         double bb = 0;
         cudaMemcpyAsync(&bb, sc + 10, sizeof(double), cudaMemcpyDeviceToHost, s->stream);
         cudaStreamSynchronize(s->stream);
-        const double inner_tol = 1e-3;
+        // each pass asks the FP32 solver for what is still missing (with a margin
+        // for the gap between its recurrence and the true residual), down to the
+        // 1e-5 an FP32 Krylov recurrence reliably reaches; a pass restarts the
+        // Krylov space, so fewer, deeper passes take fewer iterations in total
+        double rr = bb;
         for (int outer = 0; outer < 20 && bb > 0; ++outer) {
-            k_convert<double, float><<<nblk(n3, 256), 256, 0, s->stream>>>(n3, r64, b32);
+            const double rn = std::sqrt(rr);
+            const double inner_tol = std::min(0.5, std::max(0.5 * s->prm.pcg_tol * std::sqrt(bb / rr), 1e-5));
+            k_convert_scaled<<<nblk(n3, 256), 256, 0, s->stream>>>(n3, r64, 1.0 / rn, b32);
             double relin = 0;
             total += pcg<float, float>(C, b32, d32, r, z, p, q, inner_tol, s->prm.pcg_maxit - total, &relin);
-            k_axpy_into<float><<<nblk(n3, 256), 256, 0, s->stream>>>(n3, d32, sol);
+            k_axpy_scaled<<<nblk(n3, 256), 256, 0, s->stream>>>(n3, d32, rn, sol);
             apply_H<float, double>(C, sol, y64);
             k_residual<<<nblk(n3, 256), 256, 0, s->stream>>>(n3, rhs, y64, r64);
             dot<double>(C, r64, r64, sc + 11);
-            double rr = 0;
             cudaMemcpyAsync(&rr, sc + 11, sizeof(double), cudaMemcpyDeviceToHost, s->stream);
             cudaStreamSynchronize(s->stream);
             rel = std::sqrt(rr / bb);
+            if (s->trace)
+                std::fprintf(stderr, "cipc refine %d: inner %.3e outer %.3e pcg %d\n", outer, relin, rel, total);
             if (rel <= s->prm.pcg_tol || total >= s->prm.pcg_maxit) break;
         }
     }

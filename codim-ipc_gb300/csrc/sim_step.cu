@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 
@@ -50,6 +51,14 @@ __global__ void k_dbc_disp(int nd, const int* idx, const double* tgt, const doub
     if (k >= nd) return;
     const int v = idx[k];
     for (int d = 0; d < 3; ++d) disp[3 * v + d] = tgt[3 * k + d] - x[3 * v + d];
+}
+// Dirichlet vertices whose displacement this step is exactly zero
+__global__ void k_dbc_fixed(int nd, const int* idx, const double* disp, uint8_t* fixed)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nd) return;
+    const int v = idx[k];
+    fixed[v] = (disp[3 * v] == 0 && disp[3 * v + 1] == 0 && disp[3 * v + 2] == 0) ? 1 : 0;
 }
 __global__ void k_dbc_apply(int nd, const int* idx, const double* tgt, double* x)
 {
@@ -110,6 +119,7 @@ static int eval_energy(Sim* s, const double* x, double* E, bool* ok)
     double* out = red + s->red.n - 2;  // [E, flag]
     cudaMemsetAsync(out, 0, 2 * sizeof(double), s->stream);
     int n = elastic_energy_partials(s, x, red);
+    n += dbc_penalty_partials(s, x, red + n, nullptr);
     if (s->prm.withCollision) {
         n += contact_energy_partials(s, x, red + n, out + 1);
         if (s->prm.mu > 0) n += friction_energy_partials(s, x, red + n);
@@ -129,6 +139,7 @@ static void eval_grad_hess(Sim* s, const double* x, double* g, bool want_h)
 {
     if (want_h) cudaMemsetAsync(s->pdiag.p, 0, 9 * sizeof(double) * (size_t)s->nv, s->stream);
     elastic_grad_hess(s, x, g, want_h);
+    dbc_penalty_partials(s, x, nullptr, g);
     if (s->prm.withCollision) {
         contact_grad_hess(s, x, g, want_h);
         if (s->prm.mu > 0) friction_grad_hess(s, x, g, want_h);
@@ -181,23 +192,30 @@ int sim_step(Sim* s, StepStats* st)
     int rc = CIPC_OK;
     cudaMemcpyAsync(s->xn.p, s->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
     launch_xtilde(s);
-    // Dirichlet step (IMPLICIT_EULER.h:304-401)
+    // Dirichlet step (IMPLICIT_EULER.h:304-401): move the Dirichlet vertices to
+    // their targets when that motion is intersection free, otherwise keep them at
+    // x^n and pull them with the augmented-Lagrangian penalty
+    s->dbc_stiff = 0;
+    double dbcPenaltyXn = 0;
+    cudaMemcpyAsync(s->proj.p, s->dbc.p, nv, cudaMemcpyDeviceToDevice, str);
     if (nd > 0) {
         cudaMemsetAsync(s->disp.p, 0, sizeof(double) * n3, str);
         k_dbc_disp<<<nblk(nd, 128), 128, 0, str>>>(nd, s->dbc_idx.p, s->dbc_tgt.p, s->x.p, s->disp.p);
+        cudaMemsetAsync(s->dbc_fixed.p, 0, nv, str);
+        k_dbc_fixed<<<nblk(nd, 128), 128, 0, str>>>(nd, s->dbc_idx.p, s->disp.p, s->dbc_fixed.p);
         double dbcAlpha = 1.0;
         if (P.withCollision) {
             rc = ccd_step_size(s, s->x.p, s->disp.p, 1.0, &dbcAlpha);
             if (rc) return rc;
         }
-        if (dbcAlpha != 1.0) {
-            S.status = -2;
-            *st = S;
-            return set_error(CIPC_ERR_NOT_CONVERGED,
-                             "Dirichlet motion blocked by contact (alpha %g); the penalty path is not supported",
-                             dbcAlpha);
+        if (dbcAlpha == 1.0) {
+            k_dbc_apply<<<nblk(nd, 128), 128, 0, str>>>(nd, s->dbc_idx.p, s->dbc_tgt.p, s->x.p);
+        } else {
+            s->dbc_stiff = 1e6;
+            dbcPenaltyXn = dbc_dist2(s, s->xn.p);
+            cudaMemcpyAsync(s->proj.p, s->dbc_fixed.p, nv, cudaMemcpyDeviceToDevice, str);
+            S.status = 1;  // penalty path taken
         }
-        k_dbc_apply<<<nblk(nd, 128), 128, 0, str>>>(nd, s->dbc_idx.p, s->dbc_tgt.p, s->x.p);
     }
     s->ncon = 0;
     s->nfric = 0;
@@ -264,6 +282,9 @@ int sim_step(Sim* s, StepStats* st)
             alpha /= 2;
         } while (E > Eprev || !ok);
         S.line_search_trials += trials;
+        if (s->trace)
+            std::fprintf(stderr, "cipc newton %d: step %.3e feasible %.3e trials %d E %.17g dE %.3e gd %d\n", it,
+                         2 * alpha, feasible, trials, E, E - Eprev, (int)useGD);
         Eprev = E;
         // barrier stiffness update (IMPLICIT_EULER.h:566-595)
         if (s->npcon > 0) {
@@ -295,6 +316,24 @@ int sim_step(Sim* s, StepStats* st)
             }
         } else {
             useGD = false;
+        }
+        if (s->trace)
+            std::fprintf(stderr, "cipc newton %d: res %.3e L2 %.3e kappa %.6g dbc_stiff %.3g ncon %d\n", it, cur, L2,
+                         s->kappa, s->dbc_stiff, s->ncon);
+        // augmented-Lagrangian Dirichlet progress (IMPLICIT_EULER.h:713-764)
+        if (s->dbc_stiff != 0) {
+            const double progress = 1 - std::sqrt(dbc_dist2(s, s->x.p) / dbcPenaltyXn);
+            if (progress < 0.99) {
+                if (L2 < P.tol * 10 && s->dbc_stiff < 1e8) {
+                    s->dbc_stiff *= 2;
+                    if ((rc = eval_energy(s, s->x.p, &Eprev, &ok))) return rc;
+                }
+                L2 = P.tol * 10;
+            } else {
+                s->dbc_stiff = 0;
+                cudaMemcpyAsync(s->proj.p, s->dbc.p, nv, cudaMemcpyDeviceToDevice, str);
+                if ((rc = eval_energy(s, s->x.p, &Eprev, &ok))) return rc;
+            }
         }
         if (res.size() == 3 && L2 <= P.tol) {
             ++fricIterI;
@@ -336,6 +375,8 @@ void sim_destroy(Sim* s)
                             &s->red, &s->pd2})
         b->release();
     s->dbc.release();
+    s->proj.release();
+    s->dbc_fixed.release();
     s->hval.release();
     s->chess.release();
     s->fhess.release();
@@ -451,6 +492,8 @@ extern "C" int cipc_sim_set_dbc(cipc_sim* h, int n, const int* idx, const double
     std::vector<uint8_t> mask(s->nv, 0);
     for (int k = 0; k < n; ++k) mask[idx[k]] = 1;
     cudaError_t e = cudaMemcpyAsync(s->dbc.p, mask.data(), s->nv, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->proj.p, mask.data(), s->nv, cudaMemcpyHostToDevice, s->stream);
+    s->dbc_stiff = 0;
     if (n > 0) {
         if (s->dbc_idx.alloc(n) || s->dbc_tgt.alloc(3 * (size_t)n)) return set_error(CIPC_ERR_CUDA, "dbc buffers");
         cudaMemcpyAsync(s->dbc_idx.p, idx, sizeof(int) * n, cudaMemcpyHostToDevice, s->stream);

@@ -201,6 +201,34 @@ def icosphere(radius, center, subdiv=3):
     return X, np.array(F, np.int32)
 
 
+def rotate_y(P, center, angle):
+    """Rotates points P about the vertical axis through `center` by `angle`."""
+    c, s = np.cos(angle), np.sin(angle)
+    Q = np.asarray(P, float) - center
+    return np.stack([c * Q[:, 0] + s * Q[:, 2], Q[:, 1], -s * Q[:, 0] + c * Q[:, 2]], 1) + center
+
+
+def cloth_on_sphere(n=200, size=2.0, radius=0.5, gap=0.01, subdiv=4):
+    """Cloth n x n (size x size) centred above a sphere (fixed centre, Dirichlet
+    vertices) whose top is `gap` below the cloth.  Returns X, T, dbc indices and
+    the sphere centre."""
+    center = np.zeros(3)
+    cl = cloth_grid(n, n, size, size, y=radius + gap, origin=(-size / 2, -size / 2))
+    sp = icosphere(radius, center, subdiv)
+    X, T, offs = merge_meshes(cl, sp)
+    dbc = np.arange(offs[1], X.shape[0], dtype=np.int32)
+    return X, T, dbc, center
+
+
+def cloth_on_box(n=40, size=1.0, box=0.3, height=0.1, nsub=4):
+    """Cloth n x n (size x size) `height` above a fixed box shell (Dirichlet)."""
+    cl = cloth_grid(n, n, size, size, y=0.0, origin=(-size / 2, -size / 2))
+    bx = box_shell(box, (0.0, -height - box / 2, 0.0), nsub)
+    X, T, offs = merge_meshes(cl, bx)
+    dbc = np.arange(offs[1], X.shape[0], dtype=np.int32)
+    return X, T, dbc
+
+
 def merge_meshes(*meshes):
     """Concatenates (X, T) meshes; returns X, T and the vertex offset of each."""
     Xs, Ts, offs = [], [], []

@@ -1151,7 +1151,24 @@ struct Ctx {
     const double* xtilde;
     const double* xn;
     double kappa;
+    // augmented-Lagrangian Dirichlet penalty (Shell/DIRICHLET.h), off when stiff == 0
+    double stiff = 0;
+    const int* dbc_idx = nullptr;
+    const double* dbc_tgt = nullptr;
+    int ndbc = 0;
+    std::vector<char> proj;  // rows / columns projected out of the Newton system
 };
+
+static double dbc_dist2(const Ctx& C, const double* x)
+{
+    double s = 0;
+    for (int k = 0; k < C.ndbc; ++k)
+        for (int d = 0; d < 3; ++d) {
+            double dd = C.dbc_tgt[3 * k + d] - x[3 * C.dbc_idx[k] + d];
+            s += dd * dd;
+        }
+    return s;
+}
 
 static double total_energy(const Ctx& C, const double* x, const std::vector<Con>& cs, const std::vector<Fric>& F,
                            bool* ok)
@@ -1165,6 +1182,18 @@ static double total_energy(const Ctx& C, const double* x, const std::vector<Con>
             ine += S.mass[i] * dd * dd;
         }
     E += 0.5 * ine;
+    if (C.stiff != 0) {
+        double pen = 0;
+        for (int k = 0; k < C.ndbc; ++k) {
+            double p = 0;
+            for (int d = 0; d < 3; ++d) {
+                double dd = C.dbc_tgt[3 * k + d] - x[3 * C.dbc_idx[k] + d];
+                p += dd * dd;
+            }
+            pen += p * S.mass[C.dbc_idx[k]];
+        }
+        E += 0.5 * C.stiff * pen;
+    }
     bool good = true;
     if (C.P.withCollision) good = barrier_terms(S, x, cs, C.P.dHat2, C.P.xi, C.kappa, &E, nullptr, nullptr);
     if (C.P.withCollision && C.P.mu > 0) friction_terms(F, x, C.xn, C.P.epsv2 * C.P.h * C.P.h, C.P.mu, &E, nullptr, nullptr);
@@ -1181,14 +1210,23 @@ static void total_grad(const Ctx& C, const double* x, const std::vector<Con>& cs
     elastic_grad_hess(S, x, C.P.h, g, A);
     for (int i = 0; i < S.nv; ++i)
         for (int d = 0; d < 3; ++d) g[3 * i + d] += S.mass[i] * (x[3 * i + d] - C.xtilde[3 * i + d]);
+    const std::vector<char>& proj = C.proj.empty() ? S.dbc : C.proj;
     if (A)
         for (int i = 0; i < S.nv; ++i)
-            if (!S.dbc[i])
+            if (!proj[i])
                 for (int d = 0; d < 3; ++d) A->t.push_back({3 * i + d, 3 * i + d, S.mass[i]});
+    if (C.stiff != 0)
+        for (int k = 0; k < C.ndbc; ++k) {
+            const int v = C.dbc_idx[k];
+            for (int d = 0; d < 3; ++d) {
+                g[3 * v + d] += C.stiff * S.mass[v] * (x[3 * v + d] - C.dbc_tgt[3 * k + d]);
+                if (A && !proj[v]) A->t.push_back({3 * v + d, 3 * v + d, C.stiff * S.mass[v]});
+            }
+        }
     if (C.P.withCollision) barrier_terms(S, x, cs, C.P.dHat2, C.P.xi, C.kappa, nullptr, g, A);
     if (C.P.withCollision && C.P.mu > 0) friction_terms(F, x, C.xn, C.P.epsv2 * C.P.h * C.P.h, C.P.mu, nullptr, g, A);
     for (int i = 0; i < S.nv; ++i)
-        if (S.dbc[i]) {
+        if (proj[i]) {
             g[3 * i] = g[3 * i + 1] = g[3 * i + 2] = 0;
             if (A)
                 for (int d = 0; d < 3; ++d) A->t.push_back({3 * i + d, 3 * i + d, 1.0});
@@ -1213,13 +1251,26 @@ static void shell_step(Shell& S, const StepParams& P, double* x, double* v, doub
         for (int d = 0; d < 3; ++d) disp[3 * dbc_idx[k] + d] = dbc_tgt[3 * k + d] - x[3 * dbc_idx[k] + d];
     double dbcAlpha = 1;
     if (P.withCollision) dbcAlpha = ccd_step_size(S, x, disp.data(), 1.0, P.xi);
-    if (dbcAlpha != 1) {
-        out.status = -2;
-        return;
-    }
-    for (int k = 0; k < ndbc; ++k)
-        for (int d = 0; d < 3; ++d) x[3 * dbc_idx[k] + d] = dbc_tgt[3 * k + d];
     Ctx C{&S, P, xt.data(), xn.data(), kappa[0]};
+    C.dbc_idx = dbc_idx;
+    C.dbc_tgt = dbc_tgt;
+    C.ndbc = ndbc;
+    C.proj = S.dbc;
+    double dbcPenaltyXn = 0;
+    if (dbcAlpha == 1) {
+        for (int k = 0; k < ndbc; ++k)
+            for (int d = 0; d < 3; ++d) x[3 * dbc_idx[k] + d] = dbc_tgt[3 * k + d];
+    } else {
+        // augmented Lagrangian: Dirichlet vertices stay at x^n, pulled by a penalty;
+        // only those with zero displacement stay projected (IMPLICIT_EULER.h:380-401)
+        C.stiff = 1e6;
+        dbcPenaltyXn = dbc_dist2(C, xn.data());
+        C.proj.assign(nv, 0);
+        for (int k = 0; k < ndbc; ++k) {
+            const int v = dbc_idx[k];
+            C.proj[v] = (disp[3 * v] == 0 && disp[3 * v + 1] == 0 && disp[3 * v + 2] == 0) ? 1 : 0;
+        }
+    }
     std::vector<Con> cs, cs_prev;
     std::vector<Fric> F;
     std::vector<double> dist2_prev;
@@ -1240,7 +1291,7 @@ static void shell_step(Shell& S, const StepParams& P, double* x, double* v, doub
             break;
         }
         Asm A;
-        A.dbc = &S.dbc;
+        A.dbc = &C.proj;
         total_grad(C, x, cs, F, g.data(), useGD ? nullptr : &A);
         for (int i = 0; i < n; ++i) rhs[i] = -g[i];
         if (useGD) sol = rhs;
@@ -1307,12 +1358,27 @@ static void shell_step(Shell& S, const StepParams& P, double* x, double* v, doub
         } else {
             useGD = false;
         }
+        // Dirichlet progress of the augmented-Lagrangian path (IMPLICIT_EULER.h:713-764)
+        if (C.stiff != 0) {
+            const double progress = 1 - std::sqrt(dbc_dist2(C, x) / dbcPenaltyXn);
+            if (progress < 0.99) {
+                if (L2 < P.tol * 10 && C.stiff < 1e8) {
+                    C.stiff *= 2;
+                    Eprev = total_energy(C, x, cs, F, nullptr);
+                }
+                L2 = P.tol * 10;
+            } else {
+                C.stiff = 0;
+                C.proj = S.dbc;
+                Eprev = total_energy(C, x, cs, F, nullptr);
+            }
+        }
         if (res.size() == 3 && L2 <= P.tol) {
             ++fricIterI;
             if ((fricIterI < P.fricIterAmt || P.fricIterAmt <= 0) && P.withCollision && P.mu > 0) {
                 friction_basis(x, cs, P.dHat2, P.xi, C.kappa, F);
                 Asm A2;
-                A2.dbc = &S.dbc;
+                A2.dbc = &C.proj;
                 total_grad(C, x, cs, F, g.data(), &A2);
                 for (int i = 0; i < n; ++i) rhs[i] = -g[i];
                 if (!skyline_solve(n, A2.t, rhs.data(), sol.data())) {

@@ -9,9 +9,9 @@ Bars:
   * constraint sets at identical states: equal as sets (kind, vertices, multiplicity);
   * incremental potential and gradient at identical states: 1e-10 relative;
   * intersection-free step size along a direction: 1e-12 relative;
-  * positions after time steps solved to a tight Newton tolerance (1e-9) and a
+  * positions after time steps solved to a tight Newton tolerance (1e-7) and a
     tight PCG tolerance (1e-12): within 1e-8 of the bounding-box diagonal of the
-    oracle's direct-solve Newton;
+    oracle's direct-solve Newton (1e-7 on the augmented-Lagrangian Dirichlet path);
   * every step ends intersection free (minimum d^2 - xi^2 > 0).
 """
 import numpy as np
@@ -134,7 +134,11 @@ def test_steps_match_direct_solve(cuda, orc, nh):
 def test_mixed_precision_step_parity(cuda):
     """FP32 Hessians + FP32 PCG inside FP64 refinement reach the same Newton fixed
     point as the FP64 path (the gradient stays FP64): per step from identical
-    states at a tight tolerance, within 1e-8 of the bounding-box diagonal."""
+    states at a tight tolerance.  The two Newton loops stop at different
+    iterates: each stops once the RMS Newton step over its last three iterations
+    is at most tol * h, and a Newton step is the distance to the fixed point up
+    to second order, so the largest per-vertex difference is bounded by
+    2 * sqrt(free vertices) * tol * h."""
     X, T, dbc = scene(n=12, y=-0.093)
     sims = []
     for prec in (F.FP64, F.MIXED):
@@ -142,7 +146,7 @@ def test_mixed_precision_step_parity(cuda):
         k2, dhat2 = s.init_oipc(DHAT)
         sims.append((s, F.make_params(DT, dhat2, XI, newton_tol=1e-7, precision=prec, pcg_tol=1e-12,
                                       max_newton_iters=400)))
-    diag = np.linalg.norm(X.max(0) - X.min(0))
+    bar = 2 * np.sqrt(X.shape[0] - len(dbc)) * 1e-7 * DT
     ref, mix = sims
     for step in range(4):
         x0, v0 = ref[0].state()
@@ -153,7 +157,7 @@ def test_mixed_precision_step_parity(cuda):
         st_m = mix[0].step(mix[1])
         xr, xm = ref[0].state()[0], mix[0].state()[0]
         assert st_m.n_constraints == 0 or st_m.min_dist2 > 0
-        assert np.abs(xr - xm).max() <= 1e-8 * diag, (step, np.abs(xr - xm).max(), st_r.as_dict(), st_m.as_dict())
+        assert np.abs(xr - xm).max() <= bar, (step, np.abs(xr - xm).max(), st_r.as_dict(), st_m.as_dict())
 
 
 def test_mixed_precision_trajectory(cuda):
@@ -172,3 +176,51 @@ def test_mixed_precision_trajectory(cuda):
             assert st.n_constraints == 0 or st.min_dist2 > 0
             outs.append(s.state()[0])
         assert np.abs(outs[0] - outs[1]).max() <= 1e-2 * diag
+
+
+def test_penalty_dirichlet_steps_match(cuda, orc):
+    """Cloth on a sphere that turns about y (mu 0.4, xi 5e-4, dt 0.02): once the
+    cloth wraps the sphere, moving the sphere's vertices to their targets is no
+    longer intersection free and the step takes the augmented-Lagrangian path
+    (the Dirichlet vertices start at x^n, a penalty of stiffness 1e6, doubled up
+    to 1e8, pulls them until 99% of the way, then they are projected).
+    Per step from the oracle's states at a tight tolerance.  The Dirichlet
+    vertices end at the Newton iterate where 99% progress is first reached, so
+    their final positions follow the iterates; bar 1e-7 of the bounding-box
+    diagonal."""
+    X, T, dbc, c = W.cloth_on_sphere(n=16, subdiv=3)
+    sh = orc.Shell(X, T, **MAT)
+    k2o, dhat2 = sh.init_oipc(DHAT)
+    dt, xi, mu = 0.02, 5e-4, 0.4
+
+    def target(k):
+        return W.rotate_y(X[dbc], c, 2.0 * dt * (k + 1))
+
+    x = X.copy()
+    v = np.zeros_like(X)
+    for k in range(9):
+        rc, _ = sh.step(x, v, k2o, dbc, target(k), dt, dhat2, xi, mu=mu, tol=1e-3)
+        assert rc == 0
+    s = _gpu_sim(X, T, dbc)
+    s.init_oipc(DHAT)
+    prm = F.make_params(dt, dhat2, xi, mu=mu, epsv2=1e-6, fric_iters=1, newton_tol=1e-7, pcg_tol=1e-12,
+                        max_newton_iters=400)
+    diag = np.linalg.norm(X.max(0) - X.min(0))
+    penalty_steps = 0
+    for k in range(9, 12):
+        s.set_state(x, v)
+        s.set_kappa(k2o[0], k2o[1])
+        s.set_dbc(dbc, target(k))
+        xo, vo, ko = x.copy(), v.copy(), k2o.copy()
+        rc, sto = sh.step(xo, vo, ko, dbc, target(k), dt, dhat2, xi, mu=mu, tol=1e-7, max_iter=400)
+        assert rc == 0
+        stg = s.step(prm)
+        xg, _ = s.state()
+        penalty_steps += stg.status == 1
+        assert stg.min_dist2 > 0 or stg.n_constraints == 0
+        err = np.abs(xg - xo).max()
+        assert err <= 1e-7 * diag, (k, err, sto, stg.as_dict())
+        # advance the oracle at the working tolerance
+        rc, _ = sh.step(x, v, k2o, dbc, target(k), dt, dhat2, xi, mu=mu, tol=1e-3)
+        assert rc == 0
+    assert penalty_steps > 0
