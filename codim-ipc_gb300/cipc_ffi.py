@@ -44,6 +44,8 @@ _SIGS = {
     "cipc_device_count": (_c_int, []),
     "cipc_ccd_pairs": (_c_int, [_c_i64, _vp, _vp, _c_i64, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _c_int, _c_int,
                                 _vp, _vp, ctypes.POINTER(_c_i64), _vp]),
+    "cipc_ccd_pairs_noalloc": (_c_int, [_c_i64, _vp, _vp, _c_i64, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _c_int,
+                                        _c_int, _vp, _vp, ctypes.POINTER(_c_i64), _vp]),
     "cipc_barrier_pairs": (_c_int, [_c_i64, _vp, _vp, _c_i64, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _c_int, _c_int,
                                     _c_int, _vp, _vp, _vp, ctypes.POINTER(_c_i64), _vp]),
     "cipc_encode_reference_constraint": (_c_int, [_c_int, _vp, _c_int, _c_int, _vp]),
@@ -122,6 +124,23 @@ def ccd_pairs_async(type_, idx, x, dx, toc_out, hit, eta=0.1, thickness=0.0, toc
     st = lib().cipc_ccd_pairs(n, _ptr(type_), _ptr(idx), nv, _ptr(x), _ptr(dx), eta, thickness, toc_in,
                               precision, MEM_DEVICE, _ptr(toc_out), _ptr(hit), None, _stream_ptr(stream))
     return _check(st)
+
+
+NOALLOC_SLOTS = 16
+
+
+def ccd_pairs_noalloc(type_, idx, x, dx, toc_out, hit, eta=0.1, thickness=0.0, toc_in=1.0, precision=FP64,
+                      slot=0, stream=None, counts=True, allow=(CIPC_ERR_ITER_CAP,)):
+    """Device-memory CCD that allocates nothing (see cipc_ccd_pairs_noalloc).
+    Returns (status, n_overflow); with counts=False it only enqueues."""
+    n = int(type_.shape[0])
+    nv = int(x.shape[0])
+    ov = _c_i64(0)
+    st = lib().cipc_ccd_pairs_noalloc(n, _ptr(type_), _ptr(idx), nv, _ptr(x), _ptr(dx), eta, thickness, toc_in,
+                                      precision, slot, _ptr(toc_out), _ptr(hit),
+                                      ctypes.byref(ov) if counts else None, _stream_ptr(stream))
+    _check(st, allow)
+    return st, ov.value
 
 
 def barrier_pairs(type_, idx, x, x_rest, energy, grad, hess, dhat2, xi, kappa, project_pd=True,

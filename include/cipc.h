@@ -74,6 +74,35 @@ int cipc_ccd_pairs(int64_t n_pairs, const uint8_t* type, const int32_t* idx, int
                    void* stream);
 
 /*
+ * cipc_ccd_pairs for callers that must not allocate device memory (no reference
+ * counterpart: the reference's CCD runs on the host).
+ *
+ * Same pairs, same kernels and the same outputs and status codes as
+ * cipc_ccd_pairs with mem = CIPC_MEM_DEVICE, but the three counters the kernel
+ * needs (work counter, overflow count, invalid-pair count) come from a fixed
+ * scratch array compiled into the library instead of cudaMallocAsync: no
+ * cudaMalloc / cudaMallocAsync / cudaFree call, and no library call that
+ * allocates.  All buffers must already be in device memory of the current device.
+ *
+ * The scratch holds CIPC_NOALLOC_SLOTS slots of CIPC_NOALLOC_SLOT_BYTES; `slot`
+ * picks one (0 <= slot < CIPC_NOALLOC_SLOTS, anything else is rejected with
+ * CIPC_ERR_INVALID_ARG).  The call zeroes its slot on `stream` before the launch
+ * (the counters must start at zero).  Two calls that overlap in time on the same
+ * device and the same slot race on its counters and give wrong results: give
+ * each stream that may run concurrently its own slot, or order the calls.
+ * The first call on each device looks up the slot's device address
+ * (cudaGetSymbolAddress, which may load the library's kernels on that device);
+ * make that first call outside any stream capture.  With n_overflow == NULL the
+ * call only enqueues work on `stream` and reports no kernel-side counts.
+ */
+#define CIPC_NOALLOC_SLOTS 16
+#define CIPC_NOALLOC_SLOT_BYTES 128
+int cipc_ccd_pairs_noalloc(int64_t n_pairs, const uint8_t* type, const int32_t* idx, int64_t n_verts,
+                           const double* x, const double* dx, double eta, double thickness, double toc_in,
+                           int precision, int slot, double* toc_out, uint8_t* hit, int64_t* n_overflow,
+                           void* stream);
+
+/*
  * Barrier energy, gradient and PSD-projected Hessian per contact pair.
  *
  * Replaces the per-constraint bodies of Compute_Barrier, Compute_Barrier_Gradient

@@ -59,3 +59,23 @@ def test_argument_validation_without_gpu():
     e0 = np.zeros(0, np.uint8)
     st, ov = cipc_ffi.ccd_pairs(e0, np.zeros((0, 4), np.int32), x, x, np.zeros(0), np.zeros(0, np.uint8))
     assert st == 0 and ov == 0
+
+
+def test_noalloc_argument_validation_without_gpu():
+    """Slot and argument checks of cipc_ccd_pairs_noalloc run before any device work."""
+    import cipc_ffi
+    t = np.zeros(1, np.uint8)
+    idx = np.zeros((1, 4), np.int32)
+    x = np.zeros((2, 3))
+    toc = np.zeros(1)
+    hit = np.zeros(1, np.uint8)
+    for kw in (dict(slot=-1), dict(slot=cipc_ffi.NOALLOC_SLOTS), dict(eta=0.0), dict(precision=7)):
+        try:
+            cipc_ffi.ccd_pairs_noalloc(t, idx, x, x, toc, hit, **kw)
+            raise AssertionError("expected an error for %r" % (kw,))
+        except cipc_ffi.CipcError as e:
+            assert e.status == cipc_ffi.CIPC_ERR_INVALID_ARG, kw
+    e0 = np.zeros(0, np.uint8)
+    st, ov = cipc_ffi.ccd_pairs_noalloc(e0, np.zeros((0, 4), np.int32), x, x, np.zeros(0), np.zeros(0, np.uint8),
+                                        slot=cipc_ffi.NOALLOC_SLOTS - 1)
+    assert st == cipc_ffi.CIPC_OK and ov == 0
