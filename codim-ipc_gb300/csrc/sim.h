@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdlib>
 #include <vector>
 
 namespace cipc {
@@ -12,6 +13,12 @@ namespace cipc {
 // four vertices are the two edges (EEM: ea0 ea1 eb0 eb1, PEM: p p' e0 e1,
 // PPM: p p' q q', primed = the other endpoint of the point's edge)
 enum ConKind : int { cPP = 0, cPE = 1, cPT = 2, cEE = 3, cEEM = 4, cPEM = 5, cPPM = 6 };
+
+inline bool poison_buffers()
+{
+    static const bool on = std::getenv("CIPC_POISON") != nullptr;
+    return on;
+}
 
 template <typename T>
 struct DBuf {
@@ -25,6 +32,9 @@ struct DBuf {
         n = 0;
         cudaError_t e = cudaMalloc((void**)&p, (count ? count : 1) * sizeof(T));
         if (e == cudaSuccess) n = count;
+        // CIPC_POISON set: new buffers start as all-ones bytes (NaN for floating
+        // point, -1 for integers) so that a read before the first write shows
+        if (e == cudaSuccess && poison_buffers()) e = cudaMemset(p, 0xFF, (count ? count : 1) * sizeof(T));
         return e;
     }
     void release()

@@ -594,6 +594,10 @@ __global__ void __launch_bounds__(128) k_barrier_cons(BarArgs a, int want_h)
         const double s = con_d2(k, v) - a.xi2;
         if (!(s > 0)) {
             if (a.flag) *a.flag = 1.0;
+            if (want_h) {
+                HT* out = reinterpret_cast<HT*>(a.hess) + 78 * (size_t)i;
+                for (int w = 0; w < 78; ++w) out[w] = HT(0);
+            }
         } else if (s < a.shat) {
             switch (k) {
                 case kc_PP: bar_one<HT, kc_PP>(a, i, v, id, s, E, want_h); break;

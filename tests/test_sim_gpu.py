@@ -132,13 +132,18 @@ def test_steps_match_direct_solve(cuda, orc, nh):
 
 
 def test_mixed_precision_step_parity(cuda):
-    """FP32 Hessians + FP32 PCG inside FP64 refinement reach the same Newton fixed
-    point as the FP64 path (the gradient stays FP64): per step from identical
-    states at a tight tolerance.  The two Newton loops stop at different
-    iterates: each stops once the RMS Newton step over its last three iterations
-    is at most tol * h, and a Newton step is the distance to the fixed point up
-    to second order, so the largest per-vertex difference is bounded by
-    2 * sqrt(free vertices) * tol * h."""
+    """FP32 Hessians + FP32 PCG inside FP64 refinement solve the same Newton
+    problem as the FP64 path (gradient and energy stay FP64): per step from
+    identical states at a tight tolerance, the mixed endpoint must be a converged
+    point of the FP64 problem.
+
+    Positions are not compared: the symmetric cloth buckles on the box, and its
+    incremental potential then has mirror-image local minima whose energies agree
+    to ~1e-10 relative while the positions differ by up to ~1e-3 (measured: FP64
+    runs at PCG tolerances 1e-12 and 1e-9 land in the same one, the mixed run in
+    the other, both with FP64 gradients ~1e-11).  Bars: intersection free; FP64
+    incremental potential within 1e-9 relative of the FP64 endpoint's; FP64
+    gradient (free vertices) at most 10x the FP64 endpoint's plus 1e-10."""
     X, T, dbc = scene(n=12, y=-0.093)
     sims = []
     for prec in (F.FP64, F.MIXED):
@@ -146,18 +151,28 @@ def test_mixed_precision_step_parity(cuda):
         k2, dhat2 = s.init_oipc(DHAT)
         sims.append((s, F.make_params(DT, dhat2, XI, newton_tol=1e-7, precision=prec, pcg_tol=1e-12,
                                       max_newton_iters=400)))
-    bar = 2 * np.sqrt(X.shape[0] - len(dbc)) * 1e-7 * DT
     ref, mix = sims
-    for step in range(4):
+    grav = np.array([0.0, -9.81, 0.0])
+    for step in range(5):
         x0, v0 = ref[0].state()
         k2 = ref[0].kappa()
+        xt = x0 + DT * v0 + DT * DT * grav
         mix[0].set_state(x0, v0)
         mix[0].set_kappa(k2[0], k2[1])
         st_r = ref[0].step(ref[1])
         st_m = mix[0].step(mix[1])
-        xr, xm = ref[0].state()[0], mix[0].state()[0]
         assert st_m.n_constraints == 0 or st_m.min_dist2 > 0
-        assert np.abs(xr - xm).max() <= bar, (step, np.abs(xr - xm).max(), st_r.as_dict(), st_m.as_dict())
+        xr, xm = ref[0].state()[0], mix[0].state()[0]
+        # FP64 incremental potential and gradient of both endpoints at the step's kappa
+        mix[0].set_kappa(k2[0], k2[1])
+        Er, gr = mix[0].eval(ref[1], xr, xt)
+        Em, gm = mix[0].eval(ref[1], xm, xt)
+        gr[dbc] = 0
+        gm[dbc] = 0
+        info = (step, Er, Em, np.abs(gr).max(), np.abs(gm).max(), st_r.as_dict(), st_m.as_dict())
+        assert abs(Em - Er) <= 1e-9 * abs(Er), info
+        assert np.abs(gm).max() <= 10 * np.abs(gr).max() + 1e-10, info
+        mix[0].set_kappa(*ref[0].kappa())
 
 
 def test_mixed_precision_trajectory(cuda):
