@@ -33,6 +33,14 @@ struct CcdArgs {
     uint8_t* hit;
     int32_t* iters;                    // optional
     unsigned long long* counter;       // [0] work counter, [1] overflow count, [2] invalid pairs
+    // Optional running minimum (bits of a non-negative double, initialised to
+    // toc_in by the caller).  When set, a pair stops as soon as its time passes
+    // the smallest time of impact found so far, and every hit lowers it: the
+    // final minimum is the one the reference's sequential loop finds, where each
+    // narrow-phase call is bounded by the step size found so far
+    // (IPC.h:1959-2242), and pairs beyond it do no further work.  A pair that
+    // reaches the iteration cap lowers it to the time it has safely advanced to.
+    unsigned long long* toc_min = nullptr;
 };
 
 CIPC_HD double dmax(double a, double b) { return (a < b) ? b : a; }
@@ -76,6 +84,11 @@ CIPC_HD double ccd_prepare(int tp, d3 (&dv)[4])
     }
 }
 
+__device__ __forceinline__ double load_min(const unsigned long long* p)
+{
+    return __longlong_as_double((long long)*(const volatile unsigned long long*)p);
+}
+
 template <class Pol>
 __global__ void __launch_bounds__(256) k_accd(CcdArgs a)
 {
@@ -86,7 +99,7 @@ __global__ void __launch_bounds__(256) k_accd(CcdArgs a)
     bool exhausted = false;
     int tp = 0, phase = 0;
     d3 v[4], dv[4];
-    double maxDisp = 0, gap = 0, t = 0, tlb = 0;
+    double maxDisp = 0, gap = 0, t = 0, tlb = 0, lim = toc_prev;
     int64_t adv = 0;
     while (true) {
         const bool need = (pid < 0) && !exhausted;
@@ -138,6 +151,7 @@ __global__ void __launch_bounds__(256) k_accd(CcdArgs a)
             }
             maxDisp = ccd_prepare(tp, dv);
             adv = 0;
+            lim = a.toc_min ? dmin(toc_prev, load_min(a.toc_min)) : toc_prev;
             if (maxDisp == 0) {
                 a.toc_out[pid] = toc_prev;
                 a.hit[pid] = 0;
@@ -157,12 +171,14 @@ __global__ void __launch_bounds__(256) k_accd(CcdArgs a)
             if (t != 0 && (f / (dist + th) < gap)) {
                 a.toc_out[pid] = t;
                 a.hit[pid] = 1;
+                if (a.toc_min) atomicMin(a.toc_min, (unsigned long long)__double_as_longlong(t));
                 if (a.iters) a.iters[pid] = (int32_t)adv;
                 pid = -1;
                 continue;
             }
             t += tlb;
-            if (t > toc_prev) {
+            if (a.toc_min && (adv & 15) == 0) lim = dmin(lim, load_min(a.toc_min));
+            if (t > lim) {
                 a.toc_out[pid] = toc_prev;
                 a.hit[pid] = 0;
                 if (a.iters) a.iters[pid] = (int32_t)adv;
@@ -173,6 +189,7 @@ __global__ void __launch_bounds__(256) k_accd(CcdArgs a)
         if (adv >= a.max_iter) {
             a.toc_out[pid] = toc_prev;
             a.hit[pid] = 0;
+            if (a.toc_min) atomicMin(a.toc_min, (unsigned long long)__double_as_longlong(t));
             if (a.iters) a.iters[pid] = (int32_t)adv;
             atomicAdd(a.counter + 1, 1ull);
             pid = -1;

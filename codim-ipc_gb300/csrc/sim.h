@@ -90,9 +90,11 @@ struct Sim {
     std::vector<int> dbc_idx_h;
     DBuf<int> dbc_idx;
     DBuf<double> dbc_tgt;
-    // block sparsity of the elastic part (vertex blocks, 3x3)
-    int nnzb = 0;
-    DBuf<int> row_ptr, col, diag, tri_slot, hinge_slot;
+    // block sparsity of the elastic part (vertex blocks, 3x3) in ELL form: row i's
+    // k-th block is block k * nv + i (k < ell_k), column col[k * nv + i]; padding
+    // blocks are zero with the row's own column; nnzb = ell_k * nv
+    int nnzb = 0, ell_k = 0;
+    DBuf<int> col, diag, tri_slot, hinge_slot;
     // dynamic
     DBuf<double> x, xn, xt, v, g, dir, xprev, rhs, disp;
     DBuf<char> hval;  // BSR values, float or double per precision
@@ -123,6 +125,8 @@ struct Sim {
     cudaStream_t stream = nullptr;
     SimParams prm;
     StepStats last;
+    // graph-replayed PCG (sim_pcg.cu)
+    void* pcg = nullptr;
     // learned preconditioner (optional)
     void* learned = nullptr;
     std::vector<double> host_mass;

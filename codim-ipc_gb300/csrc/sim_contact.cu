@@ -533,7 +533,8 @@ struct BarArgs {
     double* g;
     double* red;
     double* flag;  // set to 1 when some s <= 0
-    void* hess;    // 78 per constraint (HT)
+    void* hess;    // 78 per constraint (HT), entry h of constraint i at h * hs + i
+    size_t hs;
     double* pdiag;
 };
 
@@ -556,7 +557,7 @@ __device__ void bar_one(const BarArgs& a, int i, const d3 (&v)[4], const int (&i
 #pragma unroll
             for (int c = 0; c < 3; ++c) atomicAdd(a.g + 3 * id[q] + c, o.g[3 * q + c]);
     if (want_h) {
-        HT* out = reinterpret_cast<HT*>(a.hess) + 78 * (size_t)i;
+        HT* out = reinterpret_cast<HT*>(a.hess) + i;
         int w = 0;
         constexpr int m = 3 * NV;
 #pragma unroll
@@ -564,7 +565,7 @@ __device__ void bar_one(const BarArgs& a, int i, const d3 (&v)[4], const int (&i
 #pragma unroll
             for (int q = p; q < m; ++q) {
                 const bool keep = !a.dbc[id[p / 3]] && !a.dbc[id[q / 3]];
-                out[w++] = keep ? o.H[p][q] : HT(0);
+                out[(w++) * a.hs] = keep ? o.H[p][q] : HT(0);
             }
         // diagonal blocks into the block-Jacobi diagonal
 #pragma unroll
@@ -595,8 +596,8 @@ __global__ void __launch_bounds__(128) k_barrier_cons(BarArgs a, int want_h)
         if (!(s > 0)) {
             if (a.flag) *a.flag = 1.0;
             if (want_h) {
-                HT* out = reinterpret_cast<HT*>(a.hess) + 78 * (size_t)i;
-                for (int w = 0; w < 78; ++w) out[w] = HT(0);
+                HT* out = reinterpret_cast<HT*>(a.hess) + i;
+                for (int w = 0; w < 78; ++w) out[w * a.hs] = HT(0);
             }
         } else if (s < a.shat) {
             switch (k) {
@@ -609,8 +610,8 @@ __global__ void __launch_bounds__(128) k_barrier_cons(BarArgs a, int want_h)
                 default: bar_one<HT, kc_PPM>(a, i, v, id, s, E, want_h); break;
             }
         } else if (want_h) {
-            HT* out = reinterpret_cast<HT*>(a.hess) + 78 * (size_t)i;
-            for (int w = 0; w < 78; ++w) out[w] = HT(0);
+            HT* out = reinterpret_cast<HT*>(a.hess) + i;
+            for (int w = 0; w < 78; ++w) out[w * a.hs] = HT(0);
         }
     }
     // energy partial
@@ -663,6 +664,7 @@ void contact_grad_hess(Sim* s, const double* x, double* g, bool want_hess)
     if (want_hess) {
         s->chess.alloc((size_t)s->cap_con * 78 * (f32 ? 4 : 8));
         a.hess = s->chess.p;
+        a.hs = (size_t)s->cap_con;
     }
     if (f32) k_barrier_cons<float><<<nblk(s->ncon, 128), 128, 0, s->stream>>>(a, want_hess ? 1 : 0);
     else k_barrier_cons<double><<<nblk(s->ncon, 128), 128, 0, s->stream>>>(a, want_hess ? 1 : 0);
@@ -1051,24 +1053,6 @@ __global__ void k_ccd_ee(CcdCand c)
     });
 }
 
-__global__ void k_min_hit_toc(int n, const double* toc, const uint8_t* hit, double* out)
-{
-    __shared__ double sh[256];
-    double m = 1e300;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        if (hit[i]) m = fmin(m, toc[i]);
-    sh[threadIdx.x] = m;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) sh[threadIdx.x] = fmin(sh[threadIdx.x], sh[threadIdx.x + w]);
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        unsigned long long bits = __double_as_longlong(sh[0]);  // non-negative: order-preserving
-        atomicMin((unsigned long long*)out, bits);
-    }
-}
-
 int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double* alpha_out)
 {
     cudaStream_t st = s->stream;
@@ -1148,15 +1132,15 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         a.hit = hit;
         a.iters = nullptr;
         a.counter = ctr + 2;
+        a.toc_min = (unsigned long long*)amin;
         cudaMemsetAsync(ctr + 2, 0, 4 * sizeof(unsigned long long), st);
+        unsigned long long init_bits;
+        memcpy(&init_bits, &alpha, sizeof(double));
+        k_set_u64<<<1, 1, 0, st>>>((unsigned long long*)amin, init_bits);
         int grid = num_sms() * accd_exact_blocks_per_sm();
         if ((np + 255) / 256 < grid) grid = (np + 255) / 256;
         e = launch_accd_exact(a, grid, st);
         if (e != cudaSuccess) return set_cuda_error(e, "ccd");
-        unsigned long long init_bits;
-        memcpy(&init_bits, &alpha, sizeof(double));
-        k_set_u64<<<1, 1, 0, st>>>((unsigned long long*)amin, init_bits);
-        k_min_hit_toc<<<std::min(nblk(np, 256), 1024), 256, 0, st>>>(np, toc, hit, amin);
         double res;
         cudaMemcpyAsync(&res, amin, sizeof(double), cudaMemcpyDeviceToHost, st);
         e = cudaStreamSynchronize(st);

@@ -11,7 +11,11 @@ struct HostScene {
     std::vector<double> X0, P, vol, hinfo, mass, b;
     std::vector<int> tri, hinge, bnode, bedge, btri;
     double lam = 0, mu = 0, kbend = 0, cell = 1;
-    std::vector<int> row_ptr, col, diag, tri_slot, hinge_slot;
+    // elastic block pattern in ELL form: row i's k-th block (k < ell_k) is block
+    // k * nv + i, column col[k * nv + i]; rows shorter than ell_k are padded with
+    // their own column and zero blocks
+    int ell_k = 0;
+    std::vector<int> col, diag, tri_slot, hinge_slot;
 };
 
 int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,

@@ -1,0 +1,587 @@
+// Preconditioned conjugate gradients on the Newton system as one persistent
+// cooperative kernel per solve, every scalar kept on the device (replaces the
+// reference's per-iteration CHOLMOD factorization and solve,
+// Library/Math/DIRECT_SOLVER.h:13-88).
+//
+// Operator H = (elastic + mass, 3x3 block CSR) + sum over contact constraints of
+// their stored PSD blocks (packed upper triangle, 78 per constraint) + sum over
+// friction constraints of w_a w_b T M T^T (applied from the 2x2 inner matrix).
+// The preconditioner is a 3x3 block per vertex (block Jacobi, or any other
+// block-diagonal M^-1 written into the same array).
+//
+// Iteration k (standard PCG arithmetic, p_k = z_k + beta_k p_{k-1}), two phases
+// separated by grid barriers:
+//   apply    p_k is formed on the fly from z and p_{k-1} wherever it is
+//            gathered; q_e = H_elastic p_k one scalar row per thread (plain
+//            stores), the contact and friction parts are accumulated into q_c
+//            with atomics, and p_k^T H p_k is summed element by element.
+//   update   alpha = (r,z)/(p,Hp); x += alpha p; r -= alpha (q_e + q_c); q_c = 0;
+//            z = M^-1 r; (r,z) and (r,r).
+// Each phase ends with per-block partial sums; after the barrier every block
+// adds the partials in the same fixed order, so all blocks take the same stop
+// decision.  Data written by other blocks during the solve is read through L2
+// (ld.global.cg), never from a stale L1 line.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "../../include/cipc.h"
+#include "cipc_util.h"
+#include "constraint_eval.cuh"
+#include "sim.h"
+#include "sim_kernels.h"
+#include "sim_pcg.h"
+
+namespace cipc {
+
+// results of one solve, and the grid barrier's state
+struct PcgScalars {
+    double rr;      // (r, r) at exit
+    double bb;      // (b, b)
+    double pq;      // last (p, Hp)
+    int it;         // completed iterations
+    int done;       // 1 converged, 2 NaN, 3 (p, Hp) <= 0, 4 iteration cap, 5 barrier wait gave up
+    int err;
+    int pad;
+    double tot[2];  // totals published by the last block to arrive at a reduction
+    // arrival counter and release generation on their own 128-byte lines, so that
+    // the waiting blocks' polling does not contend with the arrivals
+    alignas(128) unsigned int bar_count;
+    alignas(128) unsigned int bar_gen;
+    // with tracing on: block 0's time (ns) in apply, reduction 1, -, update,
+    // reduction 2, -, summed over iterations
+    unsigned long long tphase[6];
+};
+
+__device__ __forceinline__ unsigned long long gtimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+template <typename VT, typename XT, typename PT>
+struct PcgArgs {
+    int nv, ell_k;
+    const int* col;
+    const VT* val;
+    const int* ckind;
+    const int4* cverts;
+    const VT* chess;  // entry h of constraint c at chess[h * hs + c]
+    size_t hs;
+    const int* fkind;
+    const int4* fverts;
+    const double* fw;
+    const double* fT;
+    const double* fM;
+    const uint8_t* proj;
+    const PT* pinv;
+    const XT* b;
+    XT* x;
+    XT* r;
+    XT* z;
+    XT* P0;
+    XT* P1;
+    XT* qe;
+    XT* qc;
+    double* part_a;  // 1 partial per block (apply phase)
+    double* part_b;  // 2 partials per block (init / update phase)
+    PcgScalars* d;
+    double tol;
+    int maxit;
+    int ncon, nfric;
+    int trace;
+};
+
+// 256-thread blocks, 4 per SM: a grid-wide reduction costs ~5-7 us here against
+// ~9 us with one 1024-thread block per SM (block-level sums dominate)
+constexpr int kPcgThreads = 256;
+constexpr unsigned int kBarrierSpinLimit = 1u << 25;  // x >= 32 ns of sleep: over a second
+
+template <typename T>
+__device__ __forceinline__ T ldcg(const T* p)
+{
+    return __ldcg(p);
+}
+
+// sum of v over the block, returned to every thread
+template <int N>
+__device__ __forceinline__ void block_sum_all(double (&v)[N])
+{
+    __shared__ double sh[N][kPcgThreads / 32];
+    __shared__ double res[N];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        double a = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) sh[k][wid] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x < N) {
+        double a = 0;
+        for (int w = 0; w < kPcgThreads / 32; ++w) a += sh[threadIdx.x][w];
+        res[threadIdx.x] = a;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = res[k];
+    __syncthreads();
+}
+
+// Grid-wide sum of v (N values per thread, summed over all threads of all
+// blocks), returned in v to every thread, with the barrier semantics of
+// grid_barrier.  Each block writes its partial and arrives; the last block to
+// arrive adds the partials in block order, publishes the totals and releases
+// the others, which then read the totals.  Returns false if a wait gave up.
+template <int N>
+__device__ __forceinline__ bool grid_allreduce(double (&v)[N], double* part, PcgScalars* d)
+{
+    __shared__ int ok, last;
+    block_sum_all<N>(v);
+    if (threadIdx.x == 0) {
+        ok = 1;
+        last = 0;
+#pragma unroll
+        for (int k = 0; k < N; ++k) part[N * blockIdx.x + k] = v[k];
+        volatile unsigned int* gen = &d->bar_gen;
+        volatile int* err = &d->err;
+        const unsigned int g = *gen;
+        __threadfence();
+        if (atomicAdd(&d->bar_count, 1u) == gridDim.x - 1) {
+            last = 1;
+        } else {
+            unsigned int spins = 0;
+            while (*gen == g) {
+                if (*err || ++spins > kBarrierSpinLimit) {
+                    atomicExch(&d->err, 1);
+                    ok = 0;
+                    break;
+                }
+                if (spins > 512) __nanosleep(32);
+            }
+            __threadfence();
+        }
+    }
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        double acc[N];
+#pragma unroll
+        for (int k = 0; k < N; ++k) acc[k] = 0;
+        for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+#pragma unroll
+            for (int k = 0; k < N; ++k) acc[k] += ldcg(part + N * b + k);
+        block_sum_all<N>(acc);
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int k = 0; k < N; ++k) d->tot[k] = acc[k];
+            atomicExch(&d->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&d->bar_gen, 1u);
+        }
+#pragma unroll
+        for (int k = 0; k < N; ++k) v[k] = acc[k];
+        return true;
+    }
+    if (!ok) return false;
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = ldcg(d->tot + k);
+    return true;
+}
+
+// z = M^-1 r for vertex i
+template <typename XT, typename PT>
+__device__ __forceinline__ void precond_vertex(const PT* __restrict__ pinv, int i, const XT (&r)[3], XT (&z)[3])
+{
+    const PT* P = pinv + 9 * (size_t)i;
+    z[0] = (XT)__ldg(P + 0) * r[0] + (XT)__ldg(P + 1) * r[1] + (XT)__ldg(P + 2) * r[2];
+    z[1] = (XT)__ldg(P + 3) * r[0] + (XT)__ldg(P + 4) * r[1] + (XT)__ldg(P + 5) * r[2];
+    z[2] = (XT)__ldg(P + 6) * r[0] + (XT)__ldg(P + 7) * r[1] + (XT)__ldg(P + 8) * r[2];
+}
+
+// y = H_c x_c for one contact constraint of NV vertices (packed upper triangle,
+// row by row, entry h at H[h * hs]: consecutive constraints are adjacent, so a
+// warp's loads of one entry are coalesced), accumulated into q; returns x_c . y
+template <int NV, typename VT, typename XT, typename G>
+__device__ __forceinline__ double con_apply(const VT* __restrict__ H, size_t hs, int4 iv, const G& pget, XT* q)
+{
+    constexpr int M = 3 * NV;
+    const int id[4] = {iv.x, iv.y, iv.z, iv.w};
+    XT xs[M], ys[M];
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            xs[3 * k + t] = pget(3 * id[k] + t);
+            ys[3 * k + t] = 0;
+        }
+    int h = 0;
+#pragma unroll
+    for (int p = 0; p < M; ++p) {
+        ys[p] += (XT)__ldg(H + h * hs) * xs[p];
+        ++h;
+#pragma unroll
+        for (int k = p + 1; k < M; ++k, ++h) {
+            const XT hv = (XT)__ldg(H + h * hs);
+            ys[p] += hv * xs[k];
+            ys[k] += hv * xs[p];
+        }
+    }
+    double s = 0;
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            const XT y = ys[3 * k + t];
+            s += (double)xs[3 * k + t] * (double)y;
+            if (y != XT(0)) atomicAdd(q + 3 * id[k] + t, y);
+        }
+    return s;
+}
+
+// apply phase: q_e, q_c = H p_k (p_k formed on the fly and stored for the owned
+// rows); returns this thread's share of (p_k, H p_k)
+template <typename VT, typename XT, typename PT>
+__device__ __forceinline__ double apply_phase(const PcgArgs<VT, XT, PT>& a, bool first, XT beta, XT* pk,
+                                              const XT* pold)
+{
+    const XT* z = a.z;
+    auto pget = [&](int j) -> XT { return first ? ldcg(z + j) : ldcg(z + j) + beta * ldcg(pold + j); };
+    const int nrow = 3 * a.nv, ncon = a.ncon, nfric = a.nfric;
+    const int total = nrow + ncon + nfric;
+    double v = 0;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < total; w += gridDim.x * blockDim.x) {
+        if (w < nrow) {
+            // one scalar row of the elastic 3x3 block rows per thread: row 3i + r
+            const int i = w / 3, r = w - 3 * i;
+            XT acc = 0;
+            const int K = a.ell_k, nv = a.nv;
+#pragma unroll 8
+            for (int k = 0; k < K; ++k) {
+                const size_t e = (size_t)k * nv + i;
+                const int j = __ldg(a.col + e);
+                const VT* B = a.val + 9 * e + 3 * r;
+                acc += (XT)__ldg(B) * pget(3 * j) + (XT)__ldg(B + 1) * pget(3 * j + 1) +
+                       (XT)__ldg(B + 2) * pget(3 * j + 2);
+            }
+            const XT pw = pget(w);
+            pk[w] = pw;
+            a.qe[w] = acc;
+            v += (double)pw * (double)acc;
+        } else if (w < nrow + ncon) {
+            // contact constraint: packed upper triangle of its (3nv x 3nv) block
+            const int c = w - nrow;
+            const int cnv = con_nv(__ldg(a.ckind + c));
+            const int4 iv = a.cverts[c];
+            const VT* H = a.chess + c;
+            if (cnv == 2) v += con_apply<2>(H, a.hs, iv, pget, a.qc);
+            else if (cnv == 3) v += con_apply<3>(H, a.hs, iv, pget, a.qc);
+            else v += con_apply<4>(H, a.hs, iv, pget, a.qc);
+        } else {
+            // friction constraint: w_a T M T^T sum_b w_b p_b over non-projected vertices
+            const int c = w - nrow - ncon;
+            if (a.fkind[c] >= kc_EEM) continue;
+            const int cnv = con_nv(a.fkind[c]);
+            const int4 iv = a.fverts[c];
+            const int id[4] = {iv.x, iv.y, iv.z, iv.w};
+            double s0 = 0, s1 = 0, s2 = 0;
+            for (int q = 0; q < cnv; ++q) {
+                if (a.proj[id[q]]) continue;
+                const double wq = a.fw[4 * c + q];
+                s0 += wq * (double)pget(3 * id[q]);
+                s1 += wq * (double)pget(3 * id[q] + 1);
+                s2 += wq * (double)pget(3 * id[q] + 2);
+            }
+            const double* T = a.fT + 6 * (size_t)c;
+            const double t0 = T[0] * s0 + T[1] * s1 + T[2] * s2, t1 = T[3] * s0 + T[4] * s1 + T[5] * s2;
+            const double m00 = a.fM[3 * c], m01 = a.fM[3 * c + 1], m11 = a.fM[3 * c + 2];
+            const double u0 = m00 * t0 + m01 * t1, u1 = m01 * t0 + m11 * t1;
+            v += t0 * u0 + t1 * u1;
+            const double o0 = T[0] * u0 + T[3] * u1, o1 = T[1] * u0 + T[4] * u1, o2 = T[2] * u0 + T[5] * u1;
+            for (int q = 0; q < cnv; ++q) {
+                if (a.proj[id[q]]) continue;
+                const double wq = a.fw[4 * c + q];
+                atomicAdd(a.qc + 3 * id[q], (XT)(wq * o0));
+                atomicAdd(a.qc + 3 * id[q] + 1, (XT)(wq * o1));
+                atomicAdd(a.qc + 3 * id[q] + 2, (XT)(wq * o2));
+            }
+        }
+    }
+    return v;
+}
+
+template <typename VT, typename XT, typename PT>
+__global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_solve(PcgArgs<VT, XT, PT> a)
+{
+    PcgScalars* d = a.d;
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+    // r = b, x = 0, q_c = 0, z = M^-1 r
+    double tot[2];
+    {
+        double v[2] = {0, 0};
+        for (int i = gtid; i < a.nv; i += gstride) {
+            XT r[3], z[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                r[c] = a.b[3 * i + c];
+                a.r[3 * i + c] = r[c];
+                a.x[3 * i + c] = 0;
+                a.qc[3 * i + c] = 0;
+            }
+            precond_vertex<XT, PT>(a.pinv, i, r, z);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                a.z[3 * i + c] = z[c];
+                v[0] += (double)r[c] * (double)z[c];
+                v[1] += (double)r[c] * (double)r[c];
+            }
+        }
+        if (!grid_allreduce<2>(v, a.part_b, d)) return;
+        tot[0] = v[0];
+        tot[1] = v[1];
+    }
+    double rz = tot[0], rz_prev = 1, rr = tot[1], pq = 0;
+    const double bb = tot[1], thr = a.tol * a.tol * bb;
+    int done = 0, k = 0;
+    if (!(bb == bb) || !(rz == rz)) done = 2;
+    else if (!(bb > 0)) done = 1;
+    const bool tr = a.trace && blockIdx.x == 0 && threadIdx.x == 0;
+    unsigned long long tp[6] = {0, 0, 0, 0, 0, 0}, t0 = tr ? gtimer() : 0;
+    auto lap = [&](int k) {
+        if (tr) {
+            const unsigned long long t = gtimer();
+            tp[k] += t - t0;
+            t0 = t;
+        }
+    };
+    while (!done) {
+        if (k >= a.maxit) {
+            done = 4;
+            break;
+        }
+        const bool first = (k == 0);
+        const XT beta = first ? XT(0) : (XT)(rz / rz_prev);
+        XT* pk = (k & 1) ? a.P1 : a.P0;
+        const XT* pold = (k & 1) ? a.P0 : a.P1;
+        double va[1] = {apply_phase<VT, XT, PT>(a, first, beta, pk, pold)};
+        lap(0);
+        if (!grid_allreduce<1>(va, a.part_a, d)) return;
+        lap(1);
+        pq = va[0];
+        if (!(pq > 0 && pq < INFINITY)) {
+            done = (pq == pq) ? 3 : 2;
+            break;
+        }
+        const XT alpha = (XT)(rz / pq);
+        double vb[2] = {0, 0};
+        for (int i = gtid; i < a.nv; i += gstride) {
+            XT r[3], z[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const int j = 3 * i + c;
+                a.x[j] = ldcg(a.x + j) + alpha * ldcg(pk + j);
+                r[c] = ldcg(a.r + j) - alpha * (ldcg(a.qe + j) + ldcg(a.qc + j));
+                a.r[j] = r[c];
+                a.qc[j] = 0;
+            }
+            precond_vertex<XT, PT>(a.pinv, i, r, z);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                a.z[3 * i + c] = z[c];
+                vb[0] += (double)r[c] * (double)z[c];
+                vb[1] += (double)r[c] * (double)r[c];
+            }
+        }
+        lap(3);
+        if (!grid_allreduce<2>(vb, a.part_b, d)) return;
+        lap(4);
+        tot[0] = vb[0];
+        tot[1] = vb[1];
+        rz_prev = rz;
+        rz = tot[0];
+        rr = tot[1];
+        ++k;
+        if (!(rz == rz) || !(rr == rr)) done = 2;
+        else if (rr <= thr) done = 1;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        d->rr = rr;
+        d->bb = bb;
+        d->pq = pq;
+        d->it = k;
+        d->done = done;
+        for (int q = 0; q < 6; ++q) d->tphase[q] = tp[q];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kVecs = 8;  // r, z, P0, P1, q_e, q_c, and b, x of the FP32 inner solve
+
+struct PcgState {
+    DBuf<char> vec;              // kVecs vectors of 3 nv entries
+    DBuf<double> part;           // 3 partials per block
+    DBuf<PcgScalars> dsc;        // device scalars
+    PcgScalars* host = nullptr;  // pinned copy of the results
+    int grid[2] = {0, 0};        // co-resident grid per precision (0 FP64, 1 FP32)
+    ~PcgState()
+    {
+        if (host) cudaFreeHost(host);
+        vec.release();
+        part.release();
+        dsc.release();
+    }
+};
+
+template <typename VT, typename XT, typename PT>
+int coresident_grid(int nv)
+{
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_solve<VT, XT, PT>, kPcgThreads, 0);
+    if (e != cudaSuccess || per_sm < 1) return 0;
+    // every co-resident block: the apply phase has one work item per scalar row
+    // plus one per contact and friction constraint, so there is rarely spare room
+    (void)nv;
+    return per_sm * num_sms();
+}
+
+int state(Sim* s, PcgState** out)
+{
+    if (!s->pcg) {
+        PcgState* st = new PcgState();
+        if (st->dsc.alloc(1) != cudaSuccess || cudaMemset(st->dsc.p, 0, sizeof(PcgScalars)) != cudaSuccess ||
+            cudaMallocHost((void**)&st->host, sizeof(PcgScalars)) != cudaSuccess) {
+            delete st;
+            return set_error(CIPC_ERR_CUDA, "PCG state allocation");
+        }
+        st->grid[0] = coresident_grid<double, double, double>(s->nv);
+        st->grid[1] = coresident_grid<float, float, float>(s->nv);
+        const int g = std::max(st->grid[0], st->grid[1]);
+        if (g < 1 || st->part.alloc(3 * (size_t)g) != cudaSuccess) {
+            delete st;
+            return set_error(CIPC_ERR_CUDA, "PCG: no co-resident grid or partials allocation failed");
+        }
+        s->pcg = st;
+    }
+    *out = static_cast<PcgState*>(s->pcg);
+    return CIPC_OK;
+}
+
+int ensure_vectors(Sim* s, PcgState* st, size_t elem)
+{
+    const size_t vbytes = ((3 * (size_t)s->nv * elem + 255) & ~(size_t)255);
+    if (st->vec.n < kVecs * vbytes) {
+        cudaStreamSynchronize(s->stream);
+        if (st->vec.alloc(kVecs * vbytes) != cudaSuccess) return set_error(CIPC_ERR_CUDA, "PCG vectors");
+    }
+    return CIPC_OK;
+}
+
+template <typename VT, typename XT, typename PT>
+int solve(Sim* s, const XT* b, XT* x, double tol, int maxit, int* iters, double* rel)
+{
+    PcgState* st = nullptr;
+    int rc = state(s, &st);
+    if (rc || (rc = ensure_vectors(s, st, sizeof(XT)))) return rc;
+    cudaStream_t str = s->stream;
+    const size_t vbytes = ((3 * (size_t)s->nv * sizeof(XT) + 255) & ~(size_t)255);
+    auto vecp = [&](int k) { return reinterpret_cast<XT*>(st->vec.p + k * vbytes); };
+    const int g = st->grid[sizeof(XT) == 4 ? 1 : 0];
+    PcgArgs<VT, XT, PT> a;
+    std::memset(&a, 0, sizeof(a));
+    a.nv = s->nv;
+    a.ell_k = s->ell_k;
+    a.col = s->col.p;
+    a.val = reinterpret_cast<const VT*>(s->hval.p);
+    a.ckind = s->ckind.p;
+    a.cverts = s->cverts.p;
+    a.chess = reinterpret_cast<const VT*>(s->chess.p);
+    a.hs = (size_t)s->cap_con;
+    a.fkind = s->fkind.p;
+    a.fverts = s->fverts.p;
+    a.fw = s->fw.p;
+    a.fT = s->fT.p;
+    a.fM = reinterpret_cast<const double*>(s->fhess.p);
+    a.proj = s->proj.p;
+    a.pinv = reinterpret_cast<const PT*>(s->pinv.p);
+    a.b = b;
+    a.x = x;
+    a.r = vecp(0);
+    a.z = vecp(1);
+    a.P0 = vecp(2);
+    a.P1 = vecp(3);
+    a.qe = vecp(4);
+    a.qc = vecp(5);
+    a.part_a = st->part.p;
+    a.part_b = st->part.p + g;
+    a.d = st->dsc.p;
+    a.tol = tol;
+    a.maxit = maxit;
+    a.ncon = s->prm.withCollision ? s->ncon : 0;
+    a.nfric = (s->prm.withCollision && s->prm.mu > 0) ? s->nfric : 0;
+    a.trace = s->trace;
+    // barrier state starts clear (a previous solve may have given up mid-way)
+    cudaError_t e = cudaMemsetAsync(st->dsc.p, 0, sizeof(PcgScalars), str);
+    void* args[] = {&a};
+    if (e == cudaSuccess)
+        e = cudaLaunchCooperativeKernel((const void*)k_pcg_solve<VT, XT, PT>, dim3(g), dim3(kPcgThreads), args, 0,
+                                        str);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(st->host, st->dsc.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, str);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(str);
+    if (e != cudaSuccess) return set_cuda_error(e, "PCG");
+    const PcgScalars* h = st->host;
+    *iters = h->it;
+    *rel = h->bb > 0 ? std::sqrt(h->rr / h->bb) : 0.0;
+    if (s->trace) {
+        const double it = std::max(1, h->it);
+        std::fprintf(stderr,
+                     "cipc pcg: rel %.3e iters %d stop %d grid %d  us/iter: apply %.2f reduce %.2f update %.2f "
+                     "reduce %.2f\n",
+                     *rel, h->it, h->done, g, h->tphase[0] * 1e-3 / it, h->tphase[1] * 1e-3 / it,
+                     h->tphase[3] * 1e-3 / it, h->tphase[4] * 1e-3 / it);
+    }
+    if (h->err) return set_error(CIPC_ERR_CUDA, "PCG: grid barrier wait gave up");
+    if (h->done == 2) return set_error(CIPC_ERR_NAN, "PCG produced NaN");
+    if (h->done == 3) return set_error(CIPC_ERR_NOT_CONVERGED, "PCG: non-positive curvature (p, Hp) = %g", h->pq);
+    if (h->done == 4) return set_error(CIPC_ERR_NOT_CONVERGED, "PCG stopped at relative residual %g", *rel);
+    return CIPC_OK;
+}
+
+}  // namespace
+
+int pcg_solve_fp64(Sim* s, const double* b, double* x, double tol, int maxit, int* iters, double* rel)
+{
+    return solve<double, double, double>(s, b, x, tol, maxit, iters, rel);
+}
+
+int pcg_solve_fp32(Sim* s, const float* b, float* x, double tol, int maxit, int* iters, double* rel)
+{
+    return solve<float, float, float>(s, b, x, tol, maxit, iters, rel);
+}
+
+int pcg_fp32_io(Sim* s, float** b, float** x)
+{
+    PcgState* st = nullptr;
+    int rc = state(s, &st);
+    if (rc || (rc = ensure_vectors(s, st, sizeof(float)))) return rc;
+    const size_t vbytes = ((3 * (size_t)s->nv * sizeof(float) + 255) & ~(size_t)255);
+    *b = reinterpret_cast<float*>(st->vec.p + 6 * vbytes);
+    *x = reinterpret_cast<float*>(st->vec.p + 7 * vbytes);
+    return CIPC_OK;
+}
+
+void pcg_release(Sim* s)
+{
+    if (s->pcg) delete static_cast<PcgState*>(s->pcg);
+    s->pcg = nullptr;
+}
+
+}  // namespace cipc

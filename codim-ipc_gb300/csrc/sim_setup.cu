@@ -172,22 +172,26 @@ int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* t
     for (int e = 0; e < nh; ++e)
         for (int a = 0; a < 4; ++a)
             for (int b = 0; b < 4; ++b) adj[S.hinge[4 * e + a]].push_back(S.hinge[4 * e + b]);
-    S.row_ptr.assign(nv + 1, 0);
+    int K = 1;
     for (int i = 0; i < nv; ++i) {
         std::sort(adj[i].begin(), adj[i].end());
         adj[i].erase(std::unique(adj[i].begin(), adj[i].end()), adj[i].end());
-        S.row_ptr[i + 1] = S.row_ptr[i] + (int)adj[i].size();
+        K = std::max(K, (int)adj[i].size());
     }
-    S.col.resize(S.row_ptr[nv]);
+    if ((long long)K * nv >= (1ll << 31) / 9) return set_error(CIPC_ERR_INVALID_ARG, "mesh too large for the block pattern");
+    // ELL layout: block k of row i at k * nv + i, so that consecutive rows'
+    // k-th blocks are contiguous in memory
+    S.ell_k = K;
+    S.col.assign((size_t)K * nv, 0);
     S.diag.resize(nv);
-    for (int i = 0; i < nv; ++i) {
-        std::copy(adj[i].begin(), adj[i].end(), S.col.begin() + S.row_ptr[i]);
-        S.diag[i] = S.row_ptr[i] + (int)(std::lower_bound(adj[i].begin(), adj[i].end(), i) - adj[i].begin());
-    }
+    for (int i = 0; i < nv; ++i)
+        for (int k = 0; k < K; ++k) {
+            S.col[(size_t)k * nv + i] = k < (int)adj[i].size() ? adj[i][k] : i;
+            if (k < (int)adj[i].size() && adj[i][k] == i) S.diag[i] = k * nv + i;
+        }
     auto slot = [&](int r, int c) {
-        const int* b = S.col.data() + S.row_ptr[r];
-        const int* e = S.col.data() + S.row_ptr[r + 1];
-        return (int)(std::lower_bound(b, e, c) - S.col.data());
+        const int k = (int)(std::lower_bound(adj[r].begin(), adj[r].end(), c) - adj[r].begin());
+        return k * nv + r;
     };
     S.tri_slot.resize(9 * nt);
     for (int t = 0; t < nt; ++t)
@@ -237,12 +241,13 @@ int sim_upload(Sim* s, const HostScene& S)
     s->kbend = S.kbend;
     s->cell = S.cell;
     s->nnzb = (int)S.col.size();
+    s->ell_k = S.ell_k;
     cudaError_t e = cudaSuccess;
 #define UP(a, b)                       \
     if (e == cudaSuccess) e = up(a, b);
     UP(s->tri, S.tri) UP(s->hinge, S.hinge) UP(s->bnode, S.bnode) UP(s->bedge, S.bedge) UP(s->btri, S.btri)
     UP(s->P, S.P) UP(s->vol, S.vol) UP(s->hinfo, S.hinfo) UP(s->mass, S.mass) UP(s->b, S.b) UP(s->X0, S.X0)
-    UP(s->row_ptr, S.row_ptr) UP(s->col, S.col) UP(s->diag, S.diag) UP(s->tri_slot, S.tri_slot)
+    UP(s->col, S.col) UP(s->diag, S.diag) UP(s->tri_slot, S.tri_slot)
     UP(s->hinge_slot, S.hinge_slot)
 #undef UP
     const size_t n3 = 3 * (size_t)S.nv;

@@ -24,22 +24,24 @@
 #include "constraint_eval.cuh"
 #include "sim.h"
 #include "sim_kernels.h"
+#include "sim_pcg.h"
 
 namespace cipc {
 
 static inline int nblk(long long n, int bs) { return n > 0 ? (int)((n + bs - 1) / bs) : 1; }
 
 template <typename VT, typename XT>
-__global__ void __launch_bounds__(256) k_bsr_spmv(int nv, const int* __restrict__ row_ptr, const int* __restrict__ col,
+__global__ void __launch_bounds__(256) k_bsr_spmv(int nv, int ell_k, const int* __restrict__ col,
                                                   const VT* __restrict__ val, const XT* __restrict__ x,
                                                   XT* __restrict__ y)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
     XT a0 = 0, a1 = 0, a2 = 0;
-    for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
-        const int j = col[k];
-        const VT* B = val + 9 * (size_t)k;
+    for (int k = 0; k < ell_k; ++k) {
+        const size_t e = (size_t)k * nv + i;
+        const int j = col[e];
+        const VT* B = val + 9 * e;
         const XT x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
         a0 += (XT)B[0] * x0 + (XT)B[1] * x1 + (XT)B[2] * x2;
         a1 += (XT)B[3] * x0 + (XT)B[4] * x1 + (XT)B[5] * x2;
@@ -50,10 +52,11 @@ __global__ void __launch_bounds__(256) k_bsr_spmv(int nv, const int* __restrict_
     y[3 * i + 2] = a2;
 }
 
-// contact blocks: packed upper triangle (row by row) of the (3nv x 3nv) constraint Hessian
+// contact blocks: packed upper triangle (row by row) of the (3nv x 3nv) constraint
+// Hessian, entry h of constraint c at hess[h * hs + c]
 template <typename VT, typename XT>
 __global__ void __launch_bounds__(128) k_con_spmv(int n, const int* __restrict__ kind, const int4* __restrict__ verts,
-                                                  const VT* __restrict__ hess, const XT* __restrict__ x,
+                                                  const VT* __restrict__ hess, size_t hs, const XT* __restrict__ x,
                                                   XT* __restrict__ y)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -68,13 +71,13 @@ __global__ void __launch_bounds__(128) k_con_spmv(int n, const int* __restrict__
             xs[3 * q + d] = x[3 * id[q] + d];
             ys[3 * q + d] = 0;
         }
-    const VT* H = hess + 78 * (size_t)c;
-    int w = 0;
+    const VT* H = hess + c;
+    size_t w = 0;
     for (int p = 0; p < m; ++p) {
-        ys[p] += (XT)H[w] * xs[p];
+        ys[p] += (XT)H[w * hs] * xs[p];
         ++w;
         for (int q = p + 1; q < m; ++q, ++w) {
-            const XT h = (XT)H[w];
+            const XT h = (XT)H[w * hs];
             ys[p] += h * xs[q];
             ys[q] += h * xs[p];
         }
@@ -176,40 +179,6 @@ __global__ void k_dot_final(const double* part, int n, double* out)
     if (threadIdx.x == 0) *out = sh[0];
 }
 
-// z = Pinv r  (per vertex 3x3)
-template <typename XT, typename PT>
-__global__ void k_apply_precond(int nv, const PT* __restrict__ pinv, const XT* __restrict__ r, XT* __restrict__ z)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nv) return;
-    const PT* P = pinv + 9 * (size_t)i;
-    const XT r0 = r[3 * i], r1 = r[3 * i + 1], r2 = r[3 * i + 2];
-    z[3 * i] = (XT)P[0] * r0 + (XT)P[1] * r1 + (XT)P[2] * r2;
-    z[3 * i + 1] = (XT)P[3] * r0 + (XT)P[4] * r1 + (XT)P[5] * r2;
-    z[3 * i + 2] = (XT)P[6] * r0 + (XT)P[7] * r1 + (XT)P[8] * r2;
-}
-
-// x += alpha p ; r -= alpha q with alpha = sc[rz] / sc[pq]
-template <typename XT>
-__global__ void k_update_xr(int n, const double* sc, int irz, int ipq, const XT* p, const XT* q, XT* x, XT* r)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double den = sc[ipq];
-    const XT alpha = (XT)(den != 0 ? sc[irz] / den : 0.0);
-    x[i] += alpha * p[i];
-    r[i] -= alpha * q[i];
-}
-// p = z + beta p with beta = sc[rz_new] / sc[rz_old]
-template <typename XT>
-__global__ void k_update_p(int n, const double* sc, int inew, int iold, const XT* z, XT* p)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double den = sc[iold];
-    const XT beta = (XT)(den != 0 ? sc[inew] / den : 0.0);
-    p[i] = z[i] + beta * p[i];
-}
 template <typename A, typename B>
 __global__ void k_convert(int n, const A* a, B* b)
 {
@@ -262,64 +231,13 @@ template <typename VT, typename XT>
 static void apply_H(SolveCtx& C, const XT* x, XT* y)
 {
     Sim* s = C.s;
-    k_bsr_spmv<VT, XT><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, s->row_ptr.p, s->col.p, (const VT*)s->hval.p, x, y);
+    k_bsr_spmv<VT, XT><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, s->ell_k, s->col.p, (const VT*)s->hval.p, x, y);
     if (s->ncon > 0)
         k_con_spmv<VT, XT><<<nblk(s->ncon, 128), 128, 0, C.st>>>(s->ncon, s->ckind.p, s->cverts.p,
-                                                                  (const VT*)s->chess.p, x, y);
+                                                                  (const VT*)s->chess.p, (size_t)s->cap_con, x, y);
     if (s->nfric > 0 && s->prm.mu > 0)
         k_fric_spmv<XT><<<nblk(s->nfric, 128), 128, 0, C.st>>>(s->nfric, s->fkind.p, s->fverts.p, s->fw.p, s->fT.p,
                                                                 (const double*)s->fhess.p, s->proj.p, x, y);
-}
-
-// PCG on H x = b (x starts at 0).  Returns iterations; *rel = final |r|/|b| (read every `every` iterations).
-template <typename VT, typename XT>
-static int pcg(SolveCtx& C, const XT* b, XT* x, XT* r, XT* z, XT* p, XT* q, double tol, int maxit, double* rel)
-{
-    const int n = C.n3;
-    const int nb = nblk(n, 256);
-    Sim* s = C.s;
-    cudaMemsetAsync(x, 0, sizeof(XT) * n, C.st);
-    cudaMemcpyAsync(r, b, sizeof(XT) * n, cudaMemcpyDeviceToDevice, C.st);
-    double* sc = C.sc;  // [0] bb, [1] rz_a, [2] rz_b, [3] pq, [4] rr
-    dot<XT>(C, b, b, sc + 0);
-    if (s->prm.precision == 1)
-        k_apply_precond<XT, float><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, (const float*)s->pinv.p, r, z);
-    else
-        k_apply_precond<XT, double><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, (const double*)s->pinv.p, r, z);
-    cudaMemcpyAsync(p, z, sizeof(XT) * n, cudaMemcpyDeviceToDevice, C.st);
-    dot<XT>(C, r, z, sc + 1);
-    double bb = 0;
-    cudaMemcpyAsync(&bb, sc, sizeof(double), cudaMemcpyDeviceToHost, C.st);
-    cudaStreamSynchronize(C.st);
-    *rel = 0;
-    if (!(bb > 0)) return 0;
-    const double thr = tol * tol * bb;
-    int it = 0;
-    int cur = 1;
-    const int every = 8;
-    while (it < maxit) {
-        apply_H<VT, XT>(C, p, q);
-        dot<XT>(C, p, q, sc + 3);
-        k_update_xr<XT><<<nb, 256, 0, C.st>>>(n, sc, cur, 3, p, q, x, r);
-        ++it;
-        if (it % every == 0 || it == maxit) {
-            dot<XT>(C, r, r, sc + 4);
-            double rr = 0;
-            cudaMemcpyAsync(&rr, sc + 4, sizeof(double), cudaMemcpyDeviceToHost, C.st);
-            cudaStreamSynchronize(C.st);
-            *rel = std::sqrt(rr / bb);
-            if (rr <= thr || !(rr == rr)) break;
-        }
-        if (s->prm.precision == 1)
-            k_apply_precond<XT, float><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, (const float*)s->pinv.p, r, z);
-        else
-            k_apply_precond<XT, double><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, (const double*)s->pinv.p, r, z);
-        const int nxt = 3 - cur;
-        dot<XT>(C, r, z, sc + nxt);
-        k_update_p<XT><<<nb, 256, 0, C.st>>>(n, sc, nxt, cur, z, p);
-        cur = nxt;
-    }
-    return it;
 }
 
 // Finalizes the block-Jacobi preconditioner from the assembled matrix
@@ -336,40 +254,38 @@ static void build_precond(Sim* s)
 int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
 {
     const int n3 = 3 * s->nv;
-    const size_t need = (size_t)n3 * (6 * sizeof(double) + 6 * sizeof(float)) + 4096 * sizeof(double) + (1 << 16);
-    if (s->scratch.n < need) {
-        cudaStreamSynchronize(s->stream);
-        if (s->scratch.alloc(need) != cudaSuccess) return set_error(CIPC_ERR_CUDA, "solver scratch");
-    }
-    char* base = s->scratch.p;
-    size_t off = 0;
-    auto take = [&](size_t bytes) {
-        off = (off + 255) & ~(size_t)255;
-        char* p = base + off;
-        off += bytes;
-        return p;
-    };
-    SolveCtx C;
-    C.s = s;
-    C.st = s->stream;
-    C.n3 = n3;
-    C.nparts = std::min(nblk(n3, 256), 1024);
-    C.part = (double*)take(1024 * sizeof(double));
-    C.sc = (double*)take(64 * sizeof(double));
     build_precond(s);
     int total = 0;
     double rel = 0;
+    int rc = CIPC_OK;
     if (s->prm.precision != 1) {
-        double *r = (double*)take(n3 * 8), *z = (double*)take(n3 * 8), *p = (double*)take(n3 * 8),
-               *q = (double*)take(n3 * 8);
-        total = pcg<double, double>(C, rhs, sol, r, z, p, q, s->prm.pcg_tol, s->prm.pcg_maxit, &rel);
-        if (s->trace) std::fprintf(stderr, "cipc pcg: rel %.3e pcg %d\n", rel, total);
+        rc = pcg_solve_fp64(s, rhs, sol, s->prm.pcg_tol, s->prm.pcg_maxit, &total, &rel);
     } else {
         // mixed: FP32 inner PCG, FP64 iterative refinement of the residual
-        double* r64 = (double*)take(n3 * 8);
-        double* y64 = (double*)take(n3 * 8);
-        float *b32 = (float*)take(n3 * 4), *d32 = (float*)take(n3 * 4), *r = (float*)take(n3 * 4),
-              *z = (float*)take(n3 * 4), *p = (float*)take(n3 * 4), *q = (float*)take(n3 * 4);
+        const size_t need = (size_t)n3 * 2 * sizeof(double) + 4096 * sizeof(double) + (1 << 16);
+        if (s->scratch.n < need) {
+            cudaStreamSynchronize(s->stream);
+            if (s->scratch.alloc(need) != cudaSuccess) return set_error(CIPC_ERR_CUDA, "solver scratch");
+        }
+        char* base = s->scratch.p;
+        size_t off = 0;
+        auto take = [&](size_t bytes) {
+            off = (off + 255) & ~(size_t)255;
+            char* p = base + off;
+            off += bytes;
+            return p;
+        };
+        SolveCtx C;
+        C.s = s;
+        C.st = s->stream;
+        C.n3 = n3;
+        C.nparts = std::min(nblk(n3, 256), 1024);
+        C.part = (double*)take(1024 * sizeof(double));
+        C.sc = (double*)take(64 * sizeof(double));
+        double* r64 = (double*)take((size_t)n3 * 8);
+        double* y64 = (double*)take((size_t)n3 * 8);
+        float *b32 = nullptr, *d32 = nullptr;
+        if ((rc = pcg_fp32_io(s, &b32, &d32))) return rc;
         cudaMemsetAsync(sol, 0, sizeof(double) * n3, s->stream);
         cudaMemcpyAsync(r64, rhs, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s->stream);
         double* sc = C.sc;
@@ -387,7 +303,11 @@ int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
             const double inner_tol = std::min(0.5, std::max(0.5 * s->prm.pcg_tol * std::sqrt(bb / rr), 1e-5));
             k_convert_scaled<<<nblk(n3, 256), 256, 0, s->stream>>>(n3, r64, 1.0 / rn, b32);
             double relin = 0;
-            total += pcg<float, float>(C, b32, d32, r, z, p, q, inner_tol, s->prm.pcg_maxit - total, &relin);
+            int it = 0;
+            const int lr = pcg_solve_fp32(s, b32, d32, inner_tol, std::max(1, s->prm.pcg_maxit - total), &it, &relin);
+            total += it;
+            if (lr == CIPC_ERR_NAN || (lr != CIPC_OK && lr != CIPC_ERR_NOT_CONVERGED)) return lr;
+            if (it == 0 && lr != CIPC_OK) break;  // no progress possible (non-positive curvature)
             k_axpy_scaled<<<nblk(n3, 256), 256, 0, s->stream>>>(n3, d32, rn, sol);
             apply_H<float, double>(C, sol, y64);
             k_residual<<<nblk(n3, 256), 256, 0, s->stream>>>(n3, rhs, y64, r64);
@@ -399,13 +319,13 @@ int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
                 std::fprintf(stderr, "cipc refine %d: inner %.3e outer %.3e pcg %d\n", outer, relin, rel, total);
             if (rel <= s->prm.pcg_tol || total >= s->prm.pcg_maxit) break;
         }
+        rc = rel <= s->prm.pcg_tol ? CIPC_OK : set_error(CIPC_ERR_NOT_CONVERGED, "PCG stopped at relative residual %g", rel);
     }
     if (iters) *iters = total;
     cudaError_t e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) return set_cuda_error(e, "linear solve");
     if (!(rel == rel)) return set_error(CIPC_ERR_NAN, "linear solve produced NaN");
-    if (rel > s->prm.pcg_tol) return set_error(CIPC_ERR_NOT_CONVERGED, "PCG stopped at relative residual %g", rel);
-    return CIPC_OK;
+    return rc;
 }
 
 }  // namespace cipc

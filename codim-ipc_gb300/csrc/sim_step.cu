@@ -25,6 +25,7 @@
 #include "sim.h"
 #include "sim_host.h"
 #include "sim_kernels.h"
+#include "sim_pcg.h"
 
 namespace cipc {
 
@@ -190,6 +191,18 @@ int sim_step(Sim* s, StepStats* st)
     const int nv = s->nv, n3 = 3 * nv, nd = (int)s->dbc_idx_h.size();
     cudaStream_t str = s->stream;
     int rc = CIPC_OK;
+    // per-phase wall time, only with CIPC_TRACE (each mark waits for the stream):
+    // 0 setup, 1 constraint sets, 2 friction basis, 3 energies, 4 gradient +
+    // Hessian, 5 linear solves, 6 CCD step sizes, 7 other
+    double ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    auto tmark = clk::now();
+    auto mark = [&](int k) {
+        if (!s->trace) return;
+        cudaStreamSynchronize(str);
+        const auto now = clk::now();
+        ph[k] += std::chrono::duration<double, std::milli>(now - tmark).count();
+        tmark = now;
+    };
     cudaMemcpyAsync(s->xn.p, s->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
     launch_xtilde(s);
     // Dirichlet step (IMPLICIT_EULER.h:304-401): move the Dirichlet vertices to
@@ -217,16 +230,20 @@ int sim_step(Sim* s, StepStats* st)
             S.status = 1;  // penalty path taken
         }
     }
+    mark(0);
     s->ncon = 0;
     s->nfric = 0;
     s->npcon = 0;
     if (P.withCollision) {
         if ((rc = build_constraints(s, s->x.p))) return rc;
+        mark(1);
         if (P.mu > 0 && (rc = friction_basis(s, s->x.p))) return rc;
+        mark(2);
     }
     double Eprev;
     bool ok;
     if ((rc = eval_energy(s, s->x.p, &Eprev, &ok))) return rc;
+    mark(3);
     std::deque<double> res;
     int fricIterI = 0, it = 0;
     bool useGD = false;
@@ -239,6 +256,7 @@ int sim_step(Sim* s, StepStats* st)
         }
         eval_grad_hess(s, s->x.p, s->g.p, !useGD);
         k_neg<<<nblk(n3, 256), 256, 0, str>>>(n3, s->g.p, s->rhs.p);
+        mark(4);
         if (useGD) {
             cudaMemcpyAsync(s->dir.p, s->rhs.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
         } else {
@@ -252,10 +270,12 @@ int sim_step(Sim* s, StepStats* st)
                 return lr;
             }
         }
+        mark(5);
         // line search (IMPLICIT_EULER.h:9-149)
         cudaMemcpyAsync(s->xprev.p, s->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
         double alpha = 1.0;
         if (P.withCollision && (rc = ccd_step_size(s, s->xprev.p, s->dir.p, 1.0, &alpha))) return rc;
+        mark(6);
         const double feasible = alpha;
         double E = Eprev;
         int trials = 0;
@@ -267,9 +287,11 @@ int sim_step(Sim* s, StepStats* st)
             k_axpby<<<nblk(n3, 256), 256, 0, str>>>(n3, s->xprev.p, alpha, s->dir.p, s->x.p);
             if (P.withCollision) {
                 if ((rc = build_constraints(s, s->x.p))) return rc;
+                mark(1);
                 if (s->ncon > 0) {
                     double md;
                     if ((rc = min_d2(s, s->x.p, &md))) return rc;
+                    mark(7);
                     if (md <= 0) {
                         alpha /= 2;
                         E = Eprev + 1;
@@ -279,6 +301,7 @@ int sim_step(Sim* s, StepStats* st)
                 }
             }
             if ((rc = eval_energy(s, s->x.p, &E, &ok))) return rc;
+            mark(3);
             alpha /= 2;
         } while (E > Eprev || !ok);
         S.line_search_trials += trials;
@@ -320,6 +343,7 @@ int sim_step(Sim* s, StepStats* st)
         if (s->trace)
             std::fprintf(stderr, "cipc newton %d: res %.3e L2 %.3e kappa %.6g dbc_stiff %.3g ncon %d\n", it, cur, L2,
                          s->kappa, s->dbc_stiff, s->ncon);
+        mark(7);
         // augmented-Lagrangian Dirichlet progress (IMPLICIT_EULER.h:713-764)
         if (s->dbc_stiff != 0) {
             const double progress = 1 - std::sqrt(dbc_dist2(s, s->x.p) / dbcPenaltyXn);
@@ -350,6 +374,7 @@ int sim_step(Sim* s, StepStats* st)
             }
         }
     } while (res.size() < 3 || L2 > P.tol);
+    mark(7);
     k_velocity<<<nblk(n3, 256), 256, 0, str>>>(n3, s->x.p, s->xn.p, P.h, s->v.p);
     S.newton_iters = it;
     S.n_constraints = s->ncon;
@@ -358,6 +383,11 @@ int sim_step(Sim* s, StepStats* st)
     cudaError_t e = cudaStreamSynchronize(str);
     if (e != cudaSuccess) return set_cuda_error(e, "step");
     S.ms = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+    if (s->trace)
+        std::fprintf(stderr,
+                     "cipc step: %.2f ms  setup %.2f  sets %.2f  fbasis %.2f  energy %.2f  gradhess %.2f  solve %.2f  "
+                     "ccd %.2f  other %.2f  (newton %d pcg %d)\n",
+                     S.ms, ph[0], ph[1], ph[2], ph[3], ph[4], ph[5], ph[6], ph[7], it, S.pcg_iters);
     *st = S;
     return rc;
 }
@@ -366,7 +396,8 @@ void sim_destroy(Sim* s)
 {
     if (!s) return;
     cudaStreamSynchronize(s->stream);
-    for (DBuf<int>* b : {&s->tri, &s->hinge, &s->bnode, &s->bedge, &s->btri, &s->dbc_idx, &s->row_ptr, &s->col,
+    pcg_release(s);
+    for (DBuf<int>* b : {&s->tri, &s->hinge, &s->bnode, &s->bedge, &s->btri, &s->dbc_idx, &s->col,
                          &s->diag, &s->tri_slot, &s->hinge_slot, &s->ckind, &s->cmult, &s->fkind, &s->fmult,
                          &s->pkind})
         b->release();
