@@ -207,3 +207,67 @@ class Shell:
 
 def num_threads():
     return lib().orc_num_threads()
+
+
+class LearnedSystem:
+    """One Newton system in the learned preconditioner's terms (oracle_learned.cpp):
+    ELL elastic blocks (K x nv, block k of row i at k*nv+i), the contact/friction
+    part of the diagonal blocks, the Dirichlet mask and the contact blocks."""
+
+    def __init__(self, col, val, cdiag, proj, ckind, cverts, chess):
+        self.col = _c(col, np.int32)
+        self.K = self.col.shape[0]
+        self.nv = self.col.shape[1]
+        self.val = _c(val, np.float32)
+        self.cdiag = _c(cdiag, np.float32)
+        self.proj = _c(proj, np.uint8)
+        self.ckind = _c(ckind, np.int32)
+        self.cverts = _c(cverts, np.int32)
+        self.chess = _c(chess, np.float32)
+        self.ncon = self.ckind.shape[0]
+
+
+def _lp_sigs():
+    L = lib()
+    L.orc_lp_num_params.restype = ctypes.c_int
+    L.orc_lp_num_params.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.orc_lp_features.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, ctypes.c_int, _P, _P, _P, _P, _P]
+    L.orc_lp_loss_grad.restype = ctypes.c_double
+    L.orc_lp_loss_grad.argtypes = [ctypes.c_int, ctypes.c_int, _P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P,
+                                   ctypes.c_int, _P, _P, _P, _P, _P, _P, _P]
+    L.orc_lp_apply.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int, _P, _P, _P, _P, _P]
+    return L
+
+
+def lp_num_params(hidden, layers):
+    return _lp_sigs().orc_lp_num_params(hidden, layers)
+
+
+def lp_features(S):
+    L = _lp_sigs()
+    x = np.zeros((S.nv, 10))
+    a = np.zeros((S.K, S.nv))
+    E = np.zeros((S.nv, 3, 3))
+    L.orc_lp_features(S.nv, S.K, _p(S.col), _p(S.val), _p(S.cdiag), _p(S.proj), S.ncon, _p(S.ckind),
+                      _p(S.cverts), _p(x), _p(a), _p(E))
+    return x, a, E
+
+
+def lp_loss_grad(hidden, layers, params, S, r, p):
+    """(loss, gradient, z) of one triple in double precision."""
+    L = _lp_sigs()
+    prm = _c(params, np.float64)
+    g = np.zeros(prm.shape[0])
+    z = np.zeros((S.nv, 3))
+    loss = L.orc_lp_loss_grad(hidden, layers, _p(prm), S.nv, S.K, _p(S.col), _p(S.val), _p(S.cdiag), _p(S.proj),
+                              S.ncon, _p(S.ckind), _p(S.cverts), _p(S.chess), _p(_c(r, np.float64)),
+                              _p(_c(p, np.float64)), _p(g), _p(z))
+    return loss, g, z
+
+
+def lp_apply(S, x):
+    L = _lp_sigs()
+    y = np.zeros((S.nv, 3))
+    L.orc_lp_apply(S.nv, S.K, _p(S.col), _p(S.val), S.ncon, _p(S.ckind), _p(S.cverts), _p(S.chess),
+                   _p(_c(x, np.float64)), _p(y))
+    return y
