@@ -187,7 +187,8 @@ class StepParams(ctypes.Structure):
 class StepStats(ctypes.Structure):
     _fields_ = [("newton_iters", ctypes.c_int), ("pcg_iters", ctypes.c_int), ("line_search_trials", ctypes.c_int),
                 ("n_constraints", ctypes.c_int), ("status", ctypes.c_int), ("min_dist2", ctypes.c_double),
-                ("kappa", ctypes.c_double), ("ms", ctypes.c_double)]
+                ("kappa", ctypes.c_double), ("ms", ctypes.c_double), ("precond_fallbacks", ctypes.c_int),
+                ("learned_solves", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -301,3 +302,106 @@ class Sim:
         _check(lib().cipc_sim_ccd(self.h, ctypes.byref(params), xa.ctypes.data, da.ctypes.data, alpha,
                                   ctypes.byref(out)))
         return out.value
+
+
+_c_u64 = ctypes.c_uint64
+_SIGS.update({
+    "cipc_precond_create": (_c_int, [_c_int, _c_int, _c_u64, _PP]),
+    "cipc_precond_destroy": (_c_int, [_vp]),
+    "cipc_precond_num_params": (_c_int, [_vp]),
+    "cipc_precond_get_params": (_c_int, [_vp, _vp]),
+    "cipc_precond_set_params": (_c_int, [_vp, _vp]),
+    "cipc_precond_set_loss": (_c_int, [_vp, _c_int]),
+    "cipc_precond_num_systems": (_c_int, [_vp]),
+    "cipc_precond_clear_systems": (_c_int, [_vp]),
+    "cipc_precond_train": (_c_int, [_vp, _c_int, _c_int, _c_dbl, _c_u64, _vp, _vp]),
+    "cipc_precond_loss_grad": (_c_int, [_vp, _c_int, _vp, _vp]),
+    "cipc_precond_system_sizes": (_c_int, [_vp, _c_int, _vp]),
+    "cipc_precond_system_export": (_c_int, [_vp, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "cipc_sim_capture_systems": (_c_int, [_vp, _vp, _c_int]),
+    "cipc_sim_set_precond": (_c_int, [_vp, _vp]),
+})
+if _lib is not None:
+    for _name in [k for k in _SIGS if k.startswith("cipc_precond") or k in ("cipc_sim_capture_systems",
+                                                                               "cipc_sim_set_precond")]:
+        _f = getattr(_lib, _name)
+        _f.restype, _f.argtypes = _SIGS[_name]
+
+
+class Precond:
+    """Owns one cipc_precond handle (learned block-Jacobi correction)."""
+
+    def __init__(self, hidden=32, layers=2, seed=0):
+        h = ctypes.c_void_p()
+        _check(lib().cipc_precond_create(hidden, layers, seed, ctypes.byref(h)))
+        self.h = h
+        self.hidden, self.layers = hidden, layers
+        self.loss_kind = 0
+
+    def close(self):
+        if self.h:
+            lib().cipc_precond_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def num_params(self):
+        return lib().cipc_precond_num_params(self.h)
+
+    def params(self):
+        out = np.zeros(self.num_params(), np.float32)
+        _check(lib().cipc_precond_get_params(self.h, out.ctypes.data))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.shape[0] == self.num_params()
+        _check(lib().cipc_precond_set_params(self.h, p.ctypes.data))
+
+    def num_systems(self):
+        return lib().cipc_precond_num_systems(self.h)
+
+    def set_loss(self, kind):
+        _check(lib().cipc_precond_set_loss(self.h, kind))
+        self.loss_kind = kind
+
+    def clear_systems(self):
+        _check(lib().cipc_precond_clear_systems(self.h))
+
+    def train(self, epochs, batch=4, lr=1e-3, seed=0):
+        b = ctypes.c_double()
+        a = ctypes.c_double()
+        _check(lib().cipc_precond_train(self.h, epochs, batch, lr, seed, ctypes.byref(b), ctypes.byref(a)))
+        return b.value, a.value
+
+    def loss_grad(self, system):
+        loss = ctypes.c_double()
+        g = np.zeros(self.num_params(), np.float32)
+        _check(lib().cipc_precond_loss_grad(self.h, system, ctypes.byref(loss), g.ctypes.data))
+        return loss.value, g
+
+    def export_system(self, system):
+        sz = np.zeros(4, np.int32)
+        _check(lib().cipc_precond_system_sizes(self.h, system, sz.ctypes.data))
+        nv, K, nc, nf = [int(v) for v in sz]
+        out = dict(col=np.zeros((K, nv), np.int32), val=np.zeros((K, nv, 9), np.float32),
+                   cdiag=np.zeros((nv, 9), np.float32), proj=np.zeros(nv, np.uint8),
+                   ckind=np.zeros(nc, np.int32), cverts=np.zeros((nc, 4), np.int32),
+                   chess=np.zeros((nc, 78), np.float32), rhs=np.zeros((nv, 3), np.float32),
+                   sol=np.zeros((nv, 3), np.float32))
+        _check(lib().cipc_precond_system_export(self.h, system, *[out[k].ctypes.data for k in (
+            "col", "val", "cdiag", "proj", "ckind", "cverts", "chess", "rhs", "sol")]))
+        out["n_friction"] = nf
+        return out
+
+
+def sim_capture_systems(sim, precond, max_systems):
+    _check(lib().cipc_sim_capture_systems(sim.h, precond.h if precond is not None else None, max_systems))
+
+
+def sim_set_precond(sim, precond):
+    _check(lib().cipc_sim_set_precond(sim.h, precond.h if precond is not None else None))

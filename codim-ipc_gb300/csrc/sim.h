@@ -70,6 +70,8 @@ struct StepStats {
     double min_dist2 = 0;
     double kappa = 0;
     double ms = 0;
+    int precond_fallbacks = 0;
+    int learned_solves = 0;
 };
 
 struct Sim {
@@ -127,8 +129,11 @@ struct Sim {
     StepStats last;
     // graph-replayed PCG (sim_pcg.cu)
     void* pcg = nullptr;
-    // learned preconditioner (optional)
+    // learned preconditioner (LpModel, optional): used when prm.precond == 1;
+    // capture: every solved Newton system is appended to that model's data
     void* learned = nullptr;
+    void* capture = nullptr;
+    int solve_fallbacks = 0, solve_learned = 0;  // counts of the current step
     std::vector<double> host_mass;
 };
 

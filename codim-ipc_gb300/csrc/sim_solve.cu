@@ -25,6 +25,7 @@
 #include "sim.h"
 #include "sim_kernels.h"
 #include "sim_pcg.h"
+#include "learned.h"
 
 namespace cipc {
 
@@ -251,10 +252,10 @@ static void build_precond(Sim* s)
                                                                             s->pdiag.p, (double*)s->pinv.p);
 }
 
-int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
+// PCG (FP64, or FP32 inside FP64 refinement) with the preconditioner already in s->pinv
+static int solve_with_precond(Sim* s, const double* rhs, double* sol, int* iters)
 {
     const int n3 = 3 * s->nv;
-    build_precond(s);
     int total = 0;
     double rel = 0;
     int rc = CIPC_OK;
@@ -325,6 +326,33 @@ int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
     cudaError_t e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) return set_cuda_error(e, "linear solve");
     if (!(rel == rel)) return set_error(CIPC_ERR_NAN, "linear solve produced NaN");
+    return rc;
+}
+
+int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
+{
+    bool learned = false;
+    if (s->prm.precond == 1 && s->learned) learned = lp_precond(s, static_cast<LpModel*>(s->learned)) == CIPC_OK;
+    if (!learned) build_precond(s);
+    int total = 0, it = 0;
+    int rc = solve_with_precond(s, rhs, sol, &it);
+    total += it;
+    if (learned) {
+        ++s->solve_learned;
+        if (rc == CIPC_ERR_NOT_CONVERGED || rc == CIPC_ERR_NAN) {
+            // the learned preconditioner stalled or broke down: plain block Jacobi
+            // solves the same system (and is the yardstick for the network)
+            ++s->solve_fallbacks;
+            build_precond(s);
+            rc = solve_with_precond(s, rhs, sol, &it);
+            total += it;
+        }
+    }
+    if (iters) *iters = total;
+    if (rc == CIPC_OK && s->capture) {
+        const int crc = lp_capture(s, static_cast<LpModel*>(s->capture), rhs, sol);
+        if (crc) return crc;
+    }
     return rc;
 }
 

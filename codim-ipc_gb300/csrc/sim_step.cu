@@ -26,6 +26,7 @@
 #include "sim_host.h"
 #include "sim_kernels.h"
 #include "sim_pcg.h"
+#include "learned.h"
 
 namespace cipc {
 
@@ -187,6 +188,8 @@ int sim_step(Sim* s, StepStats* st)
     using clk = std::chrono::steady_clock;
     const auto t0 = clk::now();
     StepStats S;
+    s->solve_fallbacks = 0;
+    s->solve_learned = 0;
     const SimParams& P = s->prm;
     const int nv = s->nv, n3 = 3 * nv, nd = (int)s->dbc_idx_h.size();
     cudaStream_t str = s->stream;
@@ -383,6 +386,8 @@ int sim_step(Sim* s, StepStats* st)
     cudaError_t e = cudaStreamSynchronize(str);
     if (e != cudaSuccess) return set_cuda_error(e, "step");
     S.ms = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+    S.precond_fallbacks = s->solve_fallbacks;
+    S.learned_solves = s->solve_learned;
     if (s->trace)
         std::fprintf(stderr,
                      "cipc step: %.2f ms  setup %.2f  sets %.2f  fbasis %.2f  energy %.2f  gradhess %.2f  solve %.2f  "
@@ -572,6 +577,8 @@ extern "C" int cipc_sim_step(cipc_sim* h, const cipc_step_params* p, cipc_step_s
         stats->min_dist2 = S.min_dist2;
         stats->kappa = S.kappa;
         stats->ms = S.ms;
+        stats->precond_fallbacks = S.precond_fallbacks;
+        stats->learned_solves = S.learned_solves;
     }
     return rc;
 }
@@ -638,4 +645,23 @@ extern "C" int cipc_sim_ccd(cipc_sim* h, const cipc_step_params* p, const double
     cudaMemcpyAsync(s->xprev.p, x, b, cudaMemcpyHostToDevice, s->stream);
     cudaMemcpyAsync(s->disp.p, dir, b, cudaMemcpyHostToDevice, s->stream);
     return ccd_step_size(s, s->xprev.p, s->disp.p, alpha, alpha_out);
+}
+
+extern "C" int cipc_sim_capture_systems(cipc_sim* h, cipc_precond* p, int max_systems)
+{
+    if (int rc = check_sim(h)) return rc;
+    LpModel* m = lp_model(p);
+    if (p && !m) return set_error(CIPC_ERR_INVALID_ARG, "cipc_sim_capture_systems: bad preconditioner handle");
+    if (m) m->capture_max = std::max(0, max_systems);
+    h->s->capture = (m && max_systems > 0) ? m : nullptr;
+    return CIPC_OK;
+}
+
+extern "C" int cipc_sim_set_precond(cipc_sim* h, cipc_precond* p)
+{
+    if (int rc = check_sim(h)) return rc;
+    LpModel* m = lp_model(p);
+    if (p && !m) return set_error(CIPC_ERR_INVALID_ARG, "cipc_sim_set_precond: bad preconditioner handle");
+    h->s->learned = m;
+    return CIPC_OK;
 }

@@ -166,6 +166,8 @@ typedef struct cipc_step_stats {
     double min_dist2;       /* min over constraints of d^2 - xi^2 at the end of the step */
     double kappa;           /* barrier stiffness after the step (kappaVec[0]) */
     double ms;              /* wall time of the step */
+    int precond_fallbacks;  /* linear solves where the learned preconditioner stalled and block Jacobi re-solved */
+    int learned_solves;     /* linear solves that used the learned preconditioner */
 } cipc_step_stats;
 
 typedef struct cipc_sim cipc_sim;
@@ -204,6 +206,63 @@ int cipc_sim_eval(cipc_sim* sim, const cipc_step_params* params, const double* x
                   double* energy, double* grad);
 int cipc_sim_ccd(cipc_sim* sim, const cipc_step_params* params, const double* x, const double* dir, double alpha,
                  double* alpha_out);
+
+/* ------------------------------------------------------------------------
+ * Learned block-Jacobi correction for the Newton-system PCG (no reference
+ * counterpart: the reference factorizes every Newton system with CHOLMOD,
+ * Library/Math/DIRECT_SOLVER.h:13-88, and has no iterative solver to precondition).
+ *
+ * A message-passing network over the vertices of the Newton system (edges: the
+ * elastic off-diagonal blocks and the active contact constraints) maps
+ * scale-free features of each vertex's 3x3 diagonal block D_i and couplings to a
+ * lower-triangular Cm_i; the preconditioner block is Cm_i D_i^-1 Cm_i^T, so the
+ * untrained network (zero output layer) is plain block Jacobi.  PCG still stops
+ * at the same relative residual, so the network changes iteration counts, not
+ * answers; a solve that stalls or breaks down is repeated with block Jacobi.
+ * Training data are the (H, r, p) systems the solver itself produces: attach a
+ * preconditioner with cipc_sim_capture_systems, step, then train.  Loss per
+ * system: 1 - (z.r)^2 / ((z.Hz)(r.p)), z = M^-1 r, the relative H-norm error
+ * left after one preconditioned step.  All work runs on the current device;
+ * a handle is not thread-safe and must outlive the simulations using it.
+ * ------------------------------------------------------------------------ */
+typedef struct cipc_precond cipc_precond;
+
+/* hidden: 16 or 32 channels; layers: 1..8 message-passing layers; seed fixes the
+ * initial weights. */
+int cipc_precond_create(int hidden, int layers, uint64_t seed, cipc_precond** out);
+int cipc_precond_destroy(cipc_precond* p);
+/* number of float parameters (or -1 for a bad handle); get/set copy them host-side */
+int cipc_precond_num_params(const cipc_precond* p);
+int cipc_precond_get_params(const cipc_precond* p, float* out);
+int cipc_precond_set_params(cipc_precond* p, const float* in);
+/* training loss per system: 0 (default) 1 - (z.r)^2 / ((z.Hz)(r.p)), the error of
+ * the optimally scaled step; 1 |z - p|_H^2 / |p|_H^2, the error of the unit step */
+int cipc_precond_set_loss(cipc_precond* p, int kind);
+/* captured Newton systems: count (or -1) and clearing */
+int cipc_precond_num_systems(const cipc_precond* p);
+int cipc_precond_clear_systems(cipc_precond* p);
+/* Adam over the captured systems (minibatches of `batch` systems, `epochs` passes,
+ * order shuffled with `seed`); mean loss before and after training (optional). */
+int cipc_precond_train(cipc_precond* p, int epochs, int batch, double lr, uint64_t seed, double* loss_before,
+                       double* loss_after);
+/* Loss of captured system `system` and the parameter gradient (num_params floats,
+ * optional) at the current parameters. */
+int cipc_precond_loss_grad(cipc_precond* p, int system, double* loss, float* grad);
+/* sizes4 = (n_verts, ell_k, n_contacts, n_friction) of a captured system, and its
+ * arrays: ELL columns (ell_k x n_verts, block k of row i at k*n_verts+i), ELL blocks
+ * (9 floats each), contact/friction part of the diagonal blocks (9 per vertex),
+ * Dirichlet mask, contact kinds and vertices (4 per contact), contact blocks (78
+ * per contact, packed upper triangle row by row), right-hand side and solution
+ * (3 per vertex).  Any output may be NULL. */
+int cipc_precond_system_sizes(const cipc_precond* p, int system, int32_t* sizes4);
+int cipc_precond_system_export(const cipc_precond* p, int system, int32_t* col, float* val, float* cdiag,
+                               uint8_t* proj, int32_t* ckind, int32_t* cverts, float* chess, float* rhs,
+                               float* sol);
+/* Append every Newton system the simulation solves (up to max_systems in p) to p's
+ * training data; p = NULL or max_systems = 0 stops capturing. */
+int cipc_sim_capture_systems(cipc_sim* sim, cipc_precond* p, int max_systems);
+/* Preconditioner used by steps with params.preconditioner = 1 (NULL: block Jacobi). */
+int cipc_sim_set_precond(cipc_sim* sim, cipc_precond* p);
 
 #ifdef __cplusplus
 }

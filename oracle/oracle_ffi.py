@@ -42,7 +42,9 @@ def lib():
 
 
 def _p(a):
-    return None if a is None else a.ctypes.data
+    # the ctypes pointer keeps a reference to the array, so a converted temporary
+    # (``_p(_c(x, ...))``) stays alive for the duration of the call
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
 def _c(a, dt):
@@ -234,7 +236,7 @@ def _lp_sigs():
     L.orc_lp_features.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, ctypes.c_int, _P, _P, _P, _P, _P]
     L.orc_lp_loss_grad.restype = ctypes.c_double
     L.orc_lp_loss_grad.argtypes = [ctypes.c_int, ctypes.c_int, _P, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P,
-                                   ctypes.c_int, _P, _P, _P, _P, _P, _P, _P]
+                                   ctypes.c_int, _P, _P, _P, _P, _P, _P, _P, ctypes.c_int]
     L.orc_lp_apply.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int, _P, _P, _P, _P, _P]
     return L
 
@@ -253,7 +255,7 @@ def lp_features(S):
     return x, a, E
 
 
-def lp_loss_grad(hidden, layers, params, S, r, p):
+def lp_loss_grad(hidden, layers, params, S, r, p, kind=0):
     """(loss, gradient, z) of one triple in double precision."""
     L = _lp_sigs()
     prm = _c(params, np.float64)
@@ -261,7 +263,7 @@ def lp_loss_grad(hidden, layers, params, S, r, p):
     z = np.zeros((S.nv, 3))
     loss = L.orc_lp_loss_grad(hidden, layers, _p(prm), S.nv, S.K, _p(S.col), _p(S.val), _p(S.cdiag), _p(S.proj),
                               S.ncon, _p(S.ckind), _p(S.cverts), _p(S.chess), _p(_c(r, np.float64)),
-                              _p(_c(p, np.float64)), _p(g), _p(z))
+                              _p(_c(p, np.float64)), _p(g), _p(z), int(kind))
     return loss, g, z
 
 

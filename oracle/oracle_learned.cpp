@@ -17,8 +17,9 @@
 //   o = Wo h + bo (6) ; e_a = exp(0.5 clamp(o_a, -8, 8))
 //   Cm = [[e0,0,0],[o3,e1,0],[o4,o5,e2]] ; P_i = Cm D_i^-1 Cm^T ; z_i = P_i r_i
 // With Wo = 0, bo = 0 (the initial state) P_i = D_i^-1: plain block Jacobi.
-// Loss of one (H, r, p) triple, p = H^-1 r:  L = 1 - (z.r)^2 / ((z.Hz)(r.p)),
-// the relative H-norm error left after one preconditioned step.
+// Loss of one (H, r, p) triple, p = H^-1 r, kind 0:  L = 1 - (z.r)^2 / ((z.Hz)(r.p)),
+// the relative H-norm error left after one optimally scaled preconditioned step;
+// kind 1:  L = |z - p|_H^2 / |p|_H^2, the same error for the unit step.
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -330,7 +331,7 @@ void dgrad(int nv, int Ho, int Hi, const double* W, const std::vector<double>& d
 
 // loss and its gradient with respect to the parameters; returns the loss
 double loss_grad(const Net& N, const Graph& G, const Prep& P, const double* r, const double* p, Acts& A, double* grad,
-                 int nparams)
+                 int nparams, int kind)
 {
     const int nv = G.nv, H = N.H, L = N.L;
     forward(N, G, P, r, A);
@@ -344,9 +345,10 @@ double loss_grad(const Net& N, const Graph& G, const Prep& P, const double* r, c
     }
     for (int k = 0; k < nparams; ++k) grad[k] = 0;
     if (!(b > 0) || !(c > 0)) return 0;
-    const double loss = 1 - a * a / (b * c);
-    // dL/dz = (2a/(bc)) (-r + (a/b) Hz)
-    const double f = 2 * a / (b * c), t = a / b;
+    // kind 0: 1 - a^2/(bc), dL/dz = (2a/(bc)) (-r + (a/b) Hz)
+    // kind 1: |z - p|_H^2 / |p|_H^2 = (b - 2a + c)/c, dL/dz = (2/c) (-r + Hz)
+    const double loss = kind == 1 ? (b - 2 * a + c) / c : 1 - a * a / (b * c);
+    const double f = kind == 1 ? 2 / c : 2 * a / (b * c), t = kind == 1 ? 1.0 : a / b;
     // parameter gradient views (same layout as Net)
     double* gW0 = grad;
     double* gb0 = gW0 + H * F;
@@ -463,7 +465,7 @@ void orc_lp_features(int nv, int K, const int* col, const float* val, const floa
 // of one (H, r, p) triple.
 double orc_lp_loss_grad(int H, int L, const double* params, int nv, int K, const int* col, const float* val,
                         const float* cdiag, const uint8_t* proj, int ncon, const int* ckind, const int* cverts,
-                        const float* chess, const double* r, const double* p, double* grad, double* z_out)
+                        const float* chess, const double* r, const double* p, double* grad, double* z_out, int kind)
 {
     Graph G{nv, K, col, val, cdiag, proj, ncon, ckind, cverts, chess};
     Prep P;
@@ -471,7 +473,7 @@ double orc_lp_loss_grad(int H, int L, const double* params, int nv, int K, const
     Net N(H, L, params);
     Acts A;
     std::vector<double> gtmp(orc_lp_num_params(H, L));
-    const double loss = loss_grad(N, G, P, r, p, A, grad ? grad : gtmp.data(), orc_lp_num_params(H, L));
+    const double loss = loss_grad(N, G, P, r, p, A, grad ? grad : gtmp.data(), orc_lp_num_params(H, L), kind);
     if (z_out) std::memcpy(z_out, A.z.data(), sizeof(double) * A.z.size());
     return loss;
 }
