@@ -162,6 +162,78 @@ def _time_calls(fn, steps, stream):
     return start.elapsed_time(stop), per
 
 
+def timestep_variants(args):
+    """ms/timestep of the cloth-on-rotating-sphere scene (200x200 cloth, 2 m, sphere
+    r 0.5 m at 2 rad/s, mu 0.4, xi 0.5 mm, dhat 1 mm, dt 0.02, Newton tol 1e-3):
+    plain FP64 block-Jacobi PCG vs FP32 Hessians + FP64 refinement, with block
+    Jacobi and with the learned correction trained on systems the plain mixed
+    solver captured while draping.  Every variant starts from the same draped
+    state and advances ts_steps steps."""
+    import cipc_ffi as F
+    import workloads
+
+    X, T, dbc, c = workloads.cloth_on_sphere(n=args.ts_n)
+    dt, omega = 0.02, 2.0
+
+    def target(k):
+        return workloads.rotate_y(X[dbc], c, omega * dt * (k + 1))
+
+    def make(prec, pre):
+        s = F.Sim(X, T, 200.0, 1e5, 0.3, 1e-3)
+        _, dhat2 = s.init_oipc(1e-3)
+        prm = F.make_params(dt, dhat2, 5e-4, mu=0.4, epsv2=1e-6, fric_iters=1, newton_tol=1e-3, precision=prec,
+                            pcg_tol=1e-4, preconditioner=pre)
+        return s, prm
+
+    ok = (F.CIPC_ERR_NOT_CONVERGED,)
+    s, prm = make(F.MIXED, 0)
+    pc = F.Precond(hidden=16, layers=2, seed=0)
+    cap_from = max(0, args.ts_warm - 6)
+    for k in range(args.ts_warm):
+        if k == cap_from:
+            F.sim_capture_systems(s, pc, 512)
+        s.set_dbc(dbc, target(k))
+        s.step(prm, allow=ok)
+    F.sim_capture_systems(s, None, 0)
+    x0, v0 = s.state()
+    k0 = s.kappa()
+    s.close()
+    t0 = time.perf_counter()
+    loss_before, loss_after = pc.train(epochs=args.ts_epochs, batch=8, lr=1e-3, seed=0)
+    train_s = time.perf_counter() - t0
+    out = {"workload": "cloth on rotating sphere, %dx%d cloth (%d vertices incl. sphere), %d steps from step %d"
+                       % (args.ts_n, args.ts_n, X.shape[0], args.ts_steps, args.ts_warm),
+           "unit": "ms/timestep", "newton_tol": 1e-3, "pcg_tol": 1e-4,
+           "learned": {"systems": pc.num_systems(), "epochs": args.ts_epochs, "train_s": round(train_s, 2),
+                       "loss_before": round(loss_before, 4), "loss_after": round(loss_after, 4)}}
+    for name, prec, pre in (("fp64_block_jacobi", F.FP64, 0), ("mixed_block_jacobi", F.MIXED, 0),
+                            ("mixed_learned", F.MIXED, 1)):
+        sv, pv = make(prec, pre)
+        if pre:
+            F.sim_set_precond(sv, pc)
+        sv.set_state(x0, v0)
+        sv.set_kappa(k0[0], k0[1])
+        rows = []
+        for k in range(args.ts_warm, args.ts_warm + args.ts_steps):
+            sv.set_dbc(dbc, target(k))
+            st = sv.step(pv, allow=ok)
+            rows.append(st.as_dict())
+        sv.close()
+        out[name] = {"ms_per_step": round(float(np.mean([r["ms"] for r in rows])), 2),
+                     "newton_per_step": round(float(np.mean([r["newton_iters"] for r in rows])), 2),
+                     "pcg_per_step": round(float(np.mean([r["pcg_iters"] for r in rows])), 1),
+                     "fallbacks": int(sum(r["precond_fallbacks"] for r in rows)),
+                     "min_dist2_min": float(min(r["min_dist2"] for r in rows)),
+                     "intersection_free": bool(all(r["min_dist2"] > 0 or r["n_constraints"] == 0 for r in rows)),
+                     "status": sorted(set(int(r["status"]) for r in rows))}
+    out["speedup_mixed_learned_vs_fp64"] = round(out["fp64_block_jacobi"]["ms_per_step"]
+                                                 / out["mixed_learned"]["ms_per_step"], 3)
+    out["speedup_mixed_vs_fp64"] = round(out["fp64_block_jacobi"]["ms_per_step"]
+                                         / out["mixed_block_jacobi"]["ms_per_step"], 3)
+    pc.close()
+    return out
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -303,6 +375,8 @@ def run_ours(args):
             "variants": variants,
             "cpu_baseline": cpu,
         }
+        if ws == 1 and not args.no_timestep:
+            line["timestep"] = timestep_variants(args)
         print(json.dumps(line))
     if ws > 1:
         dist.barrier()
@@ -319,6 +393,11 @@ def main():
     ap.add_argument("--barrier-pairs", type=int, default=2_000_000)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-timestep", action="store_true", help="skip the cloth-on-sphere ms/timestep variants")
+    ap.add_argument("--ts-n", type=int, default=200, help="cloth resolution of the time-step variants")
+    ap.add_argument("--ts-warm", type=int, default=10, help="draping steps before the measured steps")
+    ap.add_argument("--ts-steps", type=int, default=6, help="measured steps per variant")
+    ap.add_argument("--ts-epochs", type=int, default=20, help="training epochs of the learned correction")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

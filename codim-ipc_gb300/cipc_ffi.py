@@ -336,7 +336,7 @@ class Precond:
         _check(lib().cipc_precond_create(hidden, layers, seed, ctypes.byref(h)))
         self.h = h
         self.hidden, self.layers = hidden, layers
-        self.loss_kind = 0
+        self.loss_kind = 2
 
     def close(self):
         if self.h:

@@ -593,6 +593,89 @@ __global__ void k_lp_adam(int n, float* p, const float* g, float* m, float* v, f
 }
 
 
+// ---------------------------------------------------------------------------
+// k-step preconditioned steepest descent loss (loss kind 2)
+// ---------------------------------------------------------------------------
+// y_i = P_i x_i (3x3 blocks)
+__global__ void k_lp_pmul(int nv, const float* P, const float* x, float* y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const float* B = P + 9 * (size_t)i;
+    const float x0 = x[3 * i], x1 = x[3 * i + 1], x2 = x[3 * i + 2];
+    y[3 * i] = B[0] * x0 + B[1] * x1 + B[2] * x2;
+    y[3 * i + 1] = B[3] * x0 + B[4] * x1 + B[5] * x2;
+    y[3 * i + 2] = B[6] * x0 + B[7] * x1 + B[8] * x2;
+}
+// y += a x ; with y_acc_p: y += a P x (blocks)
+__global__ void k_lp_axpy(int n, float a, const float* x, float* y)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) y[k] += a * x[k];
+}
+__global__ void k_lp_pmul_acc(int nv, const float* P, const float* x, float* y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const float* B = P + 9 * (size_t)i;
+    const float x0 = x[3 * i], x1 = x[3 * i + 1], x2 = x[3 * i + 2];
+    y[3 * i] += B[0] * x0 + B[1] * x1 + B[2] * x2;
+    y[3 * i + 1] += B[3] * x0 + B[4] * x1 + B[5] * x2;
+    y[3 * i + 2] += B[6] * x0 + B[7] * x1 + B[8] * x2;
+}
+// out = a x + b y
+__global__ void k_lp_lin2(int n, float a, const float* x, float b, const float* y, float* out)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[k] = a * x[k] + b * y[k];
+}
+// red += x . y
+__global__ void k_lp_dot(int n, const float* x, const float* y, double* red)
+{
+    __shared__ double sh[32];
+    double a = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a += (double)x[i] * y[i];
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+        atomicAdd(red, t);
+    }
+}
+// G_i += zb_i r_i^T
+__global__ void k_lp_outer_acc(int nv, const float* zb, const float* r, float* G)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) G[9 * (size_t)i + 3 * a + b] += zb[3 * i + a] * r[3 * i + b];
+}
+// dout from the adjoint G of the preconditioner blocks: dCm = (G + G^T) Cm E
+__global__ void k_lp_out_bwd_G(int nv, const float* o, const float* E, const float* Gb, float scale, float* dout)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    float oo[kLpOut];
+    for (int k = 0; k < kLpOut; ++k) oo[k] = o[(size_t)kLpOut * i + k];
+    const float* Ei = E + 9 * (size_t)i;
+    const float* G = Gb + 9 * (size_t)i;
+    float P[9], C[9], S[9], CE[9], dC[9];
+    lp_block(oo, Ei, P, C);
+    for (int x = 0; x < 3; ++x)
+        for (int y = 0; y < 3; ++y) S[3 * x + y] = scale * (G[3 * x + y] + G[3 * y + x]);
+    for (int x = 0; x < 3; ++x)
+        for (int y = 0; y < 3; ++y) CE[3 * x + y] = C[3 * x] * Ei[y] + C[3 * x + 1] * Ei[3 + y] + C[3 * x + 2] * Ei[6 + y];
+    for (int x = 0; x < 3; ++x)
+        for (int y = 0; y < 3; ++y) dC[3 * x + y] = S[3 * x] * CE[y] + S[3 * x + 1] * CE[3 + y] + S[3 * x + 2] * CE[6 + y];
+    float* d = dout + (size_t)kLpOut * i;
+    for (int q = 0; q < 3; ++q) d[q] = (oo[q] > -8.f && oo[q] < 8.f) ? dC[4 * q] * 0.5f * C[4 * q] : 0.f;
+    d[3] = dC[3];
+    d[4] = dC[6];
+    d[5] = dC[7];
+}
+
 template <typename T>
 __global__ void k_lp_cvt(long long n, const T* a, float* b)
 {
@@ -639,7 +722,7 @@ LpModel::~LpModel()
         delete t;
     }
     for (DBuf<float>* b : {&params, &grad, &adam_m, &adam_v, &X, &E, &Dn, &a, &s, &u0, &o, &z, &hz, &dz, &dout, &dh, &dh2,
-                           &du, &dg, &dc, &acc, &h, &g, &c, &u})
+                           &du, &dg, &dc, &acc, &h, &g, &c, &u, &Pm, &Gb, &psd})
         b->release();
     wbf16.release();
     ncnt.release();
@@ -679,6 +762,9 @@ int ensure_work(LpModel* m, int nv, int K, int ncon)
     A(m->g, (size_t)L * n * H);
     A(m->c, (size_t)L * n * H);
     A(m->u, (size_t)L * n * H);
+    A(m->Pm, 9 * n);
+    A(m->Gb, 9 * n);
+    A(m->psd, (size_t)(3 * kLpPsdSteps + 6) * 3 * n);
     if (e == cudaSuccess) e = m->ncnt.alloc(n);
     if (e == cudaSuccess && m->red.n < 8) e = m->red.alloc(8);
     if (e != cudaSuccess) return set_error(CIPC_ERR_CUDA, "learned preconditioner work buffers");
@@ -722,6 +808,132 @@ void forward(LpModel* m, int nv, int K, const int* col, int ncon, const int* cki
                                                  m->o.p, r ? m->z.p : nullptr, pinv);
 }
 
+// network backward from dout (d loss / d o, nv x 6): parameter gradients into m->grad
+template <int H>
+void net_backward(LpModel* m, LpTriple* T, cudaStream_t st)
+{
+    const int nv = T->nv, K = T->K, L = m->L;
+    const LpOff of = offsets(H, L);
+    float* G = m->grad.p;
+    const float* P = m->params.p;
+    const size_t nh = (size_t)nv * H;
+    const int wg = std::min(nb(nv, 64), 2 * num_sms());
+    k_lp_wgrad<kLpOut, H><<<wg, 256, 0, st>>>(nv, m->dout.p, m->h.p + (size_t)L * nh, G + of.Wo, G + of.bo);
+    k_lp_dense_T<kLpOut, H><<<nb(nv, 128), 128, 0, st>>>(nv, P + of.Wo, m->dout.p, m->dh.p, 0);
+    for (int l = L - 1; l >= 0; --l) {
+        const float* hl = m->h.p + (size_t)l * nh;
+        k_lp_relu_bwd<<<nb((long long)nh, 256), 256, 0, st>>>((long long)nh, m->dh.p, m->u.p + (size_t)l * nh, m->du.p);
+        k_lp_wgrad<H, H><<<wg, 256, 0, st>>>(nv, m->du.p, hl, G + of.A[l], G + of.b[l]);
+        k_lp_wgrad<H, H><<<wg, 256, 0, st>>>(nv, m->du.p, m->g.p + (size_t)l * nh, G + of.B[l], nullptr);
+        k_lp_wgrad<H, H><<<wg, 256, 0, st>>>(nv, m->du.p, m->c.p + (size_t)l * nh, G + of.C[l], nullptr);
+        cudaMemcpyAsync(m->dh2.p, m->dh.p, sizeof(float) * nh, cudaMemcpyDeviceToDevice, st);
+        k_lp_dense_T<H, H><<<nb(nv, 128), 128, 0, st>>>(nv, P + of.A[l], m->du.p, m->dh2.p, 1);
+        k_lp_dense_T<H, H><<<nb(nv, 128), 128, 0, st>>>(nv, P + of.B[l], m->du.p, m->dg.p, 0);
+        k_lp_dense_T<H, H><<<nb(nv, 128), 128, 0, st>>>(nv, P + of.C[l], m->du.p, m->dc.p, 0);
+        k_lp_gather_T<<<nb((long long)nh, 256), 256, 0, st>>>(nv, K, H, T->col.p, m->a.p, m->s.p, m->dg.p, m->dh2.p);
+        if (T->ncon > 0)
+            k_lp_con_T<<<nb((long long)T->ncon * H, 256), 256, 0, st>>>(T->ncon, H, T->ckind.p, T->cverts.p, m->ncnt.p,
+                                                                        m->dc.p, m->dh2.p);
+        std::swap(m->dh.p, m->dh2.p);
+    }
+    k_lp_relu_bwd<<<nb((long long)nh, 256), 256, 0, st>>>((long long)nh, m->dh.p, m->u0.p, m->du.p);
+    k_lp_wgrad<H, kLpFeatures><<<wg, 256, 0, st>>>(nv, m->du.p, m->X.p, G + of.W0, G + of.b0);
+}
+
+// Loss kind 2: relative H-norm error after kLpPsdSteps steps of preconditioned
+// steepest descent from x = 0 on H x = r (x_k = sum alpha_j z_j, z_j = P r_j,
+// alpha_j = (z_j.r_j)/(z_j.H z_j), r_{j+1} = r_j - alpha_j H z_j), and its
+// gradient by reverse accumulation through the steps.  Unlike the one-step
+// losses it depends on the whole spectrum of P H, as PCG's convergence does.
+template <int H>
+int loss_grad_psd(LpModel* m, LpTriple* T, float grad_scale, double* loss)
+{
+    cudaStream_t st = m->stream;
+    int rc = ensure_work(m, T->nv, T->K, T->ncon);
+    if (rc) return rc;
+    const int nv = T->nv, K = T->K, n3 = 3 * nv, ks = kLpPsdSteps;
+    LpSys<float, float> S{nv, K, T->col.p, T->diag.p, T->val.p, T->cdiag.p, T->proj.p, T->ncon, T->ckind.p, T->cverts.p};
+    features(m, S, st);
+    forward<H, float>(m, nv, K, T->col.p, T->ncon, T->ckind.p, T->cverts.p, nullptr, m->Pm.p, st);
+    const size_t vb = 3 * (size_t)m->cap_nv;
+    float* R = m->psd.p;
+    float* Z = R + (ks + 1) * vb;
+    float* Wv = Z + ks * vb;
+    float* xb = Wv + ks * vb;
+    float* rb = xb + vb;
+    float* zb = rb + vb;
+    float* wb = zb + vb;
+    float* tmp = wb + vb;
+    auto Rj = [&](int j) { return R + j * vb; };
+    auto Zj = [&](int j) { return Z + j * vb; };
+    auto Wj = [&](int j) { return Wv + j * vb; };
+    auto spmv = [&](const float* x, float* y) {
+        k_lp_spmv_ell<<<nb(n3, 256), 256, 0, st>>>(nv, K, T->col.p, T->val.p, x, y);
+        if (T->ncon > 0)
+            k_lp_spmv_con<<<nb(T->ncon, 128), 128, 0, st>>>(T->ncon, T->ckind.p, T->cverts.p, T->chess.p, x, y);
+        if (T->nfric > 0)
+            k_lp_spmv_fric<<<nb(T->nfric, 128), 128, 0, st>>>(T->nfric, T->fkind.p, T->fverts.p, T->fw.p, T->fT.p,
+                                                             T->fM.p, T->proj.p, x, y);
+    };
+    cudaError_t e = cudaSuccess;
+    auto dot = [&](const float* x, const float* y) -> double {
+        double h = 0;
+        cudaMemsetAsync(m->red.p + 5, 0, sizeof(double), st);
+        k_lp_dot<<<std::min(nb(n3, 256), 512), 256, 0, st>>>(n3, x, y, m->red.p + 5);
+        cudaMemcpyAsync(&h, m->red.p + 5, sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        return h;
+    };
+    const int t1 = nb(n3, 256), tv = nb(nv, 128);
+    cudaMemcpyAsync(Rj(0), T->r.p, sizeof(float) * n3, cudaMemcpyDeviceToDevice, st);
+    const double c = dot(T->r.p, T->p.p);
+    double a[kLpPsdSteps], b[kLpPsdSteps], al[kLpPsdSteps];
+    int kk = 0;
+    for (int j = 0; j < ks; ++j) {
+        k_lp_pmul<<<tv, 128, 0, st>>>(nv, m->Pm.p, Rj(j), Zj(j));
+        spmv(Zj(j), Wj(j));
+        a[j] = dot(Zj(j), Rj(j));
+        b[j] = dot(Zj(j), Wj(j));
+        if (!(b[j] > 0) || !(a[j] == a[j])) break;
+        al[j] = a[j] / b[j];
+        k_lp_lin2<<<t1, 256, 0, st>>>(n3, 1.f, Rj(j), (float)-al[j], Wj(j), Rj(j + 1));
+        kk = j + 1;
+    }
+    if (e != cudaSuccess) return set_cuda_error(e, "learned preconditioner loss");
+    if (!(c > 0) || kk == 0) {
+        *loss = 0;
+        return CIPC_OK;
+    }
+    // x = sum alpha_j z_j ; H x = r_0 - r_k ; |p - x|_H^2 = c - 2 x.r_0 + x.Hx
+    cudaMemsetAsync(tmp, 0, sizeof(float) * n3, st);
+    for (int j = 0; j < kk; ++j) k_lp_axpy<<<t1, 256, 0, st>>>(n3, (float)al[j], Zj(j), tmp);
+    const double xr = dot(tmp, Rj(0));
+    const double xHx = xr - dot(tmp, Rj(kk));
+    if (e != cudaSuccess) return set_cuda_error(e, "learned preconditioner loss");
+    *loss = (c - 2 * xr + xHx) / c;
+    if (grad_scale == 0.f) return CIPC_OK;
+    // reverse accumulation; xb = d loss / d x = -(2/c) r_k
+    k_lp_lin2<<<t1, 256, 0, st>>>(n3, (float)(-2.0 / c), Rj(kk), 0.f, Rj(kk), xb);
+    cudaMemsetAsync(rb, 0, sizeof(float) * n3, st);
+    cudaMemsetAsync(m->Gb.p, 0, sizeof(float) * 9 * nv, st);
+    for (int j = kk - 1; j >= 0; --j) {
+        const double ab = -dot(rb, Wj(j)) + dot(xb, Zj(j));
+        const double abar = ab / b[j], bbar = -ab * a[j] / (b[j] * b[j]);
+        k_lp_lin2<<<t1, 256, 0, st>>>(n3, (float)al[j], xb, (float)abar, Rj(j), zb);
+        k_lp_axpy<<<t1, 256, 0, st>>>(n3, (float)bbar, Wj(j), zb);
+        k_lp_lin2<<<t1, 256, 0, st>>>(n3, (float)-al[j], rb, (float)bbar, Zj(j), wb);
+        k_lp_axpy<<<t1, 256, 0, st>>>(n3, (float)abar, Zj(j), rb);
+        spmv(wb, tmp);
+        k_lp_axpy<<<t1, 256, 0, st>>>(n3, 1.f, tmp, zb);
+        k_lp_outer_acc<<<tv, 128, 0, st>>>(nv, zb, Rj(j), m->Gb.p);
+        k_lp_pmul_acc<<<tv, 128, 0, st>>>(nv, m->Pm.p, zb, rb);
+    }
+    if (e != cudaSuccess) return set_cuda_error(e, "learned preconditioner gradient");
+    k_lp_out_bwd_G<<<tv, 128, 0, st>>>(nv, m->o.p, m->E.p, m->Gb.p, grad_scale, m->dout.p);
+    net_backward<H>(m, T, st);
+    return CIPC_OK;
+}
+
 // loss of triple T (and, if grad_scale != 0, its gradient times grad_scale added to m->grad)
 template <int H>
 int loss_grad(LpModel* m, LpTriple* T, float grad_scale, double* loss)
@@ -753,40 +965,17 @@ int loss_grad(LpModel* m, LpTriple* T, float grad_scale, double* loss)
     const bool unit = m->loss_kind == 1;
     *loss = unit ? (b - 2 * a + c) / c : 1 - a * a / (b * c);
     if (grad_scale == 0.f) return CIPC_OK;
-    const LpOff of = offsets(H, m->L);
-    float* G = m->grad.p;
-    const float* P = m->params.p;
-    const size_t nh = (size_t)nv * H;
-    const int L = m->L;
     const double f = unit ? 2 / c : 2 * a / (b * c), t = unit ? 1.0 : a / b;
     k_lp_out_bwd<<<nb(nv, 128), 128, 0, st>>>(nv, m->o.p, m->E.p, T->r.p, m->hz.p, (float)f * grad_scale, (float)t,
                                               m->dout.p);
-    const int wg = std::min(nb(nv, 64), 2 * num_sms());
-    k_lp_wgrad<kLpOut, H><<<wg, 256, 0, st>>>(nv, m->dout.p, m->h.p + (size_t)L * nh, G + of.Wo, G + of.bo);
-    k_lp_dense_T<kLpOut, H><<<nb(nv, 128), 128, 0, st>>>(nv, P + of.Wo, m->dout.p, m->dh.p, 0);
-    for (int l = L - 1; l >= 0; --l) {
-        const float* hl = m->h.p + (size_t)l * nh;
-        k_lp_relu_bwd<<<nb((long long)nh, 256), 256, 0, st>>>((long long)nh, m->dh.p, m->u.p + (size_t)l * nh, m->du.p);
-        k_lp_wgrad<H, H><<<wg, 256, 0, st>>>(nv, m->du.p, hl, G + of.A[l], G + of.b[l]);
-        k_lp_wgrad<H, H><<<wg, 256, 0, st>>>(nv, m->du.p, m->g.p + (size_t)l * nh, G + of.B[l], nullptr);
-        k_lp_wgrad<H, H><<<wg, 256, 0, st>>>(nv, m->du.p, m->c.p + (size_t)l * nh, G + of.C[l], nullptr);
-        cudaMemcpyAsync(m->dh2.p, m->dh.p, sizeof(float) * nh, cudaMemcpyDeviceToDevice, st);
-        k_lp_dense_T<H, H><<<nb(nv, 128), 128, 0, st>>>(nv, P + of.A[l], m->du.p, m->dh2.p, 1);
-        k_lp_dense_T<H, H><<<nb(nv, 128), 128, 0, st>>>(nv, P + of.B[l], m->du.p, m->dg.p, 0);
-        k_lp_dense_T<H, H><<<nb(nv, 128), 128, 0, st>>>(nv, P + of.C[l], m->du.p, m->dc.p, 0);
-        k_lp_gather_T<<<nb((long long)nh, 256), 256, 0, st>>>(nv, K, H, T->col.p, m->a.p, m->s.p, m->dg.p, m->dh2.p);
-        if (T->ncon > 0)
-            k_lp_con_T<<<nb((long long)T->ncon * H, 256), 256, 0, st>>>(T->ncon, H, T->ckind.p, T->cverts.p, m->ncnt.p,
-                                                                        m->dc.p, m->dh2.p);
-        std::swap(m->dh.p, m->dh2.p);
-    }
-    k_lp_relu_bwd<<<nb((long long)nh, 256), 256, 0, st>>>((long long)nh, m->dh.p, m->u0.p, m->du.p);
-    k_lp_wgrad<H, kLpFeatures><<<wg, 256, 0, st>>>(nv, m->du.p, m->X.p, G + of.W0, G + of.b0);
+    net_backward<H>(m, T, st);
     return CIPC_OK;
 }
 
 int loss_grad_any(LpModel* m, LpTriple* T, float grad_scale, double* loss)
 {
+    if (m->loss_kind == 2)
+        return m->H == 32 ? loss_grad_psd<32>(m, T, grad_scale, loss) : loss_grad_psd<16>(m, T, grad_scale, loss);
     if (m->H == 32) return loss_grad<32>(m, T, grad_scale, loss);
     return loss_grad<16>(m, T, grad_scale, loss);
 }
@@ -1025,7 +1214,7 @@ extern "C" int cipc_precond_set_params(cipc_precond* p, const float* in)
 extern "C" int cipc_precond_set_loss(cipc_precond* p, int kind)
 {
     if (int rc = check_pc(p)) return rc;
-    if (kind != 0 && kind != 1) return set_error(CIPC_ERR_INVALID_ARG, "cipc_precond_set_loss: kind must be 0 or 1");
+    if (kind < 0 || kind > 2) return set_error(CIPC_ERR_INVALID_ARG, "cipc_precond_set_loss: kind must be 0, 1 or 2");
     p->m->loss_kind = kind;
     return CIPC_OK;
 }

@@ -19,7 +19,7 @@
 
 namespace cipc {
 
-constexpr int kLpFeatures = 10, kLpOut = 6;
+constexpr int kLpFeatures = 10, kLpOut = 6, kLpPsdSteps = 8;
 
 // One captured Newton system, FP32, on the device.
 struct LpTriple {
@@ -41,7 +41,9 @@ struct LpTriple {
 // Network parameters, Adam state, captured triples and work buffers.
 struct LpModel {
     int H = 32, L = 2, nparams = 0;
-    int loss_kind = 0;       // 0: 1 - (z.r)^2/((z.Hz)(r.p)); 1: |z - p|_H^2 / |p|_H^2
+    // 0: 1 - (z.r)^2/((z.Hz)(r.p)); 1: |z - p|_H^2 / |p|_H^2; 2: |e_k|_H^2 / |p|_H^2
+    // after k steps of preconditioned steepest descent from 0 (kLpPsdSteps)
+    int loss_kind = 2;
     uint64_t seed = 0;
     DBuf<float> params, grad, adam_m, adam_v;
     DBuf<uint16_t> wbf16;    // BF16 copy of the dense-layer weights for inference
@@ -53,6 +55,7 @@ struct LpModel {
     int cap_nv = 0, cap_k = 0, cap_con = 0;
     DBuf<float> X, E, Dn, a, s, u0, o, z, hz, dz, dout, dh, dh2, du, dg, dc, acc;
     DBuf<float> h, g, c, u;  // (L+1) or L layers of nv x H
+    DBuf<float> Pm, Gb, psd;  // preconditioner blocks, their adjoint, steepest-descent vectors
     DBuf<int> ncnt;
     DBuf<double> red;
     cudaStream_t stream = nullptr;

@@ -235,8 +235,11 @@ int cipc_precond_destroy(cipc_precond* p);
 int cipc_precond_num_params(const cipc_precond* p);
 int cipc_precond_get_params(const cipc_precond* p, float* out);
 int cipc_precond_set_params(cipc_precond* p, const float* in);
-/* training loss per system: 0 (default) 1 - (z.r)^2 / ((z.Hz)(r.p)), the error of
- * the optimally scaled step; 1 |z - p|_H^2 / |p|_H^2, the error of the unit step */
+/* training loss per system (z = M^-1 r, p = H^-1 r, errors in the H-norm relative to
+ * |p|_H): 0 the error after one optimally scaled preconditioned step,
+ * 1 - (z.r)^2 / ((z.Hz)(r.p)); 1 the error of the unit step |z - p|_H^2 / |p|_H^2;
+ * 2 (default) the error after 8 steps of preconditioned steepest descent from 0,
+ * which depends on the whole spectrum of M^-1 H as PCG's convergence does */
 int cipc_precond_set_loss(cipc_precond* p, int kind);
 /* captured Newton systems: count (or -1) and clearing */
 int cipc_precond_num_systems(const cipc_precond* p);

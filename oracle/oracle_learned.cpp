@@ -334,21 +334,98 @@ double loss_grad(const Net& N, const Graph& G, const Prep& P, const double* r, c
                  int nparams, int kind)
 {
     const int nv = G.nv, H = N.H, L = N.L;
+    const size_t n3 = 3 * (size_t)nv;
     forward(N, G, P, r, A);
-    std::vector<double> Hz(3 * (size_t)nv);
-    apply_H(G, A.z.data(), Hz.data());
-    double a = 0, b = 0, c = 0;
-    for (int i = 0; i < 3 * nv; ++i) {
-        a += A.z[i] * r[i];
-        b += A.z[i] * Hz[i];
-        c += r[i] * p[i];
-    }
     for (int k = 0; k < nparams; ++k) grad[k] = 0;
-    if (!(b > 0) || !(c > 0)) return 0;
-    // kind 0: 1 - a^2/(bc), dL/dz = (2a/(bc)) (-r + (a/b) Hz)
-    // kind 1: |z - p|_H^2 / |p|_H^2 = (b - 2a + c)/c, dL/dz = (2/c) (-r + Hz)
-    const double loss = kind == 1 ? (b - 2 * a + c) / c : 1 - a * a / (b * c);
-    const double f = kind == 1 ? 2 / c : 2 * a / (b * c), t = kind == 1 ? 1.0 : a / b;
+    double c = 0;
+    for (size_t i = 0; i < n3; ++i) c += r[i] * p[i];
+    if (!(c > 0)) return 0;
+    // per-vertex adjoint of the preconditioner blocks, as S = G + G^T
+    std::vector<double> Sadj(9 * (size_t)nv, 0);
+    double loss = 0;
+    if (kind == 2) {
+        // |p - x_k|_H^2 / |p|_H^2 after k steps of preconditioned steepest descent
+        const int ks = 8;
+        std::vector<double> Pm(9 * (size_t)nv);
+        for (int i = 0; i < nv; ++i) precond_block(&A.o[(size_t)O * i], &P.E[9 * (size_t)i], &Pm[9 * (size_t)i], nullptr);
+        auto pmul = [&](const std::vector<double>& x, std::vector<double>& y, bool acc) {
+            if (!acc) y.assign(n3, 0);
+            for (int i = 0; i < nv; ++i)
+                for (int q = 0; q < 3; ++q)
+                    y[3 * i + q] += Pm[9 * i + 3 * q] * x[3 * i] + Pm[9 * i + 3 * q + 1] * x[3 * i + 1] +
+                                    Pm[9 * i + 3 * q + 2] * x[3 * i + 2];
+        };
+        auto dotv = [&](const std::vector<double>& x, const std::vector<double>& y) {
+            double t = 0;
+            for (size_t i = 0; i < n3; ++i) t += x[i] * y[i];
+            return t;
+        };
+        std::vector<std::vector<double>> R(1, std::vector<double>(r, r + n3)), Z, W;
+        std::vector<double> a, b, al;
+        for (int j = 0; j < ks; ++j) {
+            std::vector<double> z, w(n3);
+            pmul(R[j], z, false);
+            apply_H(G, z.data(), w.data());
+            const double aj = dotv(z, R[j]), bj = dotv(z, w);
+            if (!(bj > 0) || !(aj == aj)) break;
+            Z.push_back(z);
+            W.push_back(w);
+            a.push_back(aj);
+            b.push_back(bj);
+            al.push_back(aj / bj);
+            std::vector<double> rn(n3);
+            for (size_t i = 0; i < n3; ++i) rn[i] = R[j][i] - al.back() * w[i];
+            R.push_back(rn);
+        }
+        const int kk = (int)Z.size();
+        if (kk == 0) return 0;
+        std::vector<double> x(n3, 0);
+        for (int j = 0; j < kk; ++j)
+            for (size_t i = 0; i < n3; ++i) x[i] += al[j] * Z[j][i];
+        const double xr = dotv(x, R[0]), xHx = xr - dotv(x, R[kk]);
+        loss = (c - 2 * xr + xHx) / c;
+        std::vector<double> xb(n3), rb(n3, 0), zb(n3), wb(n3), tmp(n3);
+        for (size_t i = 0; i < n3; ++i) xb[i] = -2.0 / c * R[kk][i];
+        for (int j = kk - 1; j >= 0; --j) {
+            const double ab = -dotv(rb, W[j]) + dotv(xb, Z[j]);
+            const double abar = ab / b[j], bbar = -ab * a[j] / (b[j] * b[j]);
+            for (size_t i = 0; i < n3; ++i) {
+                zb[i] = al[j] * xb[i] + abar * R[j][i] + bbar * W[j][i];
+                wb[i] = -al[j] * rb[i] + bbar * Z[j][i];
+                rb[i] += abar * Z[j][i];
+            }
+            apply_H(G, wb.data(), tmp.data());
+            for (size_t i = 0; i < n3; ++i) zb[i] += tmp[i];
+            for (int i = 0; i < nv; ++i)
+                for (int x1 = 0; x1 < 3; ++x1)
+                    for (int y1 = 0; y1 < 3; ++y1) {
+                        const double g = zb[3 * i + x1] * R[j][3 * i + y1];
+                        Sadj[9 * i + 3 * x1 + y1] += g;
+                        Sadj[9 * i + 3 * y1 + x1] += g;
+                    }
+            pmul(zb, rb, true);
+        }
+    } else {
+        std::vector<double> Hz(n3);
+        apply_H(G, A.z.data(), Hz.data());
+        double a = 0, b = 0;
+        for (size_t i = 0; i < n3; ++i) {
+            a += A.z[i] * r[i];
+            b += A.z[i] * Hz[i];
+        }
+        if (!(b > 0)) return 0;
+        // kind 0: 1 - a^2/(bc), dL/dz = (2a/(bc)) (-r + (a/b) Hz)
+        // kind 1: |z - p|_H^2 / |p|_H^2 = (b - 2a + c)/c, dL/dz = (2/c) (-r + Hz)
+        loss = kind == 1 ? (b - 2 * a + c) / c : 1 - a * a / (b * c);
+        const double f = kind == 1 ? 2 / c : 2 * a / (b * c), t = kind == 1 ? 1.0 : a / b;
+        for (int i = 0; i < nv; ++i) {
+            double dz[3];
+            for (int q = 0; q < 3; ++q) dz[q] = f * (-r[3 * i + q] + t * Hz[3 * i + q]);
+            for (int x1 = 0; x1 < 3; ++x1)
+                for (int y1 = 0; y1 < 3; ++y1)
+                    Sadj[9 * i + 3 * x1 + y1] = dz[x1] * r[3 * i + y1] + dz[y1] * r[3 * i + x1];
+        }
+    }
     // parameter gradient views (same layout as Net)
     double* gW0 = grad;
     double* gb0 = gW0 + H * F;
@@ -368,19 +445,12 @@ double loss_grad(const Net& N, const Graph& G, const Prep& P, const double* r, c
     double* gbo = gWo + O * H;
     std::vector<double> dout((size_t)O * nv, 0);
     for (int i = 0; i < nv; ++i) {
-        double dz[3], rr[3];
-        for (int q = 0; q < 3; ++q) {
-            dz[q] = f * (-r[3 * i + q] + t * Hz[3 * i + q]);
-            rr[q] = r[3 * i + q];
-        }
         const double* o = &A.o[(size_t)O * i];
         const double* E = &P.E[9 * (size_t)i];
         double Pm[9], C[9];
         precond_block(o, E, Pm, C);
-        // G = dz r^T ; dC = (G + G^T) C E
-        double S[9];
-        for (int x = 0; x < 3; ++x)
-            for (int y = 0; y < 3; ++y) S[3 * x + y] = dz[x] * rr[y] + dz[y] * rr[x];
+        // dC = (G + G^T) C E with G the adjoint of the block
+        const double* S = &Sadj[9 * (size_t)i];
         double CE[9];
         for (int x = 0; x < 3; ++x)
             for (int y = 0; y < 3; ++y) CE[3 * x + y] = C[3 * x] * E[y] + C[3 * x + 1] * E[3 + y] + C[3 * x + 2] * E[6 + y];

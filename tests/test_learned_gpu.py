@@ -9,6 +9,12 @@
   products are accumulated with atomics, so the Krylov sequences drift apart)
   and the same step results (within the Newton stopping bar).
 * Training on systems the plain solver produced lowers the training loss.
+* What the trained network gains over block Jacobi on held-out steps of a cloth
+  draped on a turning sphere (mu 0.4): PCG iterations of both from identical
+  states; the learned one needs no fallback and stays intersection free.  The gain is
+  reported, and must not be a collapse (< 0.5); on this scene block Jacobi is
+  close to the best block-diagonal preconditioner (the obstacle is fixed, so
+  contact blocks are vertex-local), and the measured gain is about 0.9-1.0.
 """
 import numpy as np
 import pytest
@@ -51,7 +57,7 @@ def captured(cuda):
     return dict(pc=pc, sim=s, prm=prm, X=X, T=T, dbc=dbc, dhat2=dhat2)
 
 
-@pytest.mark.parametrize("kind", [0, 1])
+@pytest.mark.parametrize("kind", [0, 1, 2])
 def test_gradient_matches_oracle(captured, orc, kind):
     pc = captured["pc"]
     pc.set_loss(kind)
@@ -80,7 +86,7 @@ def test_gradient_matches_oracle(captured, orc, kind):
         assert checked >= 1
     finally:
         pc.set_params(p0)
-        pc.set_loss(0)
+        pc.set_loss(2)
 
 
 def test_untrained_network_is_block_jacobi(cuda):
@@ -113,3 +119,54 @@ def test_training_lowers_loss(captured):
     before, after = pc.train(epochs=30, batch=4, lr=1e-3, seed=0)
     assert 0 < before < 1
     assert after < before, (before, after)
+
+
+def test_trained_network_against_block_jacobi(cuda, record_property):
+    X, T, dbc, c = W.cloth_on_sphere(n=30, subdiv=3)
+    dt = 0.02
+
+    def target(k):
+        return W.rotate_y(X[dbc], c, 2.0 * dt * (k + 1))
+
+    def make():
+        s = F.Sim(X, T, 200.0, 1e5, 0.3, 1e-3)
+        _, dhat2 = s.init_oipc(1e-3)
+        return s, dhat2
+
+    s, dhat2 = make()
+    prm = F.make_params(dt, dhat2, 5e-4, mu=0.4, newton_tol=1e-3, precision=F.MIXED, pcg_tol=1e-4)
+    prl = F.make_params(dt, dhat2, 5e-4, mu=0.4, newton_tol=1e-3, precision=F.MIXED, pcg_tol=1e-4, preconditioner=1)
+    ok = (F.CIPC_ERR_NOT_CONVERGED,)
+    pc = F.Precond(hidden=16, layers=2, seed=0)
+    for k in range(10):
+        if k == 4:
+            F.sim_capture_systems(s, pc, 256)
+        s.set_dbc(dbc, target(k))
+        s.step(prm, allow=ok)
+    F.sim_capture_systems(s, None, 0)
+    before, after = pc.train(epochs=15, batch=8, lr=1e-3, seed=0)
+    a, _ = make()
+    b, _ = make()
+    F.sim_set_precond(b, pc)
+    x, v = s.state()
+    kap = s.kappa()
+    it_bj = it_l = 0
+    for k in range(10, 14):
+        for sim in (a, b):
+            sim.set_state(x, v)
+            sim.set_kappa(*kap)
+            sim.set_dbc(dbc, target(k))
+        sa = a.step(prm, allow=ok)
+        sb = b.step(prl, allow=ok)
+        assert sb.precond_fallbacks == 0 and sb.learned_solves > 0
+        assert sb.min_dist2 > 0 and sa.min_dist2 > 0
+        it_bj += sa.pcg_iters
+        it_l += sb.pcg_iters
+        x, v = a.state()
+        kap = a.kappa()
+    gain = it_bj / it_l
+    record_property("learned_gain_pcg_iters", gain)
+    record_property("learned_loss", (before, after))
+    print("trained network vs block Jacobi: PCG iterations %d vs %d (gain %.3f), loss %.4f -> %.4f"
+          % (it_l, it_bj, gain, before, after))
+    assert gain > 0.5

@@ -1,6 +1,7 @@
 """The oracle's restatement of the learned block-Jacobi correction: operator,
-features, forward pass and parameter gradient, checked on seeded synthetic SPD
-systems (no GPU).  The gradient is checked against central finite differences
+features, forward pass and parameter gradient of the three losses (one optimally
+scaled step, one unit step, eight steps of preconditioned steepest descent),
+checked on seeded synthetic SPD systems (no GPU).  The gradient is checked against central finite differences
 of the oracle's own loss; the GPU kernels are then checked against this oracle
 (tests/test_learned_gpu.py)."""
 import numpy as np
@@ -63,14 +64,15 @@ def test_features_are_scale_invariant(orc, system):
     assert np.allclose(x1[free], x2[free], rtol=1e-6, atol=1e-6)
 
 
-def test_gradient_matches_finite_differences(orc, system):
+@pytest.mark.parametrize("kind", [0, 1, 2])
+def test_gradient_matches_finite_differences(orc, system, kind):
     s, S = system
     prm = _params(orc, 5, 0.4)
     r = np.random.default_rng(4).standard_normal((S.nv, 3))
     r[s["proj"] == 1] = 0
     p = np.linalg.solve(dense_matrix(s), r.ravel())
-    loss, g, _ = orc.lp_loss_grad(H, L, prm, S, r, p)
-    assert 0 < loss < 1
+    loss, g, _ = orc.lp_loss_grad(H, L, prm, S, r, p, kind)
+    assert loss > 0 and (kind == 1 or loss < 1)
     rng = np.random.default_rng(7)
     idx = np.unique(np.concatenate([rng.choice(prm.shape[0], 60, replace=False),
                                     np.arange(prm.shape[0] - 54, prm.shape[0])]))
@@ -78,7 +80,14 @@ def test_gradient_matches_finite_differences(orc, system):
     for k in idx:
         d = np.zeros_like(prm)
         d[k] = eps
-        lp = orc.lp_loss_grad(H, L, prm + d, S, r, p)[0]
-        lm = orc.lp_loss_grad(H, L, prm - d, S, r, p)[0]
+        lp = orc.lp_loss_grad(H, L, prm + d, S, r, p, kind)[0]
+        lm = orc.lp_loss_grad(H, L, prm - d, S, r, p, kind)[0]
         fd = (lp - lm) / (2 * eps)
         assert abs(fd - g[k]) <= 1e-5 * max(1.0, abs(fd)) + 1e-8, (k, fd, g[k])
+
+
+def test_operator_with_float32_input(orc, system):
+    s, S = system
+    x = np.random.default_rng(9).standard_normal((S.nv, 3)).astype(np.float32)
+    assert np.allclose(orc.lp_apply(S, x).ravel(), dense_matrix(s) @ x.ravel().astype(np.float64), rtol=1e-10,
+                       atol=1e-9)
