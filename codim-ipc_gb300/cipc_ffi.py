@@ -317,6 +317,7 @@ _SIGS.update({
     "cipc_precond_train": (_c_int, [_vp, _c_int, _c_int, _c_dbl, _c_u64, _vp, _vp]),
     "cipc_precond_loss_grad": (_c_int, [_vp, _c_int, _vp, _vp]),
     "cipc_precond_system_sizes": (_c_int, [_vp, _c_int, _vp]),
+    "cipc_precond_infer": (_c_int, [_vp, _c_int, _c_int, _vp, _vp]),
     "cipc_precond_system_export": (_c_int, [_vp, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cipc_sim_capture_systems": (_c_int, [_vp, _vp, _c_int]),
     "cipc_sim_set_precond": (_c_int, [_vp, _vp]),
@@ -383,6 +384,14 @@ class Precond:
         g = np.zeros(self.num_params(), np.float32)
         _check(lib().cipc_precond_loss_grad(self.h, system, ctypes.byref(loss), g.ctypes.data))
         return loss.value, g
+
+    def infer(self, system, bf16=True):
+        sz = np.zeros(4, np.int32)
+        _check(lib().cipc_precond_system_sizes(self.h, system, sz.ctypes.data))
+        o = np.zeros((int(sz[0]), 6), np.float32)
+        P = np.zeros((int(sz[0]), 3, 3), np.float32)
+        _check(lib().cipc_precond_infer(self.h, system, 1 if bf16 else 0, o.ctypes.data, P.ctypes.data))
+        return o, P
 
     def export_system(self, system):
         sz = np.zeros(4, np.int32)

@@ -594,6 +594,89 @@ __global__ void k_lp_adam(int n, float* p, const float* g, float* m, float* v, f
 
 
 // ---------------------------------------------------------------------------
+// inference: message-passing layers on the BF16 tensor cores (FP32 accumulate)
+// ---------------------------------------------------------------------------
+// Wcat_l (H x 3H, bf16, row-major) = [A_l | B_l | C_l] for every layer
+__global__ void k_lp_wcat_bf16(int H, int L, const float* params, int off0, int stride, __nv_bfloat16* out)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= L * 3 * H * H) return;
+    const int l = k / (3 * H * H), e = k - l * 3 * H * H;
+    const int r = e / (3 * H), q = e - r * 3 * H;
+    const int part = q / H, qq = q - part * H;
+    out[k] = __float2bfloat16(params[off0 + l * stride + part * H * H + r * H + qq]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
+{
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// One warp per 16 vertices: u = [h | g | c] Wcat^T + b with mma.m16n8k16 (bf16 in,
+// f32 accumulate); h_out = relu(u) + h.  c = acc / max(1, #contacts).
+template <int H>
+__global__ void __launch_bounds__(128) k_lp_layer_bf16(int nv, const float* h, const float* g, const float* acc,
+                                                       const int* ncnt, const __nv_bfloat16* Wcat, const float* bias,
+                                                       float* hout)
+{
+    constexpr int K3 = 3 * H, KT = K3 / 16, NT = H / 8;
+    __shared__ __align__(16) __nv_bfloat16 sw[H * K3];
+    __shared__ float sb[H];
+    for (int k = threadIdx.x; k < H * K3; k += blockDim.x) sw[k] = Wcat[k];
+    for (int k = threadIdx.x; k < H; k += blockDim.x) sb[k] = bias[k];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gq = lane >> 2, tq = lane & 3;
+    const int v0 = (blockIdx.x * (blockDim.x >> 5) + warp) * 16;
+    if (v0 >= nv) return;
+    const int ra = v0 + gq, rb = v0 + gq + 8;
+    const float ia = ra < nv ? 1.f / fmaxf(1.f, (float)ncnt[ra]) : 0.f;
+    const float ib = rb < nv ? 1.f / fmaxf(1.f, (float)ncnt[rb]) : 0.f;
+    // input element (row, column q of [h | g | c])
+    auto in = [&](int row, float inv, int q) -> float {
+        if (row >= nv) return 0.f;
+        if (q < H) return h[(size_t)H * row + q];
+        if (q < 2 * H) return g[(size_t)H * row + q - H];
+        return acc[(size_t)H * row + q - 2 * H] * inv;
+    };
+    float d[NT][4];
+#pragma unroll
+    for (int n = 0; n < NT; ++n) d[n][0] = d[n][1] = d[n][2] = d[n][3] = 0.f;
+#pragma unroll
+    for (int kt = 0; kt < KT; ++kt) {
+        const int c0 = 16 * kt + 2 * tq, c1 = c0 + 8;
+        const uint32_t a0 = pack_bf16(in(ra, ia, c0), in(ra, ia, c0 + 1));
+        const uint32_t a1 = pack_bf16(in(rb, ib, c0), in(rb, ib, c0 + 1));
+        const uint32_t a2 = pack_bf16(in(ra, ia, c1), in(ra, ia, c1 + 1));
+        const uint32_t a3 = pack_bf16(in(rb, ib, c1), in(rb, ib, c1 + 1));
+#pragma unroll
+        for (int n = 0; n < NT; ++n) {
+            const __nv_bfloat16* wr = sw + (size_t)(8 * n + gq) * K3;
+            const uint32_t b0 = *reinterpret_cast<const uint32_t*>(wr + c0);
+            const uint32_t b1 = *reinterpret_cast<const uint32_t*>(wr + c1);
+            asm volatile(
+                "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                "{%0,%1,%2,%3};\n"
+                : "+f"(d[n][0]), "+f"(d[n][1]), "+f"(d[n][2]), "+f"(d[n][3])
+                : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+        }
+    }
+#pragma unroll
+    for (int n = 0; n < NT; ++n) {
+        const int col = 8 * n + 2 * tq;
+        if (ra < nv) {
+            hout[(size_t)H * ra + col] = fmaxf(d[n][0] + sb[col], 0.f) + h[(size_t)H * ra + col];
+            hout[(size_t)H * ra + col + 1] = fmaxf(d[n][1] + sb[col + 1], 0.f) + h[(size_t)H * ra + col + 1];
+        }
+        if (rb < nv) {
+            hout[(size_t)H * rb + col] = fmaxf(d[n][2] + sb[col], 0.f) + h[(size_t)H * rb + col];
+            hout[(size_t)H * rb + col + 1] = fmaxf(d[n][3] + sb[col + 1], 0.f) + h[(size_t)H * rb + col + 1];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // k-step preconditioned steepest descent loss (loss kind 2)
 // ---------------------------------------------------------------------------
 // y_i = P_i x_i (3x3 blocks)
@@ -806,6 +889,38 @@ void forward(LpModel* m, int nv, int K, const int* col, int ncon, const int* cki
     }
     k_lp_out<H, PT><<<nb(nv, 128), 128, 0, st>>>(nv, m->h.p + (size_t)m->L * nh, P + of.Wo, P + of.bo, m->E.p, r,
                                                  m->o.p, r ? m->z.p : nullptr, pinv);
+}
+
+// inference forward with the message-passing layers on the BF16 tensor cores
+template <int H, typename PT>
+int forward_bf16(LpModel* m, int nv, int K, const int* col, int ncon, const int* ckind, const int4* cverts, PT* pinv,
+                 cudaStream_t st)
+{
+    const LpOff of = offsets(H, m->L);
+    const float* P = m->params.p;
+    const size_t nh = (size_t)nv * H;
+    if (!m->wbf16_valid) {
+        const int n = m->L * 3 * H * H;
+        const int stride = m->L > 1 ? of.A[1] - of.A[0] : 3 * H * H + H;
+        k_lp_wcat_bf16<<<nb(n, 256), 256, 0, st>>>(H, m->L, P, of.A[0], stride,
+                                                    reinterpret_cast<__nv_bfloat16*>(m->wbf16.p));
+        m->wbf16_valid = true;
+    }
+    k_lp_in<H><<<nb(nv, 128), 128, (H * kLpFeatures + H) * sizeof(float), st>>>(nv, m->X.p, P + of.W0, P + of.b0,
+                                                                                m->u0.p, m->h.p);
+    for (int l = 0; l < m->L; ++l) {
+        const float* hl = m->h.p + (size_t)l * nh;
+        float* gl = m->g.p + (size_t)l * nh;
+        k_lp_gather<<<nb((long long)nh, 256), 256, 0, st>>>(nv, K, H, col, m->a.p, m->s.p, hl, gl);
+        cudaMemsetAsync(m->acc.p, 0, sizeof(float) * nh, st);
+        if (ncon > 0) k_lp_con_acc<<<nb((long long)ncon * H, 256), 256, 0, st>>>(ncon, H, ckind, cverts, hl, m->acc.p);
+        k_lp_layer_bf16<H><<<nb(nv, 64), 128, 0, st>>>(
+            nv, hl, gl, m->acc.p, m->ncnt.p, reinterpret_cast<const __nv_bfloat16*>(m->wbf16.p) + (size_t)l * 3 * H * H,
+            P + of.b[l], m->h.p + (size_t)(l + 1) * nh);
+    }
+    k_lp_out<H, PT><<<nb(nv, 128), 128, 0, st>>>(nv, m->h.p + (size_t)m->L * nh, P + of.Wo, P + of.bo, m->E.p,
+                                                 nullptr, m->o.p, nullptr, pinv);
+    return CIPC_OK;
 }
 
 // network backward from dout (d loss / d o, nv x 6): parameter gradients into m->grad
@@ -1057,11 +1172,11 @@ int lp_precond(Sim* s, LpModel* m)
     }
     const int nv = s->nv, K = s->ell_k;
     if (m->H == 32) {
-        if (f32) forward<32, float>(m, nv, K, s->col.p, ncon, s->ckind.p, s->cverts.p, nullptr, (float*)s->pinv.p, st);
-        else forward<32, double>(m, nv, K, s->col.p, ncon, s->ckind.p, s->cverts.p, nullptr, (double*)s->pinv.p, st);
+        if (f32) forward_bf16<32, float>(m, nv, K, s->col.p, ncon, s->ckind.p, s->cverts.p, (float*)s->pinv.p, st);
+        else forward_bf16<32, double>(m, nv, K, s->col.p, ncon, s->ckind.p, s->cverts.p, (double*)s->pinv.p, st);
     } else {
-        if (f32) forward<16, float>(m, nv, K, s->col.p, ncon, s->ckind.p, s->cverts.p, nullptr, (float*)s->pinv.p, st);
-        else forward<16, double>(m, nv, K, s->col.p, ncon, s->ckind.p, s->cverts.p, nullptr, (double*)s->pinv.p, st);
+        if (f32) forward_bf16<16, float>(m, nv, K, s->col.p, ncon, s->ckind.p, s->cverts.p, (float*)s->pinv.p, st);
+        else forward_bf16<16, double>(m, nv, K, s->col.p, ncon, s->ckind.p, s->cverts.p, (double*)s->pinv.p, st);
     }
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CIPC_OK : set_cuda_error(e, "learned preconditioner");
@@ -1254,6 +1369,34 @@ extern "C" int cipc_precond_loss_grad(cipc_precond* p, int system, double* loss,
         if (e != cudaSuccess) return set_cuda_error(e, "cipc_precond_loss_grad");
     }
     return CIPC_OK;
+}
+
+extern "C" int cipc_precond_infer(cipc_precond* p, int system, int bf16, float* out6, float* blocks9)
+{
+    if (int rc = check_pc(p)) return rc;
+    LpModel* m = p->m;
+    if (system < 0 || system >= (int)m->data.size())
+        return set_error(CIPC_ERR_INVALID_ARG, "cipc_precond_infer: bad system index");
+    LpTriple* T = m->data[system];
+    int rc = ensure_work(m, T->nv, T->K, T->ncon);
+    if (rc) return rc;
+    cudaStream_t st = m->stream;
+    LpSys<float, float> S{T->nv, T->K, T->col.p, T->diag.p, T->val.p, T->cdiag.p, T->proj.p, T->ncon, T->ckind.p,
+                          T->cverts.p};
+    features(m, S, st);
+    const int nv = T->nv, K = T->K;
+    if (bf16) {
+        if (m->H == 32) forward_bf16<32, float>(m, nv, K, T->col.p, T->ncon, T->ckind.p, T->cverts.p, m->Pm.p, st);
+        else forward_bf16<16, float>(m, nv, K, T->col.p, T->ncon, T->ckind.p, T->cverts.p, m->Pm.p, st);
+    } else {
+        if (m->H == 32) forward<32, float>(m, nv, K, T->col.p, T->ncon, T->ckind.p, T->cverts.p, nullptr, m->Pm.p, st);
+        else forward<16, float>(m, nv, K, T->col.p, T->ncon, T->ckind.p, T->cverts.p, nullptr, m->Pm.p, st);
+    }
+    cudaError_t e = cudaSuccess;
+    if (out6) e = cudaMemcpyAsync(out6, m->o.p, sizeof(float) * kLpOut * nv, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && blocks9) e = cudaMemcpyAsync(blocks9, m->Pm.p, sizeof(float) * 9 * nv, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? CIPC_OK : set_cuda_error(e, "cipc_precond_infer");
 }
 
 extern "C" int cipc_precond_system_sizes(const cipc_precond* p, int system, int32_t* sizes4)

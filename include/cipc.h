@@ -258,6 +258,11 @@ int cipc_precond_loss_grad(cipc_precond* p, int system, double* loss, float* gra
  * per contact, packed upper triangle row by row), right-hand side and solution
  * (3 per vertex).  Any output may be NULL. */
 int cipc_precond_system_sizes(const cipc_precond* p, int system, int32_t* sizes4);
+/* Network outputs (6 per vertex) and preconditioner blocks (9 per vertex) for
+ * captured system `system`: bf16 = 1 runs the inference path the solver uses
+ * (message-passing layers on the BF16 tensor cores, FP32 accumulate), 0 the FP32
+ * training forward.  Either output may be NULL. */
+int cipc_precond_infer(cipc_precond* p, int system, int bf16, float* out6, float* blocks9);
 int cipc_precond_system_export(const cipc_precond* p, int system, int32_t* col, float* val, float* cdiag,
                                uint8_t* proj, int32_t* ckind, int32_t* cverts, float* chess, float* rhs,
                                float* sol);

@@ -170,3 +170,27 @@ def test_trained_network_against_block_jacobi(cuda, record_property):
     print("trained network vs block Jacobi: PCG iterations %d vs %d (gain %.3f), loss %.4f -> %.4f"
           % (it_l, it_bj, gain, before, after))
     assert gain > 0.5
+
+
+def test_bf16_inference_matches_fp32_forward(captured):
+    """The solver's inference path (message-passing layers as BF16 mma.m16n8k16
+    tiles, FP32 accumulate) against the FP32 training forward on captured
+    systems, with random non-zero weights: outputs within 3% of their range,
+    preconditioner blocks (exponentials of the outputs) within 8% of each
+    block's largest entry."""
+    pc = captured["pc"]
+    p0 = pc.params()
+    rng = np.random.default_rng(1)
+    pc.set_params(p0 + rng.standard_normal(p0.shape).astype(np.float32) * 0.1)
+    try:
+        for k in (0, pc.num_systems() - 1):
+            o32, P32 = pc.infer(k, bf16=False)
+            o16, P16 = pc.infer(k, bf16=True)
+            span = np.abs(o32).max()
+            assert span > 0
+            assert np.abs(o16 - o32).max() <= 0.03 * span, (k, np.abs(o16 - o32).max(), span)
+            scale = np.abs(P32).reshape(-1, 9).max(1)
+            err = np.abs(P16 - P32).reshape(-1, 9).max(1)
+            assert (err <= 0.08 * scale + 1e-30).all(), (k, (err / scale).max())
+    finally:
+        pc.set_params(p0)
