@@ -24,7 +24,7 @@ REF_ROOT = os.environ.get("CIPC_REFERENCE_ROOT", "/root/reference")
 
 def build_oracle(force=False):
     out = os.path.join(HERE, "liboracle.so")
-    srcs = [os.path.join(HERE, f) for f in ("oracle_math.cpp", "oracle_api.cpp", "oracle_shell.cpp", "oracle_learned.cpp")]
+    srcs = [os.path.join(HERE, f) for f in ("oracle_math.cpp", "oracle_api.cpp", "oracle_shell.cpp", "oracle_learned.cpp", "oracle_rod.cpp")]
     srcs = [s for s in srcs if os.path.exists(s)]
     deps = srcs + [os.path.join(HERE, f) for f in os.listdir(HERE) if f.endswith(".h")]
     if not force and os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
@@ -48,6 +48,10 @@ _REF_FUNCS = [
     ("Library/Math/BARRIER.h", "Barrier"),
     ("Library/Math/BARRIER.h", "Barrier_Gradient"),
     ("Library/Math/BARRIER.h", "Barrier_Hessian"),
+    ("Library/FEM/Shell/Rod/MASS_SPRING_DERIVATIVES.h", "g_MS"),
+    ("Library/FEM/Shell/Rod/MASS_SPRING_DERIVATIVES.h", "H_MS"),
+    ("Library/FEM/Shell/Rod/ROD_BENDING_DERIVATIVES.h", "g_RB"),
+    ("Library/FEM/Shell/Rod/ROD_BENDING_DERIVATIVES.h", "H_RB"),
 ]
 
 
@@ -89,6 +93,7 @@ def build_ref(force=False):
     parts.append("}\n")
     args12 = ", ".join("x[%d]" % k for k in range(12))
     args9 = ", ".join("x[%d]" % k for k in range(9))
+    args6 = ", ".join("x[%d]" % k for k in range(6))
     parts.append('extern "C" {\n'
                  "void ref_g_PT(const double* x, double* g) { ref::g_PT<double>(%s, g); }\n"
                  "void ref_H_PT(const double* x, double* H) { ref::H_PT<double>(%s, H); }\n"
@@ -103,7 +108,11 @@ def build_ref(force=False):
                  "  ref::Barrier<false>(d, dHat, k, out[0]);\n"
                  "  ref::Barrier_Gradient<false>(d, dHat, k, out[1]);\n"
                  "  ref::Barrier_Hessian<false>(d, dHat, k, out[2]); }\n"
-                 "}\n" % (args12, args12, args12, args12, args9, args9, args12, args12))
+                 "void ref_g_MS(double k, double l, const double* x, double* g) { ref::g_MS<double>(k, l, %s, g); }\n"
+                 "void ref_H_MS(double k, double l, const double* x, double* H) { ref::H_MS<double>(k, l, %s, H); }\n"
+                 "void ref_g_RB(const double* x, double* g) { ref::g_RB<double>(%s, g); }\n"
+                 "void ref_H_RB(const double* x, double* H) { ref::H_RB<double>(%s, H); }\n"
+                 "}\n" % (args12, args12, args12, args12, args9, args9, args12, args12, args6, args6, args9, args9))
     src = "".join(parts)
     cmd = ["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-x", "c++", "-", "-o", out]
     subprocess.run(cmd, input=src.encode(), check=True)

@@ -273,3 +273,27 @@ def lp_apply(S, x):
     L.orc_lp_apply(S.nv, S.K, _p(S.col), _p(S.val), S.ncon, _p(S.ckind), _p(S.cverts), _p(S.chess),
                    _p(_c(x, np.float64)), _p(y))
     return y
+
+
+def rod_spring(x6, L, K, project=True):
+    """(E, g[6], H[6x6]) of a rod stretching segment, E = K L/2 (|x0-x1|/L - 1)^2."""
+    lb = lib()
+    lb.orc_rod_spring.restype = ctypes.c_double
+    lb.orc_rod_spring.argtypes = [_P, ctypes.c_double, ctypes.c_double, _P, _P, ctypes.c_int]
+    x = _c(x6, np.float64)
+    g = np.zeros(6)
+    H = np.zeros((6, 6))
+    E = lb.orc_rod_spring(_p(x), L, K, _p(g), _p(H), 1 if project else 0)
+    return E, g, H
+
+
+def rod_bending(x9, lsum, Kb, project=True):
+    """(E, g[9], H[9x9]) of a rod hinge, E = Kb |kb|^2 / lsum."""
+    lb = lib()
+    lb.orc_rod_bending.restype = ctypes.c_double
+    lb.orc_rod_bending.argtypes = [_P, ctypes.c_double, ctypes.c_double, _P, _P, ctypes.c_int]
+    x = _c(x9, np.float64)
+    g = np.zeros(9)
+    H = np.zeros((9, 9))
+    E = lb.orc_rod_bending(_p(x), lsum, Kb, _p(g), _p(H), 1 if project else 0)
+    return E, g, H

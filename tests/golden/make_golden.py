@@ -1,7 +1,8 @@
 """Generates tests/golden/reference_derivs.npz from the reference's own code.
 
 The reference's symbolic-toolbox derivative routines (g_PT/H_PT, g_EE/H_EE,
-g_PE3D/H_PE3D, g_EECN2/H_EECN2) and its barrier functions are compiled from the
+g_PE3D/H_PE3D, g_EECN2/H_EECN2, the rod's g_MS/H_MS and g_RB/H_RB) and its
+barrier functions are compiled from the
 Codim-IPC sources by ``oracle/build.py:build_ref`` into
 ``oracle/_ref/libcipc_ref.so``; this script evaluates them on seeded inputs and
 stores inputs and outputs, so that the oracle and the CUDA kernels can be
@@ -59,6 +60,35 @@ def main():
         L.ref_barrier(d, dhat, kappa, o.ctypes.data)
         args.append([d, dhat, kappa, o[0], o[1], o[2]])
     out["barrier"] = np.array(args)
+    # discrete rod stretching (g_MS/H_MS with E_young = k, rest length l) and
+    # bending (g_RB/H_RB of |kb|^2)
+    for n in ("ref_g_MS", "ref_H_MS"):
+        getattr(L, n).argtypes = [ctypes.c_double, ctypes.c_double, P, P]
+    for n in ("ref_g_RB", "ref_H_RB"):
+        getattr(L, n).argtypes = [P, P]
+    XS = rng.standard_normal((32, 6))
+    KL = np.column_stack([10.0 ** rng.uniform(-1, 7, 32), rng.uniform(0.2, 2.0, 32)])
+    GS = np.zeros((32, 6))
+    HS = np.zeros((32, 6, 6))
+    for i in range(32):
+        xx = np.ascontiguousarray(XS[i])
+        g = np.zeros(6)
+        h = np.zeros(36)
+        L.ref_g_MS(KL[i, 0], KL[i, 1], xx.ctypes.data, g.ctypes.data)
+        L.ref_H_MS(KL[i, 0], KL[i, 1], xx.ctypes.data, h.ctypes.data)
+        GS[i], HS[i] = g, h.reshape(6, 6)
+    out.update(x_MS=XS, kl_MS=KL, g_MS=GS, H_MS=HS)
+    XB = rng.standard_normal((32, 9))
+    GB = np.zeros((32, 9))
+    HB = np.zeros((32, 9, 9))
+    for i in range(32):
+        xx = np.ascontiguousarray(XB[i])
+        g = np.zeros(9)
+        h = np.zeros(81)
+        L.ref_g_RB(xx.ctypes.data, g.ctypes.data)
+        L.ref_H_RB(xx.ctypes.data, h.ctypes.data)
+        GB[i], HB[i] = g, h.reshape(9, 9)
+    out.update(x_RB=XB, g_RB=GB, H_RB=HB)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_derivs.npz")
     np.savez_compressed(dst, **out)
     print("wrote", dst, os.path.getsize(dst), "bytes")

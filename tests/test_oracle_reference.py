@@ -155,3 +155,18 @@ def test_accd_is_conservative(orc):
         t_end = toc[i] if hit[i] else 1.0
         assert 0 < toc[i] <= 1.0
         assert _traj_min_d2(k, V, D, t_end, 300) > th * th
+
+
+def test_rod_elements_match_reference_golden(orc):
+    """Rod stretching and bending derivatives (ROD_STRETCHING.h, ROD_BENDING.h) of
+    the oracle's dual-number restatement against the reference's generated
+    g_MS/H_MS and g_RB/H_RB on the golden inputs (unprojected Hessians)."""
+    G = np.load(GOLD)
+    for x, kl, g, H in zip(G["x_MS"], G["kl_MS"], G["g_MS"], G["H_MS"]):
+        _, go, Ho = orc.rod_spring(x, kl[1], kl[0], project=False)
+        assert np.allclose(go, g, rtol=1e-11, atol=1e-11 * np.abs(g).max())
+        assert np.allclose(Ho, H, rtol=1e-10, atol=1e-10 * np.abs(H).max())
+    for x, g, H in zip(G["x_RB"], G["g_RB"], G["H_RB"]):
+        _, go, Ho = orc.rod_bending(x, 1.0, 1.0, project=False)
+        assert np.allclose(go, g, rtol=1e-10, atol=1e-10 * np.abs(g).max())
+        assert np.allclose(Ho, H, rtol=1e-9, atol=1e-9 * np.abs(H).max())
