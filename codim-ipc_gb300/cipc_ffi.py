@@ -198,6 +198,8 @@ _PP = ctypes.POINTER(ctypes.c_void_p)
 _SIGS.update({
     "cipc_sim_create": (_c_int, [_c_int, _vp, _c_int, _vp, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _vp, _c_dbl, _c_int, _PP]),
     "cipc_sim_destroy": (_c_int, [_vp]),
+    "cipc_sim_create_codim": (_c_int, [_c_int, _vp, _c_int, _vp, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _vp, _c_dbl, _c_int,
+                                       _vp, _PP]),
     "cipc_sim_init_oipc": (_c_int, [_vp, _c_dbl, _c_dbl, _vp, _vp]),
     "cipc_sim_set_kappa": (_c_int, [_vp, _c_dbl, _c_dbl]),
     "cipc_sim_get_kappa": (_c_int, [_vp, _vp]),
@@ -217,16 +219,38 @@ def make_params(h, dhat2, xi, mu=0.0, epsv2=1e-6, fric_iters=1, newton_tol=1e-2,
                       precision, pcg_tol, pcg_max_iters, preconditioner)
 
 
-class Sim:
-    """Owns one cipc_sim handle (device-resident shell scene)."""
+class CodimDesc(ctypes.Structure):
+    _fields_ = [("n_segments", ctypes.c_int), ("segments", ctypes.c_void_p), ("rod_E", ctypes.c_double),
+                ("rod_rho", ctypes.c_double), ("rod_thickness", ctypes.c_double), ("rod_bend_mult", ctypes.c_double),
+                ("n_particles", ctypes.c_int), ("particles", ctypes.c_void_p), ("particle_rho", ctypes.c_double),
+                ("particle_thickness", ctypes.c_double)]
 
-    def __init__(self, X, T, rho, E, nu, thickness, gravity=(0.0, -9.81, 0.0), bend_stiff_mult=1.0, nh=True):
+
+class Sim:
+    """Owns one cipc_sim handle (device-resident shell scene).
+
+    codim (optional): dict(segments=(n,2) ints, rod_E, rod_rho, rod_thickness,
+    rod_bend_mult=1, particles=(m,) ints, particle_rho, particle_thickness)."""
+
+    def __init__(self, X, T, rho, E, nu, thickness, gravity=(0.0, -9.81, 0.0), bend_stiff_mult=1.0, nh=True,
+                 codim=None):
         X = np.ascontiguousarray(X, np.float64)
-        T = np.ascontiguousarray(T, np.int32)
+        T = np.ascontiguousarray(T, np.int32).reshape(-1, 3)
         g = np.ascontiguousarray(gravity, np.float64)
         h = ctypes.c_void_p()
-        _check(lib().cipc_sim_create(X.shape[0], X.ctypes.data, T.shape[0], T.ctypes.data, rho, E, nu, thickness,
-                                     g.ctypes.data, bend_stiff_mult, 1 if nh else 0, ctypes.byref(h)))
+        if codim is None:
+            _check(lib().cipc_sim_create(X.shape[0], X.ctypes.data, T.shape[0], T.ctypes.data, rho, E, nu, thickness,
+                                         g.ctypes.data, bend_stiff_mult, 1 if nh else 0, ctypes.byref(h)))
+        else:
+            seg = np.ascontiguousarray(codim.get("segments", np.zeros((0, 2))), np.int32).reshape(-1, 2)
+            par = np.ascontiguousarray(codim.get("particles", np.zeros(0)), np.int32).reshape(-1)
+            d = CodimDesc(seg.shape[0], seg.ctypes.data if seg.size else None, codim.get("rod_E", 0.0),
+                          codim.get("rod_rho", 0.0), codim.get("rod_thickness", 0.0), codim.get("rod_bend_mult", 1.0),
+                          par.shape[0], par.ctypes.data if par.size else None, codim.get("particle_rho", 0.0),
+                          codim.get("particle_thickness", 0.0))
+            _check(lib().cipc_sim_create_codim(X.shape[0], X.ctypes.data, T.shape[0], T.ctypes.data, rho, E, nu,
+                                               thickness, g.ctypes.data, bend_stiff_mult, 1 if nh else 0,
+                                               ctypes.byref(d), ctypes.byref(h)))
         self.h = h
         self.nv = X.shape[0]
 

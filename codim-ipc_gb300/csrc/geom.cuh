@@ -152,6 +152,14 @@ CIPC_HD int ee_type(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
 
 CIPC_HD double pp_d2(d3 a, d3 b) { return n2(a - b); }
 CIPC_HD double pe_d2(d3 p, d3 e0, d3 e1) { return n2(cross(e0 - p, e1 - p)) / n2(e1 - e0); }
+
+// DISTANCE_TYPE.h:11-27, point-edge: 0 point-e0, 1 point-e1, 2 interior
+CIPC_HD int pe_type(d3 p, d3 e0, d3 e1)
+{
+    const d3 e = e1 - e0;
+    const double ratio = dot(e, p - e0) / n2(e);
+    return ratio < 0 ? 0 : (ratio > 1 ? 1 : 2);
+}
 CIPC_HD double pt_d2(d3 p, d3 t0, d3 t1, d3 t2)
 {
     const d3 b = cross(t1 - t0, t2 - t0);

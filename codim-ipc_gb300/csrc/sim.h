@@ -97,6 +97,13 @@ struct Sim {
     // blocks are zero with the row's own column; nnzb = ell_k * nv
     int nnzb = 0, ell_k = 0;
     DBuf<int> col, diag, tri_slot, hinge_slot;
+    // rods: segments (2 ints, info E L t), hinges (3 ints, info E*bendMult lsum t), block slots
+    int nrs = 0, nrh = 0;
+    DBuf<int> rseg, rhinge, rseg_slot, rhinge_slot;
+    DBuf<double> rinfo, rhinfo;
+    // boundary layout: bnode = [shell | rod nodes from codim0 | particles from codim1],
+    // the last nrod_e boundary edges are rod segments
+    int codim0 = 0, codim1 = 0, nrod_e = 0;
     // dynamic
     DBuf<double> x, xn, xt, v, g, dir, xprev, rhs, disp;
     DBuf<char> hval;  // BSR values, float or double per precision
@@ -138,8 +145,9 @@ struct Sim {
 };
 
 // host-side construction (sim_setup.cpp)
+struct CodimDesc;
 int sim_create(Sim** out, int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
-               double thickness, const double* gravity, double bendMult, int nh_model);
+               double thickness, const double* gravity, double bendMult, int nh_model, const CodimDesc* cd = nullptr);
 void sim_destroy(Sim* s);
 
 }  // namespace cipc

@@ -460,6 +460,61 @@ __global__ void k_cs_compact(ConSink S)
     }
 }
 
+// Codimensional nodes (IPC.h:271-350): rod and particle nodes (boundary nodes
+// from sv_begin) against the rod segments (the last boundary edges, grid items
+// relative to e_begin): point-edge classification, PP / PE merged like the rest.
+__global__ void k_cs_codim_pe(CsArgs a, int sv_begin, int e_begin)
+{
+    const int sv = sv_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (sv >= a.nbn) return;
+    const int vI = a.bnode[sv];
+    const d3 p = ld(a.x, vI);
+    int ql[3], qh[3];
+    ql[0] = cellc(p.x - a.dHat, a.G.inv);
+    ql[1] = cellc(p.y - a.dHat, a.G.inv);
+    ql[2] = cellc(p.z - a.dHat, a.G.inv);
+    qh[0] = cellc(p.x + a.dHat, a.G.inv);
+    qh[1] = cellc(p.y + a.dHat, a.G.inv);
+    qh[2] = cellc(p.z + a.dHat, a.G.inv);
+    grid_query(a.G, ql, qh, [&](int el) {
+        const int eI = e_begin + el;
+        const int e0 = a.bedge[2 * eI], e1 = a.bedge[2 * eI + 1];
+        if (vI == e0 || vI == e1) return;
+        if (a.dbc[vI] && a.dbc[e0] && a.dbc[e1]) return;
+        const d3 x0 = ld(a.x, e0), x1 = ld(a.x, e1);
+        const d3 mx = vmax3(x0, x1), mn = vmin3(x0, x1);
+        if (any_gt3(p - mx, a.dHat) || any_gt3(mn - p, a.dHat)) return;  // CCD.h:16-30
+        switch (pe_type(p, x0, x1)) {
+            case 0: if (pp_d2(p, x0) < a.dh2) emit_merge(a.S, kc_PP, vI, e0, -1); break;
+            case 1: if (pp_d2(p, x1) < a.dh2) emit_merge(a.S, kc_PP, vI, e1, -1); break;
+            default: if (pe_d2(p, x0, x1) < a.dh2) emit_merge(a.S, kc_PE, vI, e0, e1); break;
+        }
+    });
+}
+
+// particles (boundary nodes from sv_begin) against every later boundary node
+// (grid over all boundary nodes): point-point, merged
+__global__ void k_cs_codim_pp(CsArgs a, int sv_begin)
+{
+    const int sv = sv_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (sv >= a.nbn) return;
+    const int vI = a.bnode[sv];
+    const d3 p = ld(a.x, vI);
+    int ql[3], qh[3];
+    ql[0] = cellc(p.x - a.dHat, a.G.inv);
+    ql[1] = cellc(p.y - a.dHat, a.G.inv);
+    ql[2] = cellc(p.z - a.dHat, a.G.inv);
+    qh[0] = cellc(p.x + a.dHat, a.G.inv);
+    qh[1] = cellc(p.y + a.dHat, a.G.inv);
+    qh[2] = cellc(p.z + a.dHat, a.G.inv);
+    grid_query(a.G, ql, qh, [&](int svJ) {
+        if (svJ <= sv) return;
+        const int vJ = a.bnode[svJ];
+        if (a.dbc[vI] && a.dbc[vJ]) return;
+        if (pp_d2(p, ld(a.x, vJ)) < a.dh2) emit_merge(a.S, kc_PP, vI, vJ, -1);
+    });
+}
+
 int build_constraints(Sim* s, const double* x)
 {
     cudaStream_t st = s->stream;
@@ -473,7 +528,7 @@ int build_constraints(Sim* s, const double* x)
         // merge table: 4x the list capacity, power of two
         unsigned tsz = 1024;
         while (tsz < 4u * (unsigned)s->cap_con) tsz <<= 1;
-        const size_t need = grid_bytes(std::max(s->nbt, s->nbe), 16) + (size_t)tsz * 12 + (1 << 20);
+        const size_t need = grid_bytes(std::max(std::max(s->nbt, s->nbe), s->nbn), 16) + (size_t)tsz * 12 + (1 << 20);
         int rc = ensure_scratch(s, need);
         if (rc) return rc;
         Arena ar{s->scratch.p, s->scratch.n};
@@ -502,6 +557,35 @@ int build_constraints(Sim* s, const double* x)
         if (rc) return rc;
         a.G = G;
         k_cs_ee<<<nblk(s->nbe, 128), 128, 0, st>>>(a);
+        bool again = false;
+        if (s->nrod_e > 0 && s->nbn > s->codim0) {
+            ar.used = mark;
+            const int e_begin = s->nbe - s->nrod_e;
+            rc = build_grid(s, ar, s->nrod_e, 2, s->bedge.p + 2 * (size_t)e_begin, x, nullptr, 0, G);
+            if (rc == kNeedScratch) {
+                if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
+                again = true;
+            } else if (rc) {
+                return rc;
+            } else {
+                a.G = G;
+                k_cs_codim_pe<<<nblk(s->nbn - s->codim0, 128), 128, 0, st>>>(a, s->codim0, e_begin);
+            }
+        }
+        if (!again && s->nbn > s->codim1) {
+            ar.used = mark;
+            rc = build_grid(s, ar, s->nbn, 1, s->bnode.p, x, nullptr, 0, G);
+            if (rc == kNeedScratch) {
+                if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
+                again = true;
+            } else if (rc) {
+                return rc;
+            } else {
+                a.G = G;
+                k_cs_codim_pp<<<nblk(s->nbn - s->codim1, 128), 128, 0, st>>>(a, s->codim1);
+            }
+        }
+        if (again) continue;
         k_cs_compact<<<nblk(tsz, 256), 256, 0, st>>>(S);
         unsigned long long c[3];
         cudaMemcpyAsync(c, s->cnt.p, sizeof(c), cudaMemcpyDeviceToHost, st);
@@ -1053,6 +1137,48 @@ __global__ void k_ccd_ee(CcdCand c)
     });
 }
 
+// codimensional CCD candidates (IPC.h:2087-2165): particles (boundary nodes from
+// sv_begin) against rod segments (grid items relative to e_begin) and against every
+// later boundary node (grid over all boundary nodes, e_begin < 0)
+__global__ void k_ccd_codim(CcdCand c, int sv_begin, int e_begin)
+{
+    const int sv = sv_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (sv >= c.nbn) return;
+    const int vI = c.bnode[sv];
+    const d3 p = ld(c.x, vI), dp = ld(c.p, vI);
+    const d3 pe = p + scl(dp, c.alpha);
+    const d3 mn = vmin3(p, pe), mx = vmax3(p, pe);
+    int ql[3], qh[3];
+    ql[0] = cellc(mn.x - c.xi, c.G.inv);
+    ql[1] = cellc(mn.y - c.xi, c.G.inv);
+    ql[2] = cellc(mn.z - c.xi, c.G.inv);
+    qh[0] = cellc(mx.x + c.xi, c.G.inv);
+    qh[1] = cellc(mx.y + c.xi, c.G.inv);
+    qh[2] = cellc(mx.z + c.xi, c.G.inv);
+    const d3 mxp = vmax3(p, p + dp), mnp = vmin3(p, p + dp);
+    grid_query(c.G, ql, qh, [&](int it) {
+        if (e_begin >= 0) {
+            const int eI = e_begin + it;
+            const int e0 = c.bedge[2 * eI], e1 = c.bedge[2 * eI + 1];
+            if (vI == e0 || vI == e1) return;
+            if (c.dbc[vI] && c.dbc[e0] && c.dbc[e1]) return;
+            const d3 x0 = ld(c.x, e0), x1 = ld(c.x, e1), d0 = ld(c.p, e0), d1 = ld(c.p, e1);
+            const d3 mxe = vmax3(vmax3(x0, x1), vmax3(x0 + d0, x1 + d1));
+            const d3 mne = vmin3(vmin3(x0, x1), vmin3(x0 + d0, x1 + d1));
+            if (any_gt3(mnp - mxe, c.xi) || any_gt3(mne - mxp, c.xi)) return;  // CCD.h:238-257
+            add_pair(c, kPE, vI, e0, e1, -1);
+        } else {
+            if (it <= sv) return;
+            const int vJ = c.bnode[it];
+            if (c.dbc[vI] && c.dbc[vJ]) return;
+            const d3 q = ld(c.x, vJ), dq = ld(c.p, vJ);
+            const d3 mxq = vmax3(q, q + dq), mnq = vmin3(q, q + dq);
+            if (any_gt3(mnp - mxq, c.xi) || any_gt3(mnq - mxp, c.xi)) return;  // CCD.h:260-280
+            add_pair(c, kPP, vI, vJ, -1, -1);
+        }
+    });
+}
+
 int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double* alpha_out)
 {
     cudaStream_t st = s->stream;
@@ -1073,7 +1199,7 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
     if (span > 1) alpha /= span;
     int cap = std::max(4096, 8 * (s->nbn + s->nbe));
     for (int attempt = 0; attempt < 8; ++attempt) {
-        const size_t need = grid_bytes(std::max(s->nbt, s->nbe), 32) + (size_t)cap * (16 + 1 + 8 + 1) + (1 << 20);
+        const size_t need = grid_bytes(std::max(std::max(s->nbt, s->nbe), s->nbn), 32) + (size_t)cap * (16 + 1 + 8 + 1) + (1 << 20);
         int rc = ensure_scratch(s, need);
         if (rc) return rc;
         Arena ar{s->scratch.p, s->scratch.n};
@@ -1104,6 +1230,35 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         if (rc) return rc;
         c.G = G;
         k_ccd_ee<<<nblk(s->nbe, 128), 128, 0, st>>>(c);
+        bool again = false;
+        if (s->nrod_e > 0 && s->nbn > s->codim1) {
+            ar.used = mark;
+            const int e_begin = s->nbe - s->nrod_e;
+            rc = build_grid(s, ar, s->nrod_e, 2, s->bedge.p + 2 * (size_t)e_begin, x, p, alpha, G);
+            if (rc == kNeedScratch) {
+                if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
+                again = true;
+            } else if (rc) {
+                return rc;
+            } else {
+                c.G = G;
+                k_ccd_codim<<<nblk(s->nbn - s->codim1, 128), 128, 0, st>>>(c, s->codim1, e_begin);
+            }
+        }
+        if (!again && s->nbn > s->codim1) {
+            ar.used = mark;
+            rc = build_grid(s, ar, s->nbn, 1, s->bnode.p, x, p, alpha, G);
+            if (rc == kNeedScratch) {
+                if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
+                again = true;
+            } else if (rc) {
+                return rc;
+            } else {
+                c.G = G;
+                k_ccd_codim<<<nblk(s->nbn - s->codim1, 128), 128, 0, st>>>(c, s->codim1, -1);
+            }
+        }
+        if (again) continue;
         unsigned long long cc[2];
         cudaMemcpyAsync(cc, ctr, sizeof(cc), cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "elements.cuh"
+#include "rod.cuh"
 #include "sim.h"
 #include "sim_kernels.h"
 
@@ -150,6 +151,67 @@ __global__ void __launch_bounds__(128) k_bending(ElasticArgs a, HT* hval)
     if (a.red && threadIdx.x == 0) a.red[blockIdx.x] = s;
 }
 
+// rod stretching (ROD_STRETCHING.h:9-107): K = h^2 pi t^2 / 4 E, E = K L / 2 (l/L - 1)^2
+template <typename HT>
+__global__ void __launch_bounds__(128) k_rod_spring(ElasticArgs a, HT* hval)
+{
+    __shared__ double sh[128];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0;
+    if (t < a.nrs) {
+        const int vid[2] = {a.rseg[2 * t], a.rseg[2 * t + 1]};
+        if (!(a.dbc[vid[0]] && a.dbc[vid[1]])) {
+            const d3 x0 = ld(a.x, vid[0]), x1 = ld(a.x, vid[1]);
+            const double* ri = a.rinfo + 3 * t;
+            const double K = a.h * a.h * M_PI * ri[2] * ri[2] / 4 * ri[0];
+            double g[6];
+            e = rod_spring_eg(x0, x1, ri[1], K, a.g ? g : nullptr);
+            if (a.g)
+                for (int v = 0; v < 2; ++v)
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) atomicAdd(a.g + 3 * vid[v] + d, g[3 * v + d]);
+            if (hval) {
+                HT H[6][6];
+                rod_spring_hess<HT>(x0, x1, ri[1], K, H);
+                scatter_blocks<HT>(hval, a.rseg_slot + 4 * t, a.proj, vid, 2, &H[0][0], 6);
+            }
+        }
+    }
+    const double s = block_sum(e, sh);
+    if (a.red && threadIdx.x == 0) a.red[blockIdx.x] = s;
+}
+
+// rod bending (ROD_BENDING.h:9-120): Kb = h^2 E bendMult t^4 pi / 64, E = Kb |kb|^2 / lsum
+template <typename HT>
+__global__ void __launch_bounds__(128) k_rod_bend(ElasticArgs a, HT* hval)
+{
+    __shared__ double sh[128];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0;
+    if (t < a.nrh) {
+        const int vid[3] = {a.rhinge[3 * t], a.rhinge[3 * t + 1], a.rhinge[3 * t + 2]};
+        if (!(a.dbc[vid[0]] && a.dbc[vid[1]] && a.dbc[vid[2]])) {
+            const d3 x0 = ld(a.x, vid[0]), x1 = ld(a.x, vid[1]), x2 = ld(a.x, vid[2]);
+            const double* ri = a.rhinfo + 3 * t;
+            const double t2 = ri[2] * ri[2];
+            const double Kb = a.h * a.h * ri[0] * t2 * t2 * M_PI / 64;
+            double g[9];
+            e = rod_bend_eg(x0, x1, x2, ri[1], Kb, a.g ? g : nullptr);
+            if (a.g)
+                for (int v = 0; v < 3; ++v)
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) atomicAdd(a.g + 3 * vid[v] + d, g[3 * v + d]);
+            if (hval) {
+                HT H[9][9];
+                rod_bend_hess<HT>(x0, x1, x2, ri[1], Kb, H);
+                scatter_blocks<HT>(hval, a.rhinge_slot + 9 * t, a.proj, vid, 3, &H[0][0], 9);
+            }
+        }
+    }
+    const double s = block_sum(e, sh);
+    if (a.red && threadIdx.x == 0) a.red[blockIdx.x] = s;
+}
+
 // mass (+ Dirichlet penalty k m on penalized vertices) on free diagonal blocks,
 // identity on projected diagonal blocks
 template <typename HT>
@@ -258,20 +320,34 @@ ElasticArgs elastic_args(Sim* s, const double* x, double* g)
     a.kbend = s->kbend;
     a.nh_model = s->nh_model;
     a.red = nullptr;
+    a.nrs = s->nrs;
+    a.nrh = s->nrh;
+    a.rseg = s->rseg.p;
+    a.rhinge = s->rhinge.p;
+    a.rseg_slot = s->rseg_slot.p;
+    a.rhinge_slot = s->rhinge_slot.p;
+    a.rinfo = s->rinfo.p;
+    a.rhinfo = s->rhinfo.p;
     return a;
 }
 
-// Energy partial layout: [inertia | membrane | bending]; returns the partial count.
+// Energy partial layout: [inertia | membrane | bending | rod stretching | rod
+// bending]; returns the partial count.
 int elastic_energy_partials(Sim* s, const double* x, double* red)
 {
     const int b0 = nblk(s->nv, 256), b1 = nblk(s->nt, 128), b2 = nblk(s->nh, 128);
+    const int b3 = nblk(s->nrs, 128), b4 = nblk(s->nrh, 128);
     k_inertia<<<b0, 256, 0, s->stream>>>(s->nv, x, s->xt.p, s->mass.p, nullptr, red);
     ElasticArgs a = elastic_args(s, x, nullptr);
     a.red = red + b0;
     k_membrane<double><<<b1, 128, 0, s->stream>>>(a, nullptr);
     a.red = red + b0 + b1;
     k_bending<double><<<b2, 128, 0, s->stream>>>(a, nullptr);
-    return b0 + b1 + b2;
+    a.red = red + b0 + b1 + b2;
+    k_rod_spring<double><<<b3, 128, 0, s->stream>>>(a, nullptr);
+    a.red = red + b0 + b1 + b2 + b3;
+    k_rod_bend<double><<<b4, 128, 0, s->stream>>>(a, nullptr);
+    return b0 + b1 + b2 + b3 + b4;
 }
 
 void elastic_grad_hess(Sim* s, const double* x, double* g, bool want_hess)
@@ -284,6 +360,8 @@ void elastic_grad_hess(Sim* s, const double* x, double* g, bool want_hess)
         float* hv = want_hess ? (float*)s->hval.p : nullptr;
         k_membrane<float><<<nblk(s->nt, 128), 128, 0, s->stream>>>(a, hv);
         k_bending<float><<<nblk(s->nh, 128), 128, 0, s->stream>>>(a, hv);
+        if (s->nrs) k_rod_spring<float><<<nblk(s->nrs, 128), 128, 0, s->stream>>>(a, hv);
+        if (s->nrh) k_rod_bend<float><<<nblk(s->nrh, 128), 128, 0, s->stream>>>(a, hv);
         if (want_hess)
             k_mass_diag<float><<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->mass.p, s->proj.p, s->dbc.p,
                                                                       s->dbc_stiff, s->diag.p, hv);
@@ -291,6 +369,8 @@ void elastic_grad_hess(Sim* s, const double* x, double* g, bool want_hess)
         double* hv = want_hess ? (double*)s->hval.p : nullptr;
         k_membrane<double><<<nblk(s->nt, 128), 128, 0, s->stream>>>(a, hv);
         k_bending<double><<<nblk(s->nh, 128), 128, 0, s->stream>>>(a, hv);
+        if (s->nrs) k_rod_spring<double><<<nblk(s->nrs, 128), 128, 0, s->stream>>>(a, hv);
+        if (s->nrh) k_rod_bend<double><<<nblk(s->nrh, 128), 128, 0, s->stream>>>(a, hv);
         if (want_hess)
             k_mass_diag<double><<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->mass.p, s->proj.p, s->dbc.p,
                                                                        s->dbc_stiff, s->diag.p, hv);

@@ -20,6 +20,10 @@ struct ElasticArgs {
     double h, lam, mu, kbend;
     int nh_model;
     double* red;
+    // rods
+    int nrs, nrh;
+    const int *rseg, *rhinge, *rseg_slot, *rhinge_slot;
+    const double *rinfo, *rhinfo;
 };
 
 // sim_elastic.cu

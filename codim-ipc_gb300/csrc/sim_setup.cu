@@ -58,8 +58,22 @@ static double rest_dihedral(const double* X0, const double* X1, const double* X2
 }
 
 int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
-                     double thickness, const double* gravity, double bendMult, int nh_model)
+                     double thickness, const double* gravity, double bendMult, int nh_model, const CodimDesc* cd)
 {
+    if (cd) {
+        if (cd->nseg < 0 || cd->npart < 0 || (cd->nseg && !cd->seg) || (cd->npart && !cd->part))
+            return set_error(CIPC_ERR_INVALID_ARG, "codim setup: null arrays or negative counts");
+        for (int i = 0; i < 2 * cd->nseg; ++i)
+            if (cd->seg[i] < 0 || cd->seg[i] >= nv) return set_error(CIPC_ERR_INDEX_RANGE, "codim setup: segment index out of range");
+        for (int i = 0; i < cd->nseg; ++i)
+            if (cd->seg[2 * i] == cd->seg[2 * i + 1]) return set_error(CIPC_ERR_INVALID_ARG, "codim setup: degenerate segment");
+        for (int i = 0; i < cd->npart; ++i)
+            if (cd->part[i] < 0 || cd->part[i] >= nv) return set_error(CIPC_ERR_INDEX_RANGE, "codim setup: particle index out of range");
+        if (cd->nseg && !(cd->rod_thickness > 0 && cd->rod_rho > 0))
+            return set_error(CIPC_ERR_INVALID_ARG, "codim setup: rods need thickness > 0 and density > 0");
+        if (cd->npart && !(cd->part_thickness > 0 && cd->part_rho > 0))
+            return set_error(CIPC_ERR_INVALID_ARG, "codim setup: particles need thickness > 0 and density > 0");
+    }
     if (nv <= 0 || nt < 0 || !X || (nt && !tri))
         return set_error(CIPC_ERR_INVALID_ARG, "shell setup: empty mesh or null arrays");
     for (int i = 0; i < 3 * nt; ++i)
@@ -153,6 +167,55 @@ int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* t
     S.lam = E * nu / (1 - nu * nu);
     S.mu = E / (2 * (1 + nu));
     S.kbend = bendMult * (E * std::pow(thickness, 3) / (24 * (1 - nu * nu)));
+    // rods (DISCRETE_ROD.h:100-150): lumped segment mass, hinges between every pair
+    // of segments meeting at a vertex (vertex-ordered), rest data
+    S.codim0 = S.codim1 = (int)S.bnode.size();
+    if (cd && cd->nseg) {
+        std::map<int, std::vector<int>> nb;
+        std::map<int, double> rod_node;
+        for (int i = 0; i < cd->nseg; ++i) {
+            const int a = cd->seg[2 * i], b = cd->seg[2 * i + 1];
+            nb[a].push_back(b);
+            nb[b].push_back(a);
+            double d[3];
+            v3sub(X + 3 * a, X + 3 * b, d);
+            const double L = v3norm(d);
+            S.rseg.insert(S.rseg.end(), {a, b});
+            S.rinfo.insert(S.rinfo.end(), {cd->rod_E, L, cd->rod_thickness});
+            const double mp = L * M_PI * cd->rod_thickness * cd->rod_thickness / 4 * cd->rod_rho / 2;
+            for (int v : {a, b}) {
+                S.mass[v] += mp;
+                for (int k = 0; k < 3; ++k) S.b[3 * v + k] += mp * gravity[k];
+                rod_node[v] += 0;
+            }
+            S.bedge.insert(S.bedge.end(), {a, b});
+        }
+        for (auto& kv : nb)
+            if (kv.second.size() >= 2)
+                for (size_t i = 0; i < kv.second.size(); ++i)
+                    for (size_t j = i + 1; j < kv.second.size(); ++j) {
+                        const int x0 = kv.second[i], x1 = kv.first, x2 = kv.second[j];
+                        double d0[3], d1[3];
+                        v3sub(X + 3 * x1, X + 3 * x0, d0);
+                        v3sub(X + 3 * x2, X + 3 * x1, d1);
+                        S.rhinge.insert(S.rhinge.end(), {x0, x1, x2});
+                        S.rhinfo.insert(S.rhinfo.end(), {cd->rod_E * cd->rod_bend_mult, v3norm(d0) + v3norm(d1),
+                                                         cd->rod_thickness});
+                    }
+        for (auto& kv : rod_node) S.bnode.push_back(kv.first);
+        S.nrod_e = cd->nseg;
+    }
+    S.codim1 = (int)S.bnode.size();
+    // particles (DISCRETE_PARTICLE.h:60-69): mass 4/3 pi t^3 / 8 rho
+    if (cd && cd->npart) {
+        const double m = 4.0 / 3.0 * M_PI * std::pow(cd->part_thickness, 3) / 8 * cd->part_rho;
+        for (int i = 0; i < cd->npart; ++i) {
+            const int v = cd->part[i];
+            S.mass[v] += m;
+            for (int k = 0; k < 3; ++k) S.b[3 * v + k] += m * gravity[k];
+            S.bnode.push_back(v);
+        }
+    }
     // broad-phase cell: mean rest edge length
     double el = 0;
     int ne = (int)S.bedge.size() / 2;
@@ -172,6 +235,13 @@ int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* t
     for (int e = 0; e < nh; ++e)
         for (int a = 0; a < 4; ++a)
             for (int b = 0; b < 4; ++b) adj[S.hinge[4 * e + a]].push_back(S.hinge[4 * e + b]);
+    const int nrs = (int)S.rseg.size() / 2, nrh = (int)S.rhinge.size() / 3;
+    for (int e = 0; e < nrs; ++e)
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b) adj[S.rseg[2 * e + a]].push_back(S.rseg[2 * e + b]);
+    for (int e = 0; e < nrh; ++e)
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) adj[S.rhinge[3 * e + a]].push_back(S.rhinge[3 * e + b]);
     int K = 1;
     for (int i = 0; i < nv; ++i) {
         std::sort(adj[i].begin(), adj[i].end());
@@ -201,6 +271,14 @@ int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* t
     for (int e = 0; e < nh; ++e)
         for (int a = 0; a < 4; ++a)
             for (int b = 0; b < 4; ++b) S.hinge_slot[16 * e + 4 * a + b] = slot(S.hinge[4 * e + a], S.hinge[4 * e + b]);
+    S.rseg_slot.resize(4 * nrs);
+    for (int e = 0; e < nrs; ++e)
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b) S.rseg_slot[4 * e + 2 * a + b] = slot(S.rseg[2 * e + a], S.rseg[2 * e + b]);
+    S.rhinge_slot.resize(9 * nrh);
+    for (int e = 0; e < nrh; ++e)
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) S.rhinge_slot[9 * e + 3 * a + b] = slot(S.rhinge[3 * e + a], S.rhinge[3 * e + b]);
     return CIPC_OK;
 }
 
@@ -249,7 +327,14 @@ int sim_upload(Sim* s, const HostScene& S)
     UP(s->P, S.P) UP(s->vol, S.vol) UP(s->hinfo, S.hinfo) UP(s->mass, S.mass) UP(s->b, S.b) UP(s->X0, S.X0)
     UP(s->col, S.col) UP(s->diag, S.diag) UP(s->tri_slot, S.tri_slot)
     UP(s->hinge_slot, S.hinge_slot)
+    UP(s->rseg, S.rseg) UP(s->rhinge, S.rhinge) UP(s->rseg_slot, S.rseg_slot) UP(s->rhinge_slot, S.rhinge_slot)
+    UP(s->rinfo, S.rinfo) UP(s->rhinfo, S.rhinfo)
 #undef UP
+    s->nrs = (int)S.rseg.size() / 2;
+    s->nrh = (int)S.rhinge.size() / 3;
+    s->codim0 = S.codim0;
+    s->codim1 = S.codim1;
+    s->nrod_e = S.nrod_e;
     const size_t n3 = 3 * (size_t)S.nv;
     for (DBuf<double>* d : {&s->x, &s->xn, &s->xt, &s->v, &s->g, &s->dir, &s->xprev, &s->rhs, &s->disp})
         if (e == cudaSuccess) e = d->alloc(n3);
@@ -270,10 +355,10 @@ int sim_upload(Sim* s, const HostScene& S)
 }
 
 int sim_create(Sim** out, int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
-               double thickness, const double* gravity, double bendMult, int nh_model)
+               double thickness, const double* gravity, double bendMult, int nh_model, const CodimDesc* cd)
 {
     HostScene S;
-    int rc = build_host_scene(S, nv, X, nt, tri, rho, E, nu, thickness, gravity, bendMult, nh_model);
+    int rc = build_host_scene(S, nv, X, nt, tri, rho, E, nu, thickness, gravity, bendMult, nh_model, cd);
     if (rc != CIPC_OK) return rc;
     rc = ensure_device();
     if (rc != CIPC_OK) return rc;

@@ -111,7 +111,7 @@ __global__ void k_kappa_flag(int n, const int* kind, const int4* verts, const do
 // constraint distance is at or below the offset.
 static int eval_energy(Sim* s, const double* x, double* E, bool* ok)
 {
-    const int worst = nblk(s->nv, 256) + nblk(s->nt, 128) + nblk(s->nh, 128) +
+    const int worst = nblk(s->nv, 256) + nblk(s->nt, 128) + nblk(s->nh, 128) + nblk(s->nrs, 128) + nblk(s->nrh, 128) +
                       (s->prm.withCollision ? nblk(s->ncon, 128) + nblk(s->nfric, 128) : 0) + 16;
     if ((int)s->red.n < worst + 16) {
         cudaStreamSynchronize(s->stream);
@@ -404,11 +404,12 @@ void sim_destroy(Sim* s)
     pcg_release(s);
     for (DBuf<int>* b : {&s->tri, &s->hinge, &s->bnode, &s->bedge, &s->btri, &s->dbc_idx, &s->col,
                          &s->diag, &s->tri_slot, &s->hinge_slot, &s->ckind, &s->cmult, &s->fkind, &s->fmult,
+                         &s->rseg, &s->rhinge, &s->rseg_slot, &s->rhinge_slot,
                          &s->pkind})
         b->release();
     for (DBuf<double>* b : {&s->P, &s->vol, &s->hinfo, &s->mass, &s->b, &s->X0, &s->dbc_tgt, &s->x, &s->xn, &s->xt,
                             &s->v, &s->g, &s->dir, &s->xprev, &s->rhs, &s->disp, &s->fw, &s->fT, &s->flam, &s->pdiag,
-                            &s->red, &s->pd2})
+                            &s->red, &s->pd2, &s->rinfo, &s->rhinfo})
         b->release();
     s->dbc.release();
     s->proj.release();
@@ -451,6 +452,30 @@ extern "C" int cipc_sim_create(int nv, const double* X, int nt, const int* tri, 
     if (nv >= (1 << 21) - 1) return set_error(CIPC_ERR_INVALID_ARG, "cipc_sim_create: at most 2^21-2 vertices");
     Sim* s = nullptr;
     int rc = sim_create(&s, nv, X, nt, tri, rho, E, nu, thickness, gravity, bend_stiff_mult, membrane_model);
+    if (rc) return rc;
+    *out = new cipc_sim{s};
+    return CIPC_OK;
+}
+
+extern "C" int cipc_sim_create_codim(int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
+                                     double thickness, const double* gravity, double bend_stiff_mult,
+                                     int membrane_model, const cipc_codim_desc* codim, cipc_sim** out)
+{
+    if (!out || !gravity || !codim) return set_error(CIPC_ERR_INVALID_ARG, "cipc_sim_create_codim: null argument");
+    if (nv >= (1 << 21) - 1) return set_error(CIPC_ERR_INVALID_ARG, "cipc_sim_create_codim: at most 2^21-2 vertices");
+    CodimDesc cd;
+    cd.nseg = codim->n_segments;
+    cd.seg = codim->segments;
+    cd.rod_E = codim->rod_E;
+    cd.rod_rho = codim->rod_rho;
+    cd.rod_thickness = codim->rod_thickness;
+    cd.rod_bend_mult = codim->rod_bend_mult;
+    cd.npart = codim->n_particles;
+    cd.part = codim->particles;
+    cd.part_rho = codim->particle_rho;
+    cd.part_thickness = codim->particle_thickness;
+    Sim* s = nullptr;
+    int rc = sim_create(&s, nv, X, nt, tri, rho, E, nu, thickness, gravity, bend_stiff_mult, membrane_model, &cd);
     if (rc) return rc;
     *out = new cipc_sim{s};
     return CIPC_OK;

@@ -239,3 +239,45 @@ def merge_meshes(*meshes):
         offs.append(o)
         o += X.shape[0]
     return np.concatenate(Xs), np.concatenate(Ts).astype(np.int32), offs
+
+
+def rods_particles_on_cloth(n_rods=1000, seg_per_rod=100, rod_len=0.5, n_particles=20000, cloth_n=120,
+                            cloth_size=1.0, layer_gap=2.5e-3, particle_gap=8e-3, lift=0.02, seed=0):
+    """Mixed codimensional scene: straight rods of `seg_per_rod` segments and length
+    `rod_len`, each horizontal at its own height (layer_gap apart, so no two
+    overlap) with a seeded random in-plane direction and centre over the cloth;
+    particles on a grid (particle_gap apart) above the rods; a cloth_n x cloth_n
+    cloth (cloth_size square, y = 0) pinned at its four corners.
+
+    Returns X, T (cloth triangles), segments (n_rods*seg_per_rod, 2),
+    particles (indices), dbc (the 4 cloth corners)."""
+    rng = np.random.default_rng(seed)
+    Xc, Tc = cloth_grid(cloth_n, cloth_n, cloth_size, cloth_size, y=0.0, origin=(-cloth_size / 2, -cloth_size / 2))
+    nc = Xc.shape[0]
+    corners = np.array([0, cloth_n - 1, nc - cloth_n, nc - 1], np.int32)
+    pts = [Xc]
+    segs = []
+    o = nc
+    half = 0.5 * (cloth_size - rod_len) * 0.9
+    for r in range(n_rods):
+        th = rng.uniform(0, 2 * np.pi)
+        c = np.array([rng.uniform(-half, half), lift + r * layer_gap, rng.uniform(-half, half)])
+        d = np.array([np.cos(th), 0.0, np.sin(th)])
+        t = np.linspace(-0.5, 0.5, seg_per_rod + 1)[:, None] * rod_len
+        pts.append(c[None, :] + t * d[None, :])
+        segs.append(np.column_stack([np.arange(seg_per_rod), np.arange(1, seg_per_rod + 1)]) + o)
+        o += seg_per_rod + 1
+    top = lift + n_rods * layer_gap + particle_gap
+    side = int(np.ceil(np.sqrt(max(n_particles, 1) / 50.0)))
+    nx = max(1, min(side, int(cloth_size * 0.8 / particle_gap)))
+    ny = int(np.ceil(n_particles / (nx * nx))) if n_particles else 0
+    P = []
+    for k in range(n_particles):
+        i, j, l = k % nx, (k // nx) % nx, k // (nx * nx)
+        P.append([(i - (nx - 1) / 2) * particle_gap, top + l * particle_gap, (j - (nx - 1) / 2) * particle_gap])
+    if n_particles:
+        pts.append(np.array(P))
+    particles = np.arange(o, o + n_particles, dtype=np.int32)
+    X = np.concatenate(pts)
+    S = np.concatenate(segs).astype(np.int32) if segs else np.zeros((0, 2), np.int32)
+    return X, Tc.astype(np.int32), S, particles, corners

@@ -180,6 +180,24 @@ typedef struct cipc_sim cipc_sim;
 int cipc_sim_create(int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
                     double thickness, const double* gravity, double bend_stiff_mult, int membrane_model,
                     cipc_sim** out);
+/* Codimensional parts added to a shell scene (all vertices live in X):
+ * discrete rods (Make_Rod + Initialize_Discrete_Rod, Library/FEM/Shell/Rod/
+ * DISCRETE_ROD.h:85-150: segment mass, stretching and bending with hinges between
+ * every pair of segments meeting at a vertex) and particles
+ * (Initialize_Discrete_Particle, Library/FEM/Shell/DISCRETE_PARTICLE.h:52-75).
+ * Rod nodes and particles take part in contact as the reference's codimensional
+ * boundary nodes, rod segments as boundary edges (IMPLICIT_EULER.h:242-277). */
+typedef struct cipc_codim_desc {
+    int n_segments;
+    const int32_t* segments;  /* 2 vertex indices per rod segment */
+    double rod_E, rod_rho, rod_thickness, rod_bend_mult;
+    int n_particles;
+    const int32_t* particles; /* particle vertex indices */
+    double particle_rho, particle_thickness;
+} cipc_codim_desc;
+int cipc_sim_create_codim(int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
+                          double thickness, const double* gravity, double bend_stiff_mult, int membrane_model,
+                          const cipc_codim_desc* codim, cipc_sim** out);
 int cipc_sim_destroy(cipc_sim* sim);
 /* Offset-IPC barrier stiffness; replaces FEM.DiscreteShell.Initialize_OIPC
  * (DISCRETE_SHELL.h:555-577, export :1103).  Writes (kappa, kappa_max) and dhat^2. */

@@ -125,7 +125,7 @@ def set_threads(n):
 class Shell:
     """The oracle's shell scene and time step (oracle_shell.cpp)."""
 
-    def __init__(self, X, T, rho, E, nu, thickness, gravity=(0.0, -9.81, 0.0), bend_mult=1.0, nh=True):
+    def __init__(self, X, T, rho, E, nu, thickness, gravity=(0.0, -9.81, 0.0), bend_mult=1.0, nh=True, codim=None):
         L = lib()
         L.orc_shell_create.restype = _P
         L.orc_shell_create.argtypes = [ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_double, ctypes.c_double,
@@ -148,8 +148,23 @@ class Shell:
         self.X = _c(X, np.float64)
         T = _c(T, np.int32)
         g = _c(gravity, np.float64)
-        self.h = L.orc_shell_create(self.X.shape[0], _p(self.X), T.shape[0], _p(T), rho, E, nu, thickness, _p(g),
-                                    bend_mult, 1 if nh else 0)
+        T = T.reshape(-1, 3)
+        if codim is None:
+            self.h = L.orc_shell_create(self.X.shape[0], _p(self.X), T.shape[0], _p(T), rho, E, nu, thickness, _p(g),
+                                        bend_mult, 1 if nh else 0)
+        else:
+            L.orc_shell_create_codim.restype = _P
+            L.orc_shell_create_codim.argtypes = [ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_double,
+                                                 ctypes.c_double, ctypes.c_double, ctypes.c_double, _P,
+                                                 ctypes.c_double, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int, _P, _P]
+            seg = _c(codim.get("segments", np.zeros((0, 2))), np.int32).reshape(-1, 2)
+            par = _c(codim.get("particles", np.zeros(0)), np.int32).reshape(-1)
+            prm = np.array([codim.get("rod_E", 0.0), codim.get("rod_rho", 0.0), codim.get("rod_thickness", 0.0),
+                            codim.get("rod_bend_mult", 1.0), codim.get("particle_rho", 0.0),
+                            codim.get("particle_thickness", 0.0)])
+            self.h = L.orc_shell_create_codim(self.X.shape[0], _p(self.X), T.shape[0], _p(T), rho, E, nu, thickness,
+                                              _p(g), bend_mult, 1 if nh else 0, seg.shape[0], _p(seg), par.shape[0],
+                                              _p(par), _p(prm))
         self.nv = self.X.shape[0]
         self.dbc = np.zeros(0, np.int32)
 

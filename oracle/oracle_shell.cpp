@@ -347,6 +347,54 @@ static void shell_init(Shell& S, int nv, const double* X, int nt, const int* tri
 // offset-IPC barrier stiffness (DISCRETE_SHELL.h:555-577 with elasticIPC = false):
 // kappa = mult * 1e11 * mean(diag M) * 3 / (4e-16 * b''(1e-16; dHat^2, kappa = 1)),
 // kappa_max = 100 kappa.  Returns dHat^2.
+// Rods (DISCRETE_ROD.h:85-150) and particles (DISCRETE_PARTICLE.h:52-75) added to
+// a shell scene, with the boundary layout of IMPLICIT_EULER.h:242-277.
+static void codim_init(Shell& S, const double* X, int nseg, const int* seg, double rodE, double rodRho, double rodT,
+                       double rodBendMult, int npart, const int* part, double partRho, double partT,
+                       const double* gravity)
+{
+    S.codim0 = (int)S.bnode.size();
+    std::map<int, std::vector<int>> nb;
+    std::map<int, int> rod_node;
+    for (int i = 0; i < nseg; ++i) {
+        const int a = seg[2 * i], b = seg[2 * i + 1];
+        nb[a].push_back(b);
+        nb[b].push_back(a);
+        const double L = std::sqrt(norm2(ld3(X + 3 * a) - ld3(X + 3 * b)));
+        S.rseg.insert(S.rseg.end(), {a, b});
+        S.rinfo.insert(S.rinfo.end(), {rodE, L, rodT});
+        const double mp = L * M_PI * rodT * rodT / 4 * rodRho / 2;
+        for (int v : {a, b}) {
+            S.mass[v] += mp;
+            for (int k = 0; k < 3; ++k) S.b[3 * v + k] += mp * gravity[k];
+            rod_node[v] = 1;
+        }
+        S.bedge.insert(S.bedge.end(), {a, b});
+    }
+    for (auto& kv : nb)
+        if (kv.second.size() >= 2)
+            for (size_t i = 0; i < kv.second.size(); ++i)
+                for (size_t j = i + 1; j < kv.second.size(); ++j) {
+                    const int x0 = kv.second[i], x1 = kv.first, x2 = kv.second[j];
+                    const double l0 = std::sqrt(norm2(ld3(X + 3 * x1) - ld3(X + 3 * x0)));
+                    const double l1 = std::sqrt(norm2(ld3(X + 3 * x2) - ld3(X + 3 * x1)));
+                    S.rhinge.insert(S.rhinge.end(), {x0, x1, x2});
+                    S.rhinfo.insert(S.rhinfo.end(), {rodE * rodBendMult, l0 + l1, rodT});
+                }
+    for (auto& kv : rod_node) S.bnode.push_back(kv.first);
+    S.nrod_e = nseg;
+    S.codim1 = (int)S.bnode.size();
+    if (npart) {
+        const double m = 4.0 / 3.0 * M_PI * partT * partT * partT / 8 * partRho;
+        for (int i = 0; i < npart; ++i) {
+            const int v = part[i];
+            S.mass[v] += m;
+            for (int k = 0; k < 3; ++k) S.b[3 * v + k] += m * gravity[k];
+            S.bnode.push_back(v);
+        }
+    }
+}
+
 static double shell_oipc_kappa(const Shell& S, double dhat, double stiffMult, double* kappa)
 {
     double dHat2 = dhat * dhat;
@@ -401,11 +449,44 @@ static inline void scatter_add(double* g, const int* vid, int n, const double* i
     for (int a = 0; a < n; ++a)
         for (int d = 0; d < 3; ++d) g[3 * vid[a] + d] += in[3 * a + d];
 }
+extern "C" double orc_rod_spring(const double* x6, double L, double K, double* g, double* H, int project);
+extern "C" double orc_rod_bending(const double* x9, double lsum, double Kb, double* g, double* H, int project);
+
 static inline bool all_dbc(const Shell& S, const int* v, int n)
 {
     for (int k = 0; k < n; ++k)
         if (!S.dbc[v[k]]) return false;
     return true;
+}
+
+// rod stretching and bending (ROD_STRETCHING.h:9-107, ROD_BENDING.h:9-120)
+static double rod_terms(const Shell& S, const double* x, double h, double* g, Asm* A)
+{
+    double E = 0;
+    const int nrs = (int)S.rseg.size() / 2, nrh = (int)S.rhinge.size() / 3;
+    for (int e = 0; e < nrs; ++e) {
+        const int* v = &S.rseg[2 * e];
+        if (all_dbc(S, v, 2)) continue;
+        double xe[6], ge[6], H[36];
+        gather(x, v, 2, xe);
+        const double* ri = &S.rinfo[3 * e];
+        const double K = h * h * M_PI * ri[2] * ri[2] / 4 * ri[0];
+        E += orc_rod_spring(xe, ri[1], K, ge, A ? H : nullptr, 1);
+        if (g) scatter_add(g, v, 2, ge);
+        if (A) A->add_block(v, 2, H);
+    }
+    for (int e = 0; e < nrh; ++e) {
+        const int* v = &S.rhinge[3 * e];
+        if (all_dbc(S, v, 3)) continue;
+        double xe[9], ge[9], H[81];
+        gather(x, v, 3, xe);
+        const double* ri = &S.rhinfo[3 * e];
+        const double Kb = h * h * ri[0] * std::pow(ri[2], 4) * M_PI / 64;
+        E += orc_rod_bending(xe, ri[1], Kb, ge, A ? H : nullptr, 1);
+        if (g) scatter_add(g, v, 3, ge);
+        if (A) A->add_block(v, 3, H);
+    }
+    return E;
 }
 
 static double elastic_energy(const Shell& S, const double* x, double h)
@@ -431,11 +512,13 @@ static double elastic_energy(const Shell& S, const double* x, double h)
             E += h * h * S.kbend * (th - hi[0]) * (th - hi[0]) * hi[1] / hi[2];
         }
     }
+    E += rod_terms(S, x, h, nullptr, nullptr);
     return E;
 }
 
 static void elastic_grad_hess(const Shell& S, const double* x, double h, double* g, Asm* A)
 {
+    rod_terms(S, x, h, g, A);
     int nt = (int)S.vol.size();
     for (int t = 0; t < nt; ++t) {
         const int* v = &S.tri[3 * t];
@@ -677,6 +760,43 @@ static void constraint_set(const Shell& S, const double* x, double dHat2, double
                     }
                     break;
             }
+        }
+    }
+    // codimensional nodes (IPC.h:271-350): rod and particle nodes against rod
+    // segments (point-edge classification), particles against later boundary nodes
+    const int nbn = (int)S.bnode.size();
+    if (S.nrod_e > 0 && nbn > S.codim0) {
+        const int e_begin = ne - S.nrod_e;
+        G.cells.clear();
+        for (int e = e_begin; e < ne; ++e) {
+            V3 a = ld3(x + 3 * S.bedge[2 * e]), b = ld3(x + 3 * S.bedge[2 * e + 1]);
+            G.insert(e, vmin(a, b), vmax(a, b));
+        }
+        for (int sv = S.codim0; sv < nbn; ++sv) {
+            const int vI = S.bnode[sv];
+            V3 p = ld3(x + 3 * vI);
+            G.query(vadd(p, -dHat), vadd(p, dHat), cand);
+            for (int eI : cand) {
+                const int e0 = S.bedge[2 * eI], e1 = S.bedge[2 * eI + 1];
+                if (vI == e0 || vI == e1) continue;
+                if (S.dbc[vI] && S.dbc[e0] && S.dbc[e1]) continue;
+                V3 x0 = ld3(x + 3 * e0), x1 = ld3(x + 3 * e1);
+                if (any_gt(p - vmax(x0, x1), dHat) || any_gt(vmin(x0, x1) - p, dHat)) continue;  // CCD.h:16-30
+                switch (pe_type(p, x0, x1)) {
+                    case 0: if (pp_d2(p, x0) < dh2) add_merge(kPP, vI, e0, -1); break;
+                    case 1: if (pp_d2(p, x1) < dh2) add_merge(kPP, vI, e1, -1); break;
+                    default: if (pe_d2(p, x0, x1) < dh2) add_merge(kPE, vI, e0, e1); break;
+                }
+            }
+        }
+    }
+    for (int sv = S.codim1; sv < nbn; ++sv) {
+        const int vI = S.bnode[sv];
+        V3 p = ld3(x + 3 * vI);
+        for (int svJ = sv + 1; svJ < nbn; ++svJ) {
+            const int vJ = S.bnode[svJ];
+            if (S.dbc[vI] && S.dbc[vJ]) continue;
+            if (pp_d2(p, ld3(x + 3 * vJ)) < dh2) add_merge(kPP, vI, vJ, -1);
         }
     }
     for (auto& k : order) cs.push_back(Con{k[0], {k[1], k[2], k[3], -1}, merge[k]});
@@ -1037,6 +1157,35 @@ static double ccd_step_size(const Shell& S, const double* x, const double* p, do
             int64_t it;
             if (accd_ee(ea0, ea1, eb0, eb1, da0, da1, db0, db1, 0.1, xi, &toc, cap, &it) == 1 && toc < stepSize)
                 stepSize = toc;
+        }
+    }
+    // codimensional pairs (IPC.h:2087-2165): particles against rod segments and
+    // against later boundary nodes
+    const int nbn = (int)S.bnode.size();
+    for (int sv = S.codim1; sv < nbn; ++sv) {
+        const int vI = S.bnode[sv];
+        V3 pp = ld3(x + 3 * vI), dp = ld3(p + 3 * vI);
+        V3 mxp = vmax(pp, pp + dp), mnp = vmin(pp, pp + dp);
+        for (int eI = ne - S.nrod_e; eI < ne; ++eI) {
+            const int e0 = S.bedge[2 * eI], e1 = S.bedge[2 * eI + 1];
+            if (vI == e0 || vI == e1) continue;
+            if (S.dbc[vI] && S.dbc[e0] && S.dbc[e1]) continue;
+            V3 x0 = ld3(x + 3 * e0), x1 = ld3(x + 3 * e1), d0 = ld3(p + 3 * e0), d1 = ld3(p + 3 * e1);
+            V3 mxe = vmax(vmax(x0, x1), vmax(x0 + d0, x1 + d1)), mne = vmin(vmin(x0, x1), vmin(x0 + d0, x1 + d1));
+            if (any_gt(mnp - mxe, xi) || any_gt(mne - mxp, xi)) continue;
+            double toc = stepSize;
+            int64_t it;
+            if (accd_pe(pp, x0, x1, dp, d0, d1, 0.1, xi, &toc, cap, &it) == 1 && toc < stepSize) stepSize = toc;
+        }
+        for (int svJ = sv + 1; svJ < nbn; ++svJ) {
+            const int vJ = S.bnode[svJ];
+            if (S.dbc[vI] && S.dbc[vJ]) continue;
+            V3 q = ld3(x + 3 * vJ), dq = ld3(p + 3 * vJ);
+            V3 mxq = vmax(q, q + dq), mnq = vmin(q, q + dq);
+            if (any_gt(mnp - mxq, xi) || any_gt(mnq - mxp, xi)) continue;
+            double toc = stepSize;
+            int64_t it;
+            if (accd_pp(pp, q, dp, dq, 0.1, xi, &toc, cap, &it) == 1 && toc < stepSize) stepSize = toc;
         }
     }
     return stepSize;
@@ -1412,6 +1561,17 @@ void* orc_shell_create(int nv, const double* X, int nt, const int* tri, double r
 {
     Shell* S = new Shell();
     shell_init(*S, nv, X, nt, tri, rho, E, nu, thickness, gravity, bendMult, nh_model);
+    return S;
+}
+
+// shell scene plus rods and particles; codim = (rodE, rodRho, rodT, rodBendMult, partRho, partT)
+void* orc_shell_create_codim(int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
+                             double thickness, const double* gravity, double bendMult, int nh_model, int nseg,
+                             const int* seg, int npart, const int* part, const double* codim)
+{
+    Shell* S = new Shell();
+    shell_init(*S, nv, X, nt, tri, rho, E, nu, thickness, gravity, bendMult, nh_model);
+    codim_init(*S, X, nseg, seg, codim[0], codim[1], codim[2], codim[3], npart, part, codim[4], codim[5], gravity);
     return S;
 }
 

@@ -31,6 +31,12 @@ struct Shell {
     std::vector<int> bnode, bedge, btri;  // contact primitives
     std::vector<char> dbc;            // nv mask
     int nh_model = 1;                 // membrane: 1 Neo-Hookean (reference default), 0 StVK
+    // discrete rods: segments (2) with (E, L, t), hinges (3) with (E bendMult, lsum, t)
+    std::vector<int> rseg, rhinge;
+    std::vector<double> rinfo, rhinfo;
+    // bnode = [shell nodes | rod nodes from codim0 | particles from codim1];
+    // the last nrod_e boundary edges are the rod segments
+    int codim0 = 0, codim1 = 0, nrod_e = 0;
 };
 
 struct StepParams {
