@@ -181,7 +181,8 @@ class StepParams(ctypes.Structure):
     _fields_ = [("h", ctypes.c_double), ("dhat2", ctypes.c_double), ("xi", ctypes.c_double), ("mu", ctypes.c_double),
                 ("epsv2", ctypes.c_double), ("fric_iters", ctypes.c_int), ("newton_tol", ctypes.c_double),
                 ("with_collision", ctypes.c_int), ("max_newton_iters", ctypes.c_int), ("precision", ctypes.c_int),
-                ("pcg_tol", ctypes.c_double), ("pcg_max_iters", ctypes.c_int), ("preconditioner", ctypes.c_int)]
+                ("pcg_tol", ctypes.c_double), ("pcg_max_iters", ctypes.c_int), ("preconditioner", ctypes.c_int),
+                ("forcing", ctypes.c_int)]
 
 
 class StepStats(ctypes.Structure):
@@ -214,9 +215,10 @@ _SIGS.update({
 
 
 def make_params(h, dhat2, xi, mu=0.0, epsv2=1e-6, fric_iters=1, newton_tol=1e-2, with_collision=True,
-                max_newton_iters=200, precision=FP64, pcg_tol=1e-6, pcg_max_iters=10000, preconditioner=0):
+                max_newton_iters=200, precision=FP64, pcg_tol=1e-6, pcg_max_iters=10000, preconditioner=0,
+                forcing=0):
     return StepParams(h, dhat2, xi, mu, epsv2, fric_iters, newton_tol, int(bool(with_collision)), max_newton_iters,
-                      precision, pcg_tol, pcg_max_iters, preconditioner)
+                      precision, pcg_tol, pcg_max_iters, preconditioner, forcing)
 
 
 class CodimDesc(ctypes.Structure):

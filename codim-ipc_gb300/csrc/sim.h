@@ -59,6 +59,7 @@ struct SimParams {
     double pcg_tol = 1e-6;    // relative residual of the Newton system (FP64)
     int pcg_maxit = 10000;
     int precond = 0;          // 0 block-Jacobi, 1 learned correction (when a model is loaded)
+    int forcing = 0;          // 1: inexact Newton (Eisenstat-Walker forcing term)
 };
 
 struct StepStats {
@@ -141,6 +142,7 @@ struct Sim {
     void* learned = nullptr;
     void* capture = nullptr;
     int solve_fallbacks = 0, solve_learned = 0;  // counts of the current step
+    double solve_tol = 0;                        // relative tolerance of the next linear solve (0: prm.pcg_tol)
     std::vector<double> host_mass;
 };
 

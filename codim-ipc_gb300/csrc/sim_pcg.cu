@@ -17,15 +17,19 @@
 //            with atomics, and p_k^T H p_k is summed element by element.
 //   update   alpha = (r,z)/(p,Hp); x += alpha p; r -= alpha (q_e + q_c); q_c = 0;
 //            z = M^-1 r; (r,z) and (r,r).
-// Each phase ends with per-block partial sums; after the barrier every block
-// adds the partials in the same fixed order, so all blocks take the same stop
-// decision.  Data written by other blocks during the solve is read through L2
-// (ld.global.cg), never from a stale L1 line.
+// Each phase ends with a grid-wide sum: every block adds its block sum into a
+// triple-buffered FP64 accumulator with fire-and-forget reductions, arrives on a
+// monotone counter with release semantics and polls it with acquire loads; the
+// totals are then read from the accumulator, so every block reads the same value
+// and takes the same stop decision (the order of the additions, and so the last
+// bits of a total, may differ from run to run).  Data written by other blocks
+// during the solve is read through L2 (ld.global.cg), never from a stale L1 line.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "../../include/cipc.h"
@@ -37,7 +41,7 @@
 
 namespace cipc {
 
-// results of one solve, and the grid barrier's state
+// results of one solve, and the grid reduction's state (zeroed before each solve)
 struct PcgScalars {
     double rr;      // (r, r) at exit
     double bb;      // (b, b)
@@ -46,11 +50,10 @@ struct PcgScalars {
     int done;       // 1 converged, 2 NaN, 3 (p, Hp) <= 0, 4 iteration cap, 5 barrier wait gave up
     int err;
     int pad;
-    double tot[2];  // totals published by the last block to arrive at a reduction
-    // arrival counter and release generation on their own 128-byte lines, so that
-    // the waiting blocks' polling does not contend with the arrivals
-    alignas(128) unsigned int bar_count;
-    alignas(128) unsigned int bar_gen;
+    // arrivals (monotone: gridDim.x per reduction) and the accumulators, on their
+    // own 128-byte lines; reduction e adds into acc[e % 3]
+    alignas(128) unsigned int arrive;
+    alignas(128) double acc[3][4];
     // with tracing on: block 0's time (ns) in apply, reduction 1, -, update,
     // reduction 2, -, summed over iterations
     unsigned long long tphase[6];
@@ -87,8 +90,6 @@ struct PcgArgs {
     XT* P1;
     XT* qe;
     XT* qc;
-    double* part_a;  // 1 partial per block (apply phase)
-    double* part_b;  // 2 partials per block (init / update phase)
     PcgScalars* d;
     double tol;
     int maxit;
@@ -99,7 +100,11 @@ struct PcgArgs {
 // 256-thread blocks, 4 per SM: a grid-wide reduction costs ~5-7 us here against
 // ~9 us with one 1024-thread block per SM (block-level sums dominate)
 constexpr int kPcgThreads = 256;
-constexpr unsigned int kBarrierSpinLimit = 1u << 25;  // x >= 32 ns of sleep: over a second
+// polls of the arrival counter before a wait gives up: each poll is an L2 round
+// trip (>= ~0.3 us), and past kBarrierBackoff polls a 64 ns sleep is added, so the
+// limit is over a second
+constexpr unsigned int kBarrierSpinLimit = 1u << 22;
+constexpr unsigned int kBarrierBackoff = 4096;
 
 template <typename T>
 __device__ __forceinline__ T ldcg(const T* p)
@@ -107,12 +112,36 @@ __device__ __forceinline__ T ldcg(const T* p)
     return __ldcg(p);
 }
 
-// sum of v over the block, returned to every thread
-template <int N>
-__device__ __forceinline__ void block_sum_all(double (&v)[N])
+__device__ __forceinline__ void red_add_f64(double* p, double v)
 {
+    asm volatile("red.relaxed.gpu.global.add.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+__device__ __forceinline__ void red_release_add_u32(unsigned int* p, unsigned int v)
+{
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p)
+{
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid-wide sum of v (N <= 4 values per thread, summed over all threads of all
+// blocks), returned in v to every thread; also a grid barrier.  epoch counts the
+// reductions this thread has taken part in (the same in every thread).  Thread 0
+// of each block adds the block's sums into acc[epoch % 3], arrives with release
+// semantics and polls the counter until every block of reduction `epoch` has
+// arrived.  acc[(epoch + 2) % 3] held the totals of reduction epoch - 1, which
+// every block has read before arriving here, so block 0 clears it for reduction
+// epoch + 2.  Returns false if the wait gave up (err set; the kernel returns).
+template <int N>
+__device__ __forceinline__ bool grid_allreduce(double (&v)[N], PcgScalars* d, unsigned int& epoch)
+{
+    static_assert(N >= 1 && N <= 4, "reduction width");
     __shared__ double sh[N][kPcgThreads / 32];
     __shared__ double res[N];
+    __shared__ int ok;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < N; ++k) {
@@ -122,75 +151,42 @@ __device__ __forceinline__ void block_sum_all(double (&v)[N])
         if (lane == 0) sh[k][wid] = a;
     }
     __syncthreads();
-    if (threadIdx.x < N) {
-        double a = 0;
-        for (int w = 0; w < kPcgThreads / 32; ++w) a += sh[threadIdx.x][w];
-        res[threadIdx.x] = a;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < N; ++k) v[k] = res[k];
-    __syncthreads();
-}
-
-// Grid-wide sum of v (N values per thread, summed over all threads of all
-// blocks), returned in v to every thread, with the barrier semantics of
-// grid_barrier.  Each block writes its partial and arrives; the last block to
-// arrive adds the partials in block order, publishes the totals and releases
-// the others, which then read the totals.  Returns false if a wait gave up.
-template <int N>
-__device__ __forceinline__ bool grid_allreduce(double (&v)[N], double* part, PcgScalars* d)
-{
-    __shared__ int ok, last;
-    block_sum_all<N>(v);
     if (threadIdx.x == 0) {
-        ok = 1;
-        last = 0;
+        double* acc = d->acc[epoch % 3];
 #pragma unroll
-        for (int k = 0; k < N; ++k) part[N * blockIdx.x + k] = v[k];
-        volatile unsigned int* gen = &d->bar_gen;
-        volatile int* err = &d->err;
-        const unsigned int g = *gen;
-        __threadfence();
-        if (atomicAdd(&d->bar_count, 1u) == gridDim.x - 1) {
-            last = 1;
-        } else {
-            unsigned int spins = 0;
-            while (*gen == g) {
-                if (*err || ++spins > kBarrierSpinLimit) {
-                    atomicExch(&d->err, 1);
-                    ok = 0;
-                    break;
-                }
-                if (spins > 512) __nanosleep(32);
-            }
-            __threadfence();
+        for (int k = 0; k < N; ++k) {
+            double a = 0;
+#pragma unroll
+            for (int w = 0; w < kPcgThreads / 32; ++w) a += sh[k][w];
+            red_add_f64(acc + k, a);
         }
+        red_release_add_u32(&d->arrive, 1u);
+        const unsigned int target = (epoch + 1) * gridDim.x;
+        int good = 1;
+        unsigned int spins = 0;
+        while ((int)(ld_acquire_u32(&d->arrive) - target) < 0) {
+            ++spins;
+            if (spins > kBarrierSpinLimit || ((spins & 255) == 0 && *(volatile int*)&d->err)) {
+                atomicExch(&d->err, 1);
+                good = 0;
+                break;
+            }
+            if (spins > kBarrierBackoff) __nanosleep(64);
+        }
+#pragma unroll
+        for (int k = 0; k < N; ++k) res[k] = __ldcg(acc + k);
+        if (blockIdx.x == 0) {
+            double* z = d->acc[(epoch + 2) % 3];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) z[k] = 0;
+        }
+        ok = good;
     }
     __syncthreads();
-    if (last) {
-        __threadfence();
-        double acc[N];
-#pragma unroll
-        for (int k = 0; k < N; ++k) acc[k] = 0;
-        for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
-#pragma unroll
-            for (int k = 0; k < N; ++k) acc[k] += ldcg(part + N * b + k);
-        block_sum_all<N>(acc);
-        if (threadIdx.x == 0) {
-#pragma unroll
-            for (int k = 0; k < N; ++k) d->tot[k] = acc[k];
-            atomicExch(&d->bar_count, 0u);
-            __threadfence();
-            atomicAdd(&d->bar_gen, 1u);
-        }
-#pragma unroll
-        for (int k = 0; k < N; ++k) v[k] = acc[k];
-        return true;
-    }
+    ++epoch;
     if (!ok) return false;
 #pragma unroll
-    for (int k = 0; k < N; ++k) v[k] = ldcg(d->tot + k);
+    for (int k = 0; k < N; ++k) v[k] = res[k];
     return true;
 }
 
@@ -316,9 +312,10 @@ __device__ __forceinline__ double apply_phase(const PcgArgs<VT, XT, PT>& a, bool
 }
 
 template <typename VT, typename XT, typename PT>
-__global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_solve(PcgArgs<VT, XT, PT> a)
+__global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_solve(PcgArgs<VT, XT, PT> a)
 {
     PcgScalars* d = a.d;
+    unsigned int epoch = 0;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     // r = b, x = 0, q_c = 0, z = M^-1 r
     double tot[2];
@@ -341,7 +338,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_solve(PcgArgs<VT, XT, PT
                 v[1] += (double)r[c] * (double)r[c];
             }
         }
-        if (!grid_allreduce<2>(v, a.part_b, d)) return;
+        if (!grid_allreduce<2>(v, d, epoch)) return;
         tot[0] = v[0];
         tot[1] = v[1];
     }
@@ -370,7 +367,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_solve(PcgArgs<VT, XT, PT
         const XT* pold = (k & 1) ? a.P0 : a.P1;
         double va[1] = {apply_phase<VT, XT, PT>(a, first, beta, pk, pold)};
         lap(0);
-        if (!grid_allreduce<1>(va, a.part_a, d)) return;
+        if (!grid_allreduce<1>(va, d, epoch)) return;
         lap(1);
         pq = va[0];
         if (!(pq > 0 && pq < INFINITY)) {
@@ -398,7 +395,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_solve(PcgArgs<VT, XT, PT
             }
         }
         lap(3);
-        if (!grid_allreduce<2>(vb, a.part_b, d)) return;
+        if (!grid_allreduce<2>(vb, d, epoch)) return;
         lap(4);
         tot[0] = vb[0];
         tot[1] = vb[1];
@@ -428,7 +425,6 @@ constexpr int kVecs = 8;  // r, z, P0, P1, q_e, q_c, and b, x of the FP32 inner 
 
 struct PcgState {
     DBuf<char> vec;              // kVecs vectors of 3 nv entries
-    DBuf<double> part;           // 3 partials per block
     DBuf<PcgScalars> dsc;        // device scalars
     PcgScalars* host = nullptr;  // pinned copy of the results
     int grid[2] = {0, 0};        // co-resident grid per precision (0 FP64, 1 FP32)
@@ -436,7 +432,6 @@ struct PcgState {
     {
         if (host) cudaFreeHost(host);
         vec.release();
-        part.release();
         dsc.release();
     }
 };
@@ -447,8 +442,14 @@ int coresident_grid(int nv)
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_solve<VT, XT, PT>, kPcgThreads, 0);
     if (e != cudaSuccess || per_sm < 1) return 0;
-    // every co-resident block: the apply phase has one work item per scalar row
-    // plus one per contact and friction constraint, so there is rarely spare room
+    // CIPC_PCG_BLOCKS_PER_SM (1..occupancy) trades apply-phase parallelism against
+    // the cost of the grid reductions, which grows with the number of blocks
+    if (const char* env = std::getenv("CIPC_PCG_BLOCKS_PER_SM")) {
+        const int b = std::atoi(env);
+        if (b >= 1 && b < per_sm) per_sm = b;
+    }
+    // the apply phase has one work item per scalar row plus one per contact and
+    // friction constraint, so every co-resident block has work
     (void)nv;
     return per_sm * num_sms();
 }
@@ -464,10 +465,9 @@ int state(Sim* s, PcgState** out)
         }
         st->grid[0] = coresident_grid<double, double, double>(s->nv);
         st->grid[1] = coresident_grid<float, float, float>(s->nv);
-        const int g = std::max(st->grid[0], st->grid[1]);
-        if (g < 1 || st->part.alloc(3 * (size_t)g) != cudaSuccess) {
+        if (std::min(st->grid[0], st->grid[1]) < 1) {
             delete st;
-            return set_error(CIPC_ERR_CUDA, "PCG: no co-resident grid or partials allocation failed");
+            return set_error(CIPC_ERR_CUDA, "PCG: no co-resident grid");
         }
         s->pcg = st;
     }
@@ -520,8 +520,6 @@ int solve(Sim* s, const XT* b, XT* x, double tol, int maxit, int* iters, double*
     a.P1 = vecp(3);
     a.qe = vecp(4);
     a.qc = vecp(5);
-    a.part_a = st->part.p;
-    a.part_b = st->part.p + g;
     a.d = st->dsc.p;
     a.tol = tol;
     a.maxit = maxit;

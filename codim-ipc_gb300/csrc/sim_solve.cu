@@ -256,11 +256,12 @@ static void build_precond(Sim* s)
 static int solve_with_precond(Sim* s, const double* rhs, double* sol, int* iters)
 {
     const int n3 = 3 * s->nv;
+    const double tol = s->solve_tol > 0 ? s->solve_tol : s->prm.pcg_tol;
     int total = 0;
     double rel = 0;
     int rc = CIPC_OK;
     if (s->prm.precision != 1) {
-        rc = pcg_solve_fp64(s, rhs, sol, s->prm.pcg_tol, s->prm.pcg_maxit, &total, &rel);
+        rc = pcg_solve_fp64(s, rhs, sol, tol, s->prm.pcg_maxit, &total, &rel);
     } else {
         // mixed: FP32 inner PCG, FP64 iterative refinement of the residual
         const size_t need = (size_t)n3 * 2 * sizeof(double) + 4096 * sizeof(double) + (1 << 16);
@@ -301,7 +302,7 @@ static int solve_with_precond(Sim* s, const double* rhs, double* sol, int* iters
         double rr = bb;
         for (int outer = 0; outer < 20 && bb > 0; ++outer) {
             const double rn = std::sqrt(rr);
-            const double inner_tol = std::min(0.5, std::max(0.5 * s->prm.pcg_tol * std::sqrt(bb / rr), 1e-5));
+            const double inner_tol = std::min(0.5, std::max(0.5 * tol * std::sqrt(bb / rr), 1e-5));
             k_convert_scaled<<<nblk(n3, 256), 256, 0, s->stream>>>(n3, r64, 1.0 / rn, b32);
             double relin = 0;
             int it = 0;
@@ -318,9 +319,9 @@ static int solve_with_precond(Sim* s, const double* rhs, double* sol, int* iters
             rel = std::sqrt(rr / bb);
             if (s->trace)
                 std::fprintf(stderr, "cipc refine %d: inner %.3e outer %.3e pcg %d\n", outer, relin, rel, total);
-            if (rel <= s->prm.pcg_tol || total >= s->prm.pcg_maxit) break;
+            if (rel <= tol || total >= s->prm.pcg_maxit) break;
         }
-        rc = rel <= s->prm.pcg_tol ? CIPC_OK : set_error(CIPC_ERR_NOT_CONVERGED, "PCG stopped at relative residual %g", rel);
+        rc = rel <= tol ? CIPC_OK : set_error(CIPC_ERR_NOT_CONVERGED, "PCG stopped at relative residual %g", rel);
     }
     if (iters) *iters = total;
     cudaError_t e = cudaStreamSynchronize(s->stream);

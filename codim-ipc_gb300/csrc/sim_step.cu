@@ -251,6 +251,12 @@ int sim_step(Sim* s, StepStats* st)
     int fricIterI = 0, it = 0;
     bool useGD = false;
     double L2 = 0;
+    // inexact Newton: Eisenstat-Walker forcing term, choice 2 (gamma 0.9, alpha 2)
+    // with its safeguard, clamped to [pcg_tol, 0.1]; full accuracy once the last
+    // step was within 10x of the Newton tolerance, so the stopping test (and the
+    // friction re-solve below) always sees a direction solved to pcg_tol
+    double gnorm_prev = -1, eta_prev = 0.1;
+    s->solve_tol = 0;
     do {
         if (it >= P.maxIter) {
             S.status = -1;
@@ -263,8 +269,23 @@ int sim_step(Sim* s, StepStats* st)
         if (useGD) {
             cudaMemcpyAsync(s->dir.p, s->rhs.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
         } else {
+            if (P.forcing) {
+                const double gn = std::sqrt(sum_sq(s, s->rhs.p, n3));
+                double eta = 0.1;
+                if (gnorm_prev > 0) {
+                    eta = 0.9 * (gn / gnorm_prev) * (gn / gnorm_prev);
+                    const double safe = 0.9 * eta_prev * eta_prev;
+                    if (safe > 0.1) eta = std::max(eta, safe);
+                }
+                eta = std::min(0.1, std::max(P.pcg_tol, eta));
+                if (!res.empty() && res.back() < 10 * P.tol) eta = P.pcg_tol;
+                gnorm_prev = gn;
+                eta_prev = eta;
+                s->solve_tol = eta;
+            }
             int pit = 0;
             const int lr = linear_solve(s, s->rhs.p, s->dir.p, &pit);
+            s->solve_tol = 0;
             S.pcg_iters += pit;
             if (lr == CIPC_ERR_NAN) {
                 useGD = true;
@@ -579,6 +600,7 @@ static void to_params(const cipc_step_params* p, SimParams& q)
     q.pcg_tol = p->pcg_tol > 0 ? p->pcg_tol : 1e-6;
     q.pcg_maxit = p->pcg_max_iters > 0 ? p->pcg_max_iters : 10000;
     q.precond = p->preconditioner;
+    q.forcing = p->forcing;
 }
 
 extern "C" int cipc_sim_step(cipc_sim* h, const cipc_step_params* p, cipc_step_stats* stats)

@@ -155,6 +155,9 @@ typedef struct cipc_step_params {
     double pcg_tol;        /* relative residual of each Newton system (0 = 1e-6) */
     int pcg_max_iters;     /* 0 = 10000 */
     int preconditioner;    /* 0 block-Jacobi, 1 learned correction when a model is set */
+    int forcing;           /* 0: every Newton system to pcg_tol; 1: inexact Newton, the
+                              Eisenstat-Walker forcing term (choice 2, gamma 0.9, alpha 2)
+                              clamped to [pcg_tol, 0.1], pcg_tol once RMS(step)/h < 10 tol */
 } cipc_step_params;
 
 typedef struct cipc_step_stats {
