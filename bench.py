@@ -10,6 +10,13 @@ device-resident inputs; `e2e` runs the same pass through the C ABI with pinned
 host buffers (copies in the timed region).  The FP64 kernel and the barrier
 (energy/gradient/PSD Hessian) pass are reported under "variants".
 
+Also reported (single GPU): "timestep", ms/timestep of the 200x200 cloth on the
+rotating sphere for plain FP64 block-Jacobi PCG, FP32 Hessians with FP64
+refinement, the learned block-Jacobi correction, and each with inexact-Newton
+forcing; "scenes", absolute steps/s of the cloth-on-cube (with the CPU oracle
+on the same steps), mixed codimensional (rods + particles + cloth) and stacked
+shell scenes.
+
   python bench.py [--gpus N --steps K --warmup W] [--impl ours|reference]
 
 Multi-GPU: each rank runs its own replica with its own seed (weak scaling, no
@@ -178,11 +185,11 @@ def timestep_variants(args):
     def target(k):
         return workloads.rotate_y(X[dbc], c, omega * dt * (k + 1))
 
-    def make(prec, pre):
+    def make(prec, pre, forcing=0):
         s = F.Sim(X, T, 200.0, 1e5, 0.3, 1e-3)
         _, dhat2 = s.init_oipc(1e-3)
         prm = F.make_params(dt, dhat2, 5e-4, mu=0.4, epsv2=1e-6, fric_iters=1, newton_tol=1e-3, precision=prec,
-                            pcg_tol=1e-4, preconditioner=pre)
+                            pcg_tol=1e-4, preconditioner=pre, forcing=forcing)
         return s, prm
 
     ok = (F.CIPC_ERR_NOT_CONVERGED,)
@@ -206,9 +213,11 @@ def timestep_variants(args):
            "unit": "ms/timestep", "newton_tol": 1e-3, "pcg_tol": 1e-4,
            "learned": {"systems": pc.num_systems(), "epochs": args.ts_epochs, "train_s": round(train_s, 2),
                        "loss_before": round(loss_before, 4), "loss_after": round(loss_after, 4)}}
-    for name, prec, pre in (("fp64_block_jacobi", F.FP64, 0), ("mixed_block_jacobi", F.MIXED, 0),
-                            ("mixed_learned", F.MIXED, 1)):
-        sv, pv = make(prec, pre)
+    variants = (("fp64_block_jacobi", F.FP64, 0, 0), ("mixed_block_jacobi", F.MIXED, 0, 0),
+                ("mixed_learned", F.MIXED, 1, 0), ("fp64_block_jacobi_inexact", F.FP64, 0, 1),
+                ("mixed_block_jacobi_inexact", F.MIXED, 0, 1), ("mixed_learned_inexact", F.MIXED, 1, 1))
+    for name, prec, pre, forcing in variants:
+        sv, pv = make(prec, pre, forcing)
         if pre:
             F.sim_set_precond(sv, pc)
         sv.set_state(x0, v0)
@@ -230,7 +239,112 @@ def timestep_variants(args):
                                                  / out["mixed_learned"]["ms_per_step"], 3)
     out["speedup_mixed_vs_fp64"] = round(out["fp64_block_jacobi"]["ms_per_step"]
                                          / out["mixed_block_jacobi"]["ms_per_step"], 3)
+    out["speedup_mixed_learned_inexact_vs_fp64"] = round(out["fp64_block_jacobi"]["ms_per_step"]
+                                                         / out["mixed_learned_inexact"]["ms_per_step"], 3)
+    out["speedup_mixed_inexact_vs_fp64"] = round(out["fp64_block_jacobi"]["ms_per_step"]
+                                                 / out["mixed_block_jacobi_inexact"]["ms_per_step"], 3)
+    out["note"] = ("*_inexact: Eisenstat-Walker forcing term for the Newton systems (cipc_step_params.forcing = 1); "
+                   "the Newton tolerance is the same for every variant")
     pc.close()
+    return out
+
+
+def _scene_stats(rows):
+    ms = [r["ms"] for r in rows]
+    con = [r for r in rows if r["n_constraints"] > 0]
+    return {"steps": len(rows), "ms_per_step": round(float(np.mean(ms)), 2),
+            "steps_per_s": round(1000.0 / float(np.mean(ms)), 3),
+            "newton_per_step": round(float(np.mean([r["newton_iters"] for r in rows])), 2),
+            "pcg_per_step": round(float(np.mean([r["pcg_iters"] for r in rows])), 1),
+            "constraints_max": int(max(r["n_constraints"] for r in rows)),
+            "min_dist2_min": float(min(r["min_dist2"] for r in con)) if con else None,
+            "intersection_free": bool(all(r["min_dist2"] > 0 for r in con)),
+            "status": sorted(set(int(r["status"]) for r in rows))}
+
+
+def scene_runs(args):
+    """Absolute steps/s of the other named scenes, each from its initial state:
+    the 40x40 cloth falling on a fixed 0.3 m cube (StVK, 50 steps, dt 0.04, Newton
+    tol 1e-2; FP64 and mixed, and the CPU oracle on its first steps), the mixed
+    codimensional scene (1000 rods x 100 segments, 20000 particles, 120x120 cloth
+    pinned at its corners; dt 0.01, mu 0.2) and the 8-layer stacked shells
+    (8 x 180x180 cloths between a fixed and a descending plate at 0.05 m/s;
+    dt 0.01, mu 0.3, xi = dhat = 0.5 mm)."""
+    import cipc_ffi as F
+    import workloads
+
+    ok = (F.CIPC_ERR_NOT_CONVERGED,)
+
+    def run(sim, prm, dbc, tgt, steps):
+        rows = []
+        for k in range(steps):
+            sim.set_dbc(dbc, tgt(k))
+            rows.append(sim.step(prm, allow=ok).as_dict())
+        return rows
+
+    out = {"precond": "block Jacobi", "pcg_tol": 1e-4}
+    # cloth on cube
+    X, T, dbc = workloads.cloth_on_box(n=40)
+    c1 = {"workload": "40x40 cloth (1 m, StVK E 1e5, t 1 mm) falling 0.1 m onto a fixed 0.3 m cube, dt 0.04, "
+                      "xi = dhat = 1 mm, Newton tol 1e-2, %d vertices incl. the cube" % X.shape[0]}
+    for name, prec in (("fp64", F.FP64), ("mixed", F.MIXED)):
+        s = F.Sim(X, T, 200.0, 1e5, 0.3, 1e-3, nh=False)
+        _, dhat2 = s.init_oipc(1e-3)
+        prm = F.make_params(0.04, dhat2, 1e-3, newton_tol=1e-2, precision=prec, pcg_tol=1e-4)
+        rows = run(s, prm, dbc, lambda k: X[dbc], args.c1_steps)
+        s.close()
+        c1[name] = _scene_stats(rows)
+        c1[name]["first_%d_ms_per_step" % args.c1_cpu_steps] = round(
+            float(np.mean([r["ms"] for r in rows[:args.c1_cpu_steps]])), 2)
+    if not args.no_cpu_baseline and args.c1_cpu_steps > 0:
+        from oracle import oracle_ffi as orc
+        sh = orc.Shell(X, T, 200.0, 1e5, 0.3, 1e-3, nh=False)
+        k2, dhat2 = sh.init_oipc(1e-3)
+        x, v = X.copy(), np.zeros_like(X)
+        t0 = time.perf_counter()
+        newton = []
+        for _ in range(args.c1_cpu_steps):
+            rc, st = sh.step(x, v, k2, dbc, X[dbc], 0.04, dhat2, 1e-3, tol=1e-2)
+            newton.append(st["newton_iters"])
+        cpu_ms = (time.perf_counter() - t0) * 1e3 / args.c1_cpu_steps
+        c1["cpu_oracle"] = {"kind": "port", "cores": orc.num_threads(), "ms_per_step": round(cpu_ms, 1),
+                            "newton_per_step": round(float(np.mean(newton)), 2),
+                            "sample": "first %d steps, direct (skyline LDL^T) Newton solves" % args.c1_cpu_steps}
+        c1["speedup_mixed_vs_cpu_oracle"] = round(cpu_ms / c1["mixed"]["first_%d_ms_per_step" % args.c1_cpu_steps], 1)
+    out["cloth_on_cube_40"] = c1
+    # mixed codimensional scene
+    X, T, S, P, corners = workloads.rods_particles_on_cloth_full()
+    codim = dict(segments=S, rod_E=1e7, rod_rho=1000.0, rod_thickness=1e-3, particles=P, particle_rho=1000.0,
+                 particle_thickness=4e-3)
+    s = F.Sim(X, T, 200.0, 1e5, 0.3, 1e-3, codim=codim)
+    _, dhat2 = s.init_oipc(1e-3)
+    prm = F.make_params(0.01, dhat2, 1e-3, mu=0.2, epsv2=1e-6, fric_iters=1, newton_tol=1e-2, precision=F.MIXED,
+                        pcg_tol=1e-4)
+    rows = run(s, prm, corners, lambda k: X[corners], args.sc_steps)
+    s.close()
+    out["rods_particles_on_cloth"] = dict(
+        workload="1000 rods x 100 segments (0.5 m, E 1e7, 5 layers of 200 with seeded directions), 20000 particles "
+                 "(4 mm), 120x120 cloth pinned at its corners; %d vertices; dt 0.01, xi = dhat = 1 mm, mu 0.2; "
+                 "first %d steps, mixed precision" % (X.shape[0], args.sc_steps), **_scene_stats(rows))
+    # stacked shells
+    X, T, dbc, top = workloads.stacked_shells()
+    s = F.Sim(X, T, 200.0, 1e5, 0.3, 1e-3)
+    _, dhat2 = s.init_oipc(5e-4)
+    prm = F.make_params(0.01, dhat2, 5e-4, mu=0.3, epsv2=1e-6, fric_iters=1, newton_tol=1e-2, precision=F.MIXED,
+                        pcg_tol=1e-4)
+    istop = np.isin(dbc, top)
+
+    def plate(k):
+        Y = X[dbc].copy()
+        Y[istop, 1] -= 0.05 * 0.01 * (k + 1)
+        return Y
+
+    rows = run(s, prm, dbc, plate, args.sc_steps)
+    s.close()
+    out["stacked_shells_8x180"] = dict(
+        workload="8 layers of 180x180 cloth (1 m, 5 mm apart, 1 mm seeded in-plane jitter) between a fixed plate and "
+                 "a plate descending at 0.05 m/s; %d vertices; dt 0.01, xi = dhat = 0.5 mm, mu 0.3; first %d steps, "
+                 "mixed precision" % (X.shape[0], args.sc_steps), **_scene_stats(rows))
     return out
 
 
@@ -377,6 +491,8 @@ def run_ours(args):
         }
         if ws == 1 and not args.no_timestep:
             line["timestep"] = timestep_variants(args)
+        if ws == 1 and not args.no_scenes:
+            line["scenes"] = scene_runs(args)
         print(json.dumps(line))
     if ws > 1:
         dist.barrier()
@@ -398,6 +514,10 @@ def main():
     ap.add_argument("--ts-warm", type=int, default=10, help="draping steps before the measured steps")
     ap.add_argument("--ts-steps", type=int, default=6, help="measured steps per variant")
     ap.add_argument("--ts-epochs", type=int, default=20, help="training epochs of the learned correction")
+    ap.add_argument("--no-scenes", action="store_true", help="skip the cube / codimensional / stacked-shell scenes")
+    ap.add_argument("--c1-steps", type=int, default=50, help="steps of the cloth-on-cube scene")
+    ap.add_argument("--c1-cpu-steps", type=int, default=8, help="cloth-on-cube steps run by the CPU oracle")
+    ap.add_argument("--sc-steps", type=int, default=6, help="steps of the codimensional and stacked scenes")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -97,8 +97,9 @@ struct PcgArgs {
     int trace;
 };
 
-// 256-thread blocks, 4 per SM: a grid-wide reduction costs ~5-7 us here against
-// ~9 us with one 1024-thread block per SM (block-level sums dominate)
+// 256-thread blocks: a grid-wide reduction costs ~2.5 us with 152 blocks, ~3.7
+// with 304 and ~6 with 608 (arrivals on one counter), against ~3.5 / ~5 with
+// 512-thread blocks (the block-level sum grows)
 constexpr int kPcgThreads = 256;
 // polls of the arrival counter before a wait gives up: each poll is an L2 round
 // trip (>= ~0.3 us), and past kBarrierBackoff polls a 64 ns sleep is added, so the
@@ -200,43 +201,44 @@ __device__ __forceinline__ void precond_vertex(const PT* __restrict__ pinv, int 
     z[2] = (XT)__ldg(P + 6) * r[0] + (XT)__ldg(P + 7) * r[1] + (XT)__ldg(P + 8) * r[2];
 }
 
-// y = H_c x_c for one contact constraint of NV vertices (packed upper triangle,
-// row by row, entry h at H[h * hs]: consecutive constraints are adjacent, so a
-// warp's loads of one entry are coalesced), accumulated into q; returns x_c . y
+// y = H_c x_c for one contact constraint of NV vertices by a group of 4 lanes
+// (lane k of the group owns vertex k; lanes k >= NV only pass values along).
+// The packed upper triangle is stored row by row, entry h at H[h * hs], so
+// consecutive constraints are adjacent and loads of one entry by several groups
+// share cache lines.  Each owning lane gathers its vertex's 3 values, the group
+// exchanges them by shuffles, and the lane forms its 3 rows of H_c x_c and adds
+// them into q; returns the lane's share of x_c . H_c x_c.  All 4 lanes of the
+// group must call this together (gmask = the group's lanes, gbase = its first).
 template <int NV, typename VT, typename XT, typename G>
-__device__ __forceinline__ double con_apply(const VT* __restrict__ H, size_t hs, int4 iv, const G& pget, XT* q)
+__device__ __forceinline__ double con_apply_lane(const VT* __restrict__ H, size_t hs, int4 iv, int k, unsigned gmask,
+                                                 int gbase, const G& pget, XT* q)
 {
     constexpr int M = 3 * NV;
-    const int id[4] = {iv.x, iv.y, iv.z, iv.w};
-    XT xs[M], ys[M];
+    const bool own = k < NV;
+    const int me = k == 0 ? iv.x : (k == 1 ? iv.y : (k == 2 ? iv.z : iv.w));
+    XT xk[3];
 #pragma unroll
-    for (int k = 0; k < NV; ++k)
+    for (int t = 0; t < 3; ++t) xk[t] = own ? pget(3 * me + t) : XT(0);
+    XT xs[M];
 #pragma unroll
-        for (int t = 0; t < 3; ++t) {
-            xs[3 * k + t] = pget(3 * id[k] + t);
-            ys[3 * k + t] = 0;
-        }
-    int h = 0;
+    for (int j = 0; j < NV; ++j)
 #pragma unroll
-    for (int p = 0; p < M; ++p) {
-        ys[p] += (XT)__ldg(H + h * hs) * xs[p];
-        ++h;
-#pragma unroll
-        for (int k = p + 1; k < M; ++k, ++h) {
-            const XT hv = (XT)__ldg(H + h * hs);
-            ys[p] += hv * xs[k];
-            ys[k] += hv * xs[p];
-        }
-    }
+        for (int t = 0; t < 3; ++t) xs[3 * j + t] = __shfl_sync(gmask, xk[t], gbase + j);
+    if (!own) return 0.0;
     double s = 0;
 #pragma unroll
-    for (int k = 0; k < NV; ++k)
+    for (int r = 0; r < 3; ++r) {
+        const int p = 3 * k + r;
+        XT y = 0;
 #pragma unroll
-        for (int t = 0; t < 3; ++t) {
-            const XT y = ys[3 * k + t];
-            s += (double)xs[3 * k + t] * (double)y;
-            if (y != XT(0)) atomicAdd(q + 3 * id[k] + t, y);
+        for (int m = 0; m < M; ++m) {
+            const int i = min(p, m), j = max(p, m);
+            const int h = i * M - (i * (i - 1)) / 2 + (j - i);
+            y += (XT)__ldg(H + (size_t)h * hs) * xs[m];
         }
+        s += (double)xk[r] * (double)y;
+        if (y != XT(0)) atomicAdd(q + 3 * me + r, y);
+    }
     return s;
 }
 
@@ -248,8 +250,12 @@ __device__ __forceinline__ double apply_phase(const PcgArgs<VT, XT, PT>& a, bool
 {
     const XT* z = a.z;
     auto pget = [&](int j) -> XT { return first ? ldcg(z + j) : ldcg(z + j) + beta * ldcg(pold + j); };
+    // work items: elastic scalar rows, then 4 lanes per contact constraint
+    // (starting 4-aligned, so a constraint's lanes are 4 aligned lanes of one warp:
+    // the grid stride is a multiple of 32), then friction constraints
     const int nrow = 3 * a.nv, ncon = a.ncon, nfric = a.nfric;
-    const int total = nrow + ncon + nfric;
+    const int cbeg = (nrow + 3) & ~3, cend = cbeg + 4 * ncon;
+    const int total = cend + nfric;
     double v = 0;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < total; w += gridDim.x * blockDim.x) {
         if (w < nrow) {
@@ -269,18 +275,22 @@ __device__ __forceinline__ double apply_phase(const PcgArgs<VT, XT, PT>& a, bool
             pk[w] = pw;
             a.qe[w] = acc;
             v += (double)pw * (double)acc;
-        } else if (w < nrow + ncon) {
-            // contact constraint: packed upper triangle of its (3nv x 3nv) block
-            const int c = w - nrow;
+        } else if (w < cbeg) {
+            continue;
+        } else if (w < cend) {
+            // contact constraint c, lane k of its group of 4
+            const int c = (w - cbeg) >> 2, k = (w - cbeg) & 3;
+            const int lane = threadIdx.x & 31, gbase = lane & ~3;
+            const unsigned gmask = 0xFu << gbase;
             const int cnv = con_nv(__ldg(a.ckind + c));
             const int4 iv = a.cverts[c];
             const VT* H = a.chess + c;
-            if (cnv == 2) v += con_apply<2>(H, a.hs, iv, pget, a.qc);
-            else if (cnv == 3) v += con_apply<3>(H, a.hs, iv, pget, a.qc);
-            else v += con_apply<4>(H, a.hs, iv, pget, a.qc);
+            if (cnv == 2) v += con_apply_lane<2>(H, a.hs, iv, k, gmask, gbase, pget, a.qc);
+            else if (cnv == 3) v += con_apply_lane<3>(H, a.hs, iv, k, gmask, gbase, pget, a.qc);
+            else v += con_apply_lane<4>(H, a.hs, iv, k, gmask, gbase, pget, a.qc);
         } else {
             // friction constraint: w_a T M T^T sum_b w_b p_b over non-projected vertices
-            const int c = w - nrow - ncon;
+            const int c = w - cend;
             if (a.fkind[c] >= kc_EEM) continue;
             const int cnv = con_nv(a.fkind[c]);
             const int4 iv = a.fverts[c];
@@ -312,7 +322,7 @@ __device__ __forceinline__ double apply_phase(const PcgArgs<VT, XT, PT>& a, bool
 }
 
 template <typename VT, typename XT, typename PT>
-__global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_solve(PcgArgs<VT, XT, PT> a)
+__global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_solve(PcgArgs<VT, XT, PT> a)
 {
     PcgScalars* d = a.d;
     unsigned int epoch = 0;
@@ -442,12 +452,16 @@ int coresident_grid(int nv)
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_solve<VT, XT, PT>, kPcgThreads, 0);
     if (e != cudaSuccess || per_sm < 1) return 0;
-    // CIPC_PCG_BLOCKS_PER_SM (1..occupancy) trades apply-phase parallelism against
-    // the cost of the grid reductions, which grows with the number of blocks
+    // blocks per SM trade apply-phase parallelism against the cost of the grid
+    // reductions, which grows with the number of blocks: two per SM measured best
+    // on the 200x200 cloth (FP32: 26 us per iteration against 30 with four and 35
+    // with one); CIPC_PCG_BLOCKS_PER_SM (1..occupancy) overrides
+    int want = 2;
     if (const char* env = std::getenv("CIPC_PCG_BLOCKS_PER_SM")) {
         const int b = std::atoi(env);
-        if (b >= 1 && b < per_sm) per_sm = b;
+        if (b >= 1) want = b;
     }
+    per_sm = std::min(per_sm, want);
     // the apply phase has one work item per scalar row plus one per contact and
     // friction constraint, so every co-resident block has work
     (void)nv;

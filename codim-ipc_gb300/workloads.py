@@ -242,12 +242,15 @@ def merge_meshes(*meshes):
 
 
 def rods_particles_on_cloth(n_rods=1000, seg_per_rod=100, rod_len=0.5, n_particles=20000, cloth_n=120,
-                            cloth_size=1.0, layer_gap=2.5e-3, particle_gap=8e-3, lift=0.02, seed=0):
+                            cloth_size=1.0, layer_gap=2.5e-3, particle_gap=8e-3, lift=0.02, seed=0,
+                            rods_per_layer=1, rod_spacing=5e-3, particles_per_row=None):
     """Mixed codimensional scene: straight rods of `seg_per_rod` segments and length
-    `rod_len`, each horizontal at its own height (layer_gap apart, so no two
-    overlap) with a seeded random in-plane direction and centre over the cloth;
-    particles on a grid (particle_gap apart) above the rods; a cloth_n x cloth_n
-    cloth (cloth_size square, y = 0) pinned at its four corners.
+    `rod_len` in horizontal layers `layer_gap` apart, `rods_per_layer` parallel rods
+    `rod_spacing` apart in a layer, each layer with a seeded random in-plane
+    direction and (single-rod layers) a seeded random centre over the cloth;
+    particles on a grid (`particle_gap` apart, `particles_per_row` per row, default
+    a tall column) above the rods; a cloth_n x cloth_n cloth (cloth_size square,
+    y = 0) pinned at its four corners.
 
     Returns X, T (cloth triangles), segments (n_rods*seg_per_rod, 2),
     particles (indices), dbc (the 4 cloth corners)."""
@@ -259,18 +262,32 @@ def rods_particles_on_cloth(n_rods=1000, seg_per_rod=100, rod_len=0.5, n_particl
     segs = []
     o = nc
     half = 0.5 * (cloth_size - rod_len) * 0.9
-    for r in range(n_rods):
+    n_layers = (n_rods + rods_per_layer - 1) // rods_per_layer
+    t = np.linspace(-0.5, 0.5, seg_per_rod + 1)[:, None] * rod_len
+    r = 0
+    for layer in range(n_layers):
         th = rng.uniform(0, 2 * np.pi)
-        c = np.array([rng.uniform(-half, half), lift + r * layer_gap, rng.uniform(-half, half)])
         d = np.array([np.cos(th), 0.0, np.sin(th)])
-        t = np.linspace(-0.5, 0.5, seg_per_rod + 1)[:, None] * rod_len
-        pts.append(c[None, :] + t * d[None, :])
-        segs.append(np.column_stack([np.arange(seg_per_rod), np.arange(1, seg_per_rod + 1)]) + o)
-        o += seg_per_rod + 1
-    top = lift + n_rods * layer_gap + particle_gap
-    side = int(np.ceil(np.sqrt(max(n_particles, 1) / 50.0)))
-    nx = max(1, min(side, int(cloth_size * 0.8 / particle_gap)))
-    ny = int(np.ceil(n_particles / (nx * nx))) if n_particles else 0
+        nrm = np.array([-d[2], 0.0, d[0]])
+        y = lift + layer * layer_gap
+        if rods_per_layer == 1:
+            centres = [np.array([rng.uniform(-half, half), y, rng.uniform(-half, half)])]
+        else:
+            k = min(rods_per_layer, n_rods - r)
+            off = (np.arange(k) - (k - 1) / 2) * rod_spacing
+            shift = rng.uniform(-0.25, 0.25) * rod_spacing
+            centres = [np.array([0.0, y, 0.0]) + (q + shift) * nrm for q in off]
+        for c in centres:
+            pts.append(c[None, :] + t * d[None, :])
+            segs.append(np.column_stack([np.arange(seg_per_rod), np.arange(1, seg_per_rod + 1)]) + o)
+            o += seg_per_rod + 1
+            r += 1
+    top = lift + n_layers * layer_gap + particle_gap
+    if particles_per_row is None:
+        side = int(np.ceil(np.sqrt(max(n_particles, 1) / 50.0)))
+        nx = max(1, min(side, int(cloth_size * 0.8 / particle_gap)))
+    else:
+        nx = int(particles_per_row)
     P = []
     for k in range(n_particles):
         i, j, l = k % nx, (k // nx) % nx, k // (nx * nx)
@@ -281,3 +298,39 @@ def rods_particles_on_cloth(n_rods=1000, seg_per_rod=100, rod_len=0.5, n_particl
     X = np.concatenate(pts)
     S = np.concatenate(segs).astype(np.int32) if segs else np.zeros((0, 2), np.int32)
     return X, Tc.astype(np.int32), S, particles, corners
+
+
+def rods_particles_on_cloth_full(seed=0):
+    """The mixed codimensional scene at full size: 1000 rods x 100 segments (0.5 m)
+    in 5 layers of 200 parallel rods 5 mm apart (seeded layer directions), 20000
+    particles in two 100 x 100 layers 8 mm apart, on a 120 x 120 cloth (1 m)
+    pinned at its corners; 135,400 vertices."""
+    return rods_particles_on_cloth(n_rods=1000, seg_per_rod=100, rod_len=0.5, n_particles=20000, cloth_n=120,
+                                   cloth_size=1.0, layer_gap=5e-3, particle_gap=8e-3, lift=5e-3, seed=seed,
+                                   rods_per_layer=200, rod_spacing=5e-3, particles_per_row=100)
+
+
+def stacked_shells(n=180, layers=8, size=1.0, gap=5e-3, jitter=1e-3, plate_n=21, plate_margin=0.1, seed=0):
+    """`layers` cloths of n x n vertices (size x size) stacked `gap` apart, every
+    vertex moved in-plane by a seeded uniform jitter in [-jitter, jitter] (rest
+    shape = jittered shape), between a fixed ground plate `gap` below the lowest
+    layer and a top plate `gap` above the highest (plates: plate_n x plate_n
+    grids, `plate_margin` wider than the cloth on each side, Dirichlet).
+
+    Returns X, T, dbc (all plate vertices), top (the top plate's vertices, which
+    the scene moves down)."""
+    rng = np.random.default_rng(seed)
+    meshes = []
+    for l in range(layers):
+        Xl, Tl = cloth_grid(n, n, size, size, y=l * gap, origin=(-size / 2, -size / 2))
+        J = rng.uniform(-jitter, jitter, size=(Xl.shape[0], 2))
+        Xl[:, 0] += J[:, 0]
+        Xl[:, 2] += J[:, 1]
+        meshes.append((Xl, Tl))
+    ps = size + 2 * plate_margin
+    meshes.append(cloth_grid(plate_n, plate_n, ps, ps, y=-gap, origin=(-ps / 2, -ps / 2)))
+    meshes.append(cloth_grid(plate_n, plate_n, ps, ps, y=layers * gap, origin=(-ps / 2, -ps / 2)))
+    X, T, offs = merge_meshes(*meshes)
+    dbc = np.arange(offs[layers], X.shape[0], dtype=np.int32)
+    top = np.arange(offs[layers + 1], X.shape[0], dtype=np.int32)
+    return X, T, dbc, top
