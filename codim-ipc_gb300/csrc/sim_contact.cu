@@ -36,6 +36,11 @@ __global__ void k_set_u64(unsigned long long* p, unsigned long long v) { *p = v;
 
 // internal status: the scratch buffer was too small; Sim::scratch_bytes holds the need
 static const int kNeedScratch = 1000;
+// a grid would hold more than kMaxGridEntries (item, cell) entries: boxes swept by
+// an enormous step (the step-size search then halves its trial step) or
+// primitives far larger than the cells
+static const int kSpanTooLarge = 1001;
+static const unsigned long long kMaxGridEntries = 1ull << 27;
 
 // ---------------------------------------------------------------------------
 // exclusive scan of int counts (three-phase block scan, recursive over blocks)
@@ -108,12 +113,15 @@ struct ItemArgs {
     int* lo;
     int* hi;
     int* count;
+    unsigned long long* total;  // sum over items of the uncapped cell counts
 };
 
-__global__ void k_item_cells(ItemArgs a)
+__global__ void __launch_bounds__(256) k_item_cells(ItemArgs a)
 {
+    __shared__ unsigned long long part[8];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.n) return;
+    unsigned long long want = 0;
+    if (t < a.n) {
     double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
     for (int k = 0; k < a.nvi; ++k) {
         const int v = a.verts[a.nvi * t + k];
@@ -133,9 +141,20 @@ __global__ void k_item_cells(ItemArgs a)
         const int l = cellc(mn[d], a.inv), h = cellc(mx[d], a.inv);
         a.lo[3 * t + d] = l;
         a.hi[3 * t + d] = h;
-        c *= (long long)(h - l + 1);
+        c = min(c * max((long long)h - (long long)l + 1, 1ll), (long long)kMaxGridEntries + 1);
     }
     a.count[t] = (int)min(c, (long long)(1 << 28));
+    want = (unsigned long long)c;
+    }
+    // block sum, one atomic per block (each term <= 2^27 + 1, so no overflow)
+    for (int o = 16; o > 0; o >>= 1) want += __shfl_down_sync(0xffffffffu, want, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = want;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long b = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += part[w];
+        atomicAdd(a.total, b);
+    }
 }
 
 __global__ void k_item_emit(int n, const int* lo, const int* hi, const int* off, unsigned mask, unsigned* ebucket,
@@ -199,13 +218,19 @@ static int build_grid(Sim* s, Arena& ar, int n, int nvi, const int* verts, const
     int* cnt = ar.take<int>((size_t)n + 1);
     int* off = ar.take<int>((size_t)n + 2);
     int* tmp = ar.take<int>(2 * ((size_t)n / 1024 + 8) + 64);
+    unsigned long long* want = ar.take<unsigned long long>(1);
     if (ar.used > ar.cap) {  // checked before any kernel writes into the arena
         s->scratch_bytes = 2 * ar.used + grid_bytes(n, 64);
         return kNeedScratch;
     }
-    ItemArgs a{n, nvi, verts, x, dir, alpha, inv, lo, hi, cnt};
+    cudaMemsetAsync(want, 0, sizeof(unsigned long long), st);
+    ItemArgs a{n, nvi, verts, x, dir, alpha, inv, lo, hi, cnt, want};
     if (n > 0) k_item_cells<<<nblk(n, 256), 256, 0, st>>>(a);
     else cudaMemsetAsync(cnt, 0, sizeof(int), st);
+    unsigned long long hw = 0;
+    cudaMemcpyAsync(&hw, want, sizeof(hw), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    if (hw > kMaxGridEntries) return kSpanTooLarge;  // before the int scan could overflow
     scan_exclusive(cnt, off, std::max(n, 1), tmp, st);
     int total = 0;
     cudaMemcpyAsync(&total, off + std::max(n, 1), sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -239,6 +264,15 @@ static int build_grid(Sim* s, Arena& ar, int n, int nvi, const int* verts, const
     G.bstart = bstart;
     G.items = items;
     return CIPC_OK;
+}
+
+// constraint-set grids have no step to shrink: an oversized grid is an error
+static int static_grid(int rc)
+{
+    if (rc == kSpanTooLarge)
+        return set_error(CIPC_ERR_INVALID_ARG, "spatial grid: primitives span more than %llu cells",
+                         (unsigned long long)kMaxGridEntries);
+    return rc;
 }
 
 // upper bound of scratch bytes for a grid over n items with ~c cells per item
@@ -540,7 +574,7 @@ int build_constraints(Sim* s, const double* x)
         ConSink S{s->ckind.p, s->cverts.p, s->cmult.p, s->cap_con, s->cnt.p, tkeys, tcount, tsz - 1};
         size_t mark = ar.used;
         Grid G;
-        rc = build_grid(s, ar, s->nbt, 3, s->btri.p, x, nullptr, 0, G);
+        rc = static_grid(build_grid(s, ar, s->nbt, 3, s->btri.p, x, nullptr, 0, G));
         if (rc == kNeedScratch) {
             if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
             continue;
@@ -549,7 +583,7 @@ int build_constraints(Sim* s, const double* x)
         CsArgs a{s->nbn, s->nbe, s->bnode.p, s->bedge.p, s->btri.p, x, s->X0.p, s->dbc.p, dHat, dHat * dHat, G, S};
         k_cs_pt<<<nblk(s->nbn, 128), 128, 0, st>>>(a);
         ar.used = mark;
-        rc = build_grid(s, ar, s->nbe, 2, s->bedge.p, x, nullptr, 0, G);
+        rc = static_grid(build_grid(s, ar, s->nbe, 2, s->bedge.p, x, nullptr, 0, G));
         if (rc == kNeedScratch) {
             if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
             continue;
@@ -561,7 +595,7 @@ int build_constraints(Sim* s, const double* x)
         if (s->nrod_e > 0 && s->nbn > s->codim0) {
             ar.used = mark;
             const int e_begin = s->nbe - s->nrod_e;
-            rc = build_grid(s, ar, s->nrod_e, 2, s->bedge.p + 2 * (size_t)e_begin, x, nullptr, 0, G);
+            rc = static_grid(build_grid(s, ar, s->nrod_e, 2, s->bedge.p + 2 * (size_t)e_begin, x, nullptr, 0, G));
             if (rc == kNeedScratch) {
                 if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
                 again = true;
@@ -574,7 +608,7 @@ int build_constraints(Sim* s, const double* x)
         }
         if (!again && s->nbn > s->codim1) {
             ar.used = mark;
-            rc = build_grid(s, ar, s->nbn, 1, s->bnode.p, x, nullptr, 0, G);
+            rc = static_grid(build_grid(s, ar, s->nbn, 1, s->bnode.p, x, nullptr, 0, G));
             if (rc == kNeedScratch) {
                 if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
                 again = true;
@@ -1198,6 +1232,7 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
     const double span = alpha * pSize / voxel;
     if (span > 1) alpha /= span;
     int cap = std::max(4096, 8 * (s->nbn + s->nbe));
+    int shrink = 0;
     for (int attempt = 0; attempt < 8; ++attempt) {
         const size_t need = grid_bytes(std::max(std::max(s->nbt, s->nbe), s->nbn), 32) + (size_t)cap * (16 + 1 + 8 + 1) + (1 << 20);
         int rc = ensure_scratch(s, need);
@@ -1213,6 +1248,12 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         size_t mark = ar.used;
         Grid G;
         rc = build_grid(s, ar, s->nbt, 3, s->btri.p, x, p, alpha, G);
+        if (rc == kSpanTooLarge) {
+            if (++shrink > 60) return set_error(CIPC_ERR_NOT_CONVERGED, "CCD: swept boxes span too many cells");
+            alpha *= 0.5;  // a smaller trial step: the bound stays conservative
+            --attempt;
+            continue;
+        }
         if (rc == kNeedScratch) {
             if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
             continue;
@@ -1223,6 +1264,12 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         k_ccd_pt<<<nblk(s->nbn, 128), 128, 0, st>>>(c);
         ar.used = mark;
         rc = build_grid(s, ar, s->nbe, 2, s->bedge.p, x, p, alpha, G);
+        if (rc == kSpanTooLarge) {
+            if (++shrink > 60) return set_error(CIPC_ERR_NOT_CONVERGED, "CCD: swept boxes span too many cells");
+            alpha *= 0.5;  // a smaller trial step: the bound stays conservative
+            --attempt;
+            continue;
+        }
         if (rc == kNeedScratch) {
             if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
             continue;
@@ -1235,6 +1282,12 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
             ar.used = mark;
             const int e_begin = s->nbe - s->nrod_e;
             rc = build_grid(s, ar, s->nrod_e, 2, s->bedge.p + 2 * (size_t)e_begin, x, p, alpha, G);
+            if (rc == kSpanTooLarge) {
+                if (++shrink > 60) return set_error(CIPC_ERR_NOT_CONVERGED, "CCD: swept boxes span too many cells");
+                alpha *= 0.5;  // a smaller trial step: the bound stays conservative
+                --attempt;
+                continue;
+            }
             if (rc == kNeedScratch) {
                 if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
                 again = true;
@@ -1248,6 +1301,12 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         if (!again && s->nbn > s->codim1) {
             ar.used = mark;
             rc = build_grid(s, ar, s->nbn, 1, s->bnode.p, x, p, alpha, G);
+            if (rc == kSpanTooLarge) {
+                if (++shrink > 60) return set_error(CIPC_ERR_NOT_CONVERGED, "CCD: swept boxes span too many cells");
+                alpha *= 0.5;  // a smaller trial step: the bound stays conservative
+                --attempt;
+                continue;
+            }
             if (rc == kNeedScratch) {
                 if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
                 again = true;

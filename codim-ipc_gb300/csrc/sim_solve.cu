@@ -332,11 +332,21 @@ static int solve_with_precond(Sim* s, const double* rhs, double* sol, int* iters
 
 int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
 {
+    // The learned correction is used once a block-Jacobi solve has set the
+    // yardstick, and not after it has stalled twice in this step.  It stalls when
+    // it needs more than three times the iterations of the latest block-Jacobi
+    // solve (at least 100; consecutive Newton systems differ in difficulty by up
+    // to ~2x), breaks down or yields NaN; block Jacobi then solves the same
+    // system, so a poor network costs at most ~4x a plain solve.
     bool learned = false;
-    if (s->prm.precond == 1 && s->learned) learned = lp_precond(s, static_cast<LpModel*>(s->learned)) == CIPC_OK;
+    if (s->prm.precond == 1 && s->learned && s->bj_last_iters > 0 && s->solve_fallbacks < 2)
+        learned = lp_precond(s, static_cast<LpModel*>(s->learned)) == CIPC_OK;
     if (!learned) build_precond(s);
     int total = 0, it = 0;
+    const int maxit = s->prm.pcg_maxit;
+    if (learned) s->prm.pcg_maxit = std::min(maxit, std::max(100, 3 * s->bj_last_iters));
     int rc = solve_with_precond(s, rhs, sol, &it);
+    s->prm.pcg_maxit = maxit;
     total += it;
     if (learned) {
         ++s->solve_learned;
@@ -347,7 +357,10 @@ int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
             build_precond(s);
             rc = solve_with_precond(s, rhs, sol, &it);
             total += it;
+            s->bj_last_iters = std::max(1, it);
         }
+    } else {
+        s->bj_last_iters = std::max(1, it);
     }
     if (iters) *iters = total;
     if (rc == CIPC_OK && s->capture) {

@@ -302,11 +302,13 @@ def rods_particles_on_cloth(n_rods=1000, seg_per_rod=100, rod_len=0.5, n_particl
 
 def rods_particles_on_cloth_full(seed=0):
     """The mixed codimensional scene at full size: 1000 rods x 100 segments (0.5 m)
-    in 5 layers of 200 parallel rods 5 mm apart (seeded layer directions), 20000
-    particles in two 100 x 100 layers 8 mm apart, on a 120 x 120 cloth (1 m)
-    pinned at its corners; 135,400 vertices."""
+    in 5 layers of 200 parallel rods 5 mm apart (seeded layer directions, layers
+    2.5 mm apart, the lowest 1.5 mm above the cloth, i.e. in contact range from
+    the start: rods and cloth fall together, so contact develops only where they
+    already touch), 20000 particles in two 100 x 100 layers 5 mm apart, on a
+    120 x 120 cloth (1 m) pinned at its corners; 135,400 vertices."""
     return rods_particles_on_cloth(n_rods=1000, seg_per_rod=100, rod_len=0.5, n_particles=20000, cloth_n=120,
-                                   cloth_size=1.0, layer_gap=5e-3, particle_gap=8e-3, lift=5e-3, seed=seed,
+                                   cloth_size=1.0, layer_gap=2.5e-3, particle_gap=5e-3, lift=1.5e-3, seed=seed,
                                    rods_per_layer=200, rod_spacing=5e-3, particles_per_row=100)
 
 
