@@ -204,6 +204,8 @@ _SIGS.update({
     "cipc_sim_init_oipc": (_c_int, [_vp, _c_dbl, _c_dbl, _vp, _vp]),
     "cipc_sim_set_kappa": (_c_int, [_vp, _c_dbl, _c_dbl]),
     "cipc_sim_get_kappa": (_c_int, [_vp, _vp]),
+    "cipc_sim_set_strain_limit": (_c_int, [_vp, _vp, _vp, _vp]),
+    "cipc_sim_get_strain_limit": (_c_int, [_vp, _vp]),
     "cipc_sim_set_state": (_c_int, [_vp, _vp, _vp]),
     "cipc_sim_get_state": (_c_int, [_vp, _vp, _vp]),
     "cipc_sim_set_dbc": (_c_int, [_vp, _c_int, _vp, _vp]),
@@ -279,6 +281,16 @@ class Sim:
     def kappa(self):
         k2 = np.zeros(2)
         _check(lib().cipc_sim_get_kappa(self.h, k2.ctypes.data))
+        return k2
+
+    def set_strain_limit(self, s, s_hat, kappa_s):
+        """Isotropic strain limiting (the reference's s, sHat, kappa_s pairs)."""
+        a, b, k = (np.ascontiguousarray(v, np.float64).reshape(2) for v in (s, s_hat, kappa_s))
+        _check(lib().cipc_sim_set_strain_limit(self.h, a.ctypes.data, b.ctypes.data, k.ctypes.data))
+
+    def strain_kappa(self):
+        k2 = np.zeros(2)
+        _check(lib().cipc_sim_get_strain_limit(self.h, k2.ctypes.data))
         return k2
 
     def set_state(self, x=None, v=None):

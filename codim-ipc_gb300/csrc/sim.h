@@ -7,6 +7,8 @@
 #include <cstdlib>
 #include <vector>
 
+#include "sl_params.h"
+
 namespace cipc {
 
 // constraint kinds: PP, PE, PT, EE and the mollified edge-edge family whose
@@ -82,6 +84,9 @@ struct Sim {
     double lam = 0, mu = 0, kbend = 0;
     double cell = 1;  // broad-phase cell size (mean rest edge length)
     double kappa = 1, kappa_max = 100;
+    SlParams sl;              // strain limiting (kappa_s doubles during steps, like kappa)
+    DBuf<double> sl_prev;     // per-triangle largest stretch after the previous Newton iteration
+    bool sl_have_prev = false;
     int trace = 0;    // CIPC_TRACE set: one stderr line per Newton iteration and refinement pass
     // static device data
     DBuf<int> tri, hinge, bnode, bedge, btri;

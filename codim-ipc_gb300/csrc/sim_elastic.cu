@@ -12,8 +12,11 @@
 
 #include <vector>
 
+#include "../../include/cipc.h"
+#include "cipc_util.h"
 #include "elements.cuh"
 #include "rod.cuh"
+#include "strain_limit.cuh"
 #include "sim.h"
 #include "sim_kernels.h"
 
@@ -212,6 +215,56 @@ __global__ void __launch_bounds__(128) k_rod_bend(ElasticArgs a, HT* hval)
     if (a.red && threadIdx.x == 0) a.red[blockIdx.x] = s;
 }
 
+// isotropic strain limiting (INEXT.h:120-466): barrier on the singular values of
+// each triangle's deformation; an infeasible triangle sets *a.flag
+template <typename HT>
+__global__ void __launch_bounds__(128) k_strain_limit(ElasticArgs a, HT* hval)
+{
+    __shared__ double sh[128];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0;
+    if (t < a.nt) {
+        const int vid[3] = {a.tri[3 * t], a.tri[3 * t + 1], a.tri[3 * t + 2]};
+        if (!(a.dbc[vid[0]] && a.dbc[vid[1]] && a.dbc[vid[2]])) {
+            const d3 x[3] = {ld(a.x, vid[0]), ld(a.x, vid[1]), ld(a.x, vid[2])};
+            const double kh = a.h * a.h * a.vol[t];
+            double g[9];
+            if (!sl_eg(x, a.P + 3 * t, a.sl, kh, e, a.g ? g : nullptr) && a.flag) *a.flag = 1.0;
+            if (a.g)
+                for (int v = 0; v < 3; ++v)
+#pragma unroll
+                    for (int d = 0; d < 3; ++d)
+                        if (g[3 * v + d] != 0) atomicAdd(a.g + 3 * vid[v] + d, g[3 * v + d]);
+            if (hval) {
+                HT H[9][9];
+                if (sl_hess<HT>(x, a.P + 3 * t, a.sl, kh, true, H))
+                    scatter_blocks<HT>(hval, a.tri_slot + 9 * t, a.proj, vid, 3, &H[0][0], 9);
+            }
+        }
+    }
+    const double s = block_sum(e, sh);
+    if (a.red && threadIdx.x == 0) a.red[blockIdx.x] = s;
+}
+
+// kappa_s update test (IMPLICIT_EULER.h:606-628): a triangle whose largest
+// stretch was within thr of the limit s0 after the previous Newton iteration and
+// still is sets *flag; prev[] takes the current stretches (1 for triangles with
+// all vertices Dirichlet, as in Compute_Inextensibility)
+__global__ void k_strain_update(int nt, const int* tri, const uint8_t* dbc, const double* x, const double* P,
+                                double s0, double thr, int have_prev, double* prev, unsigned long long* flag)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const int v0 = tri[3 * t], v1 = tri[3 * t + 1], v2 = tri[3 * t + 2];
+    double st = 1;
+    if (!(dbc[v0] && dbc[v1] && dbc[v2])) {
+        const d3 xs[3] = {ld(x, v0), ld(x, v1), ld(x, v2)};
+        st = sl_max_strain(xs, P + 3 * t);
+    }
+    if (have_prev && s0 - prev[t] < thr && s0 - st < thr) *flag = 1ull;
+    prev[t] = st;
+}
+
 // mass (+ Dirichlet penalty k m on penalized vertices) on free diagonal blocks,
 // identity on projected diagonal blocks
 template <typename HT>
@@ -328,12 +381,15 @@ ElasticArgs elastic_args(Sim* s, const double* x, double* g)
     a.rhinge_slot = s->rhinge_slot.p;
     a.rinfo = s->rinfo.p;
     a.rhinfo = s->rhinfo.p;
+    a.sl = s->sl;
+    a.flag = nullptr;
     return a;
 }
 
 // Energy partial layout: [inertia | membrane | bending | rod stretching | rod
-// bending]; returns the partial count.
-int elastic_energy_partials(Sim* s, const double* x, double* red)
+// bending | strain limiting (when on)]; returns the partial count.  flag (device
+// double, may be null) is set to 1 by a strain-infeasible triangle.
+int elastic_energy_partials(Sim* s, const double* x, double* red, double* flag)
 {
     const int b0 = nblk(s->nv, 256), b1 = nblk(s->nt, 128), b2 = nblk(s->nh, 128);
     const int b3 = nblk(s->nrs, 128), b4 = nblk(s->nrh, 128);
@@ -347,7 +403,51 @@ int elastic_energy_partials(Sim* s, const double* x, double* red)
     k_rod_spring<double><<<b3, 128, 0, s->stream>>>(a, nullptr);
     a.red = red + b0 + b1 + b2 + b3;
     k_rod_bend<double><<<b4, 128, 0, s->stream>>>(a, nullptr);
-    return b0 + b1 + b2 + b3 + b4;
+    int n = b0 + b1 + b2 + b3 + b4;
+    if (s->sl.k0 > 0) {
+        a.red = red + n;
+        a.flag = flag;
+        k_strain_limit<double><<<b1, 128, 0, s->stream>>>(a, nullptr);
+        n += b1;
+    }
+    return n;
+}
+
+int strain_feasible(Sim* s, const double* x, bool* ok)
+{
+    *ok = true;
+    if (!(s->sl.k0 > 0)) return CIPC_OK;
+    double* flag = s->red.p + s->red.n - 1;
+    cudaMemsetAsync(flag, 0, sizeof(double), s->stream);
+    ElasticArgs a = elastic_args(s, x, nullptr);
+    a.flag = flag;
+    k_strain_limit<double><<<nblk(s->nt, 128), 128, 0, s->stream>>>(a, nullptr);
+    double h = 0;
+    cudaMemcpyAsync(&h, flag, sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return set_cuda_error(e, "strain feasibility");
+    *ok = h == 0;
+    return CIPC_OK;
+}
+
+int strain_kappa_update(Sim* s, const double* x, bool* raise)
+{
+    *raise = false;
+    if (!(s->sl.k0 > 0) || s->nt == 0) return CIPC_OK;
+    if (s->sl_prev.n < (size_t)s->nt && s->sl_prev.alloc(s->nt) != cudaSuccess)
+        return set_error(CIPC_ERR_CUDA, "strain buffer");
+    unsigned long long* flag = s->cnt.p + 40;
+    cudaMemsetAsync(flag, 0, sizeof(unsigned long long), s->stream);
+    k_strain_update<<<nblk(s->nt, 256), 256, 0, s->stream>>>(s->nt, s->tri.p, s->dbc.p, x, s->P.p, s->sl.s0,
+                                                             1.0e-4 * (s->sl.s0 - s->sl.sh0), s->sl_have_prev ? 1 : 0,
+                                                             s->sl_prev.p, flag);
+    unsigned long long h = 0;
+    cudaMemcpyAsync(&h, flag, sizeof(h), cudaMemcpyDeviceToHost, s->stream);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return set_cuda_error(e, "strain update");
+    s->sl_have_prev = true;
+    *raise = h != 0;
+    return CIPC_OK;
 }
 
 void elastic_grad_hess(Sim* s, const double* x, double* g, bool want_hess)
@@ -362,6 +462,7 @@ void elastic_grad_hess(Sim* s, const double* x, double* g, bool want_hess)
         k_bending<float><<<nblk(s->nh, 128), 128, 0, s->stream>>>(a, hv);
         if (s->nrs) k_rod_spring<float><<<nblk(s->nrs, 128), 128, 0, s->stream>>>(a, hv);
         if (s->nrh) k_rod_bend<float><<<nblk(s->nrh, 128), 128, 0, s->stream>>>(a, hv);
+        if (s->sl.k0 > 0) k_strain_limit<float><<<nblk(s->nt, 128), 128, 0, s->stream>>>(a, hv);
         if (want_hess)
             k_mass_diag<float><<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->mass.p, s->proj.p, s->dbc.p,
                                                                       s->dbc_stiff, s->diag.p, hv);
@@ -371,6 +472,7 @@ void elastic_grad_hess(Sim* s, const double* x, double* g, bool want_hess)
         k_bending<double><<<nblk(s->nh, 128), 128, 0, s->stream>>>(a, hv);
         if (s->nrs) k_rod_spring<double><<<nblk(s->nrs, 128), 128, 0, s->stream>>>(a, hv);
         if (s->nrh) k_rod_bend<double><<<nblk(s->nrh, 128), 128, 0, s->stream>>>(a, hv);
+        if (s->sl.k0 > 0) k_strain_limit<double><<<nblk(s->nt, 128), 128, 0, s->stream>>>(a, hv);
         if (want_hess)
             k_mass_diag<double><<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->mass.p, s->proj.p, s->dbc.p,
                                                                        s->dbc_stiff, s->diag.p, hv);

@@ -24,11 +24,16 @@ struct ElasticArgs {
     int nrs, nrh;
     const int *rseg, *rhinge, *rseg_slot, *rhinge_slot;
     const double *rinfo, *rhinfo;
+    // strain limiting (on when sl.k0 > 0); flag set to 1 by an infeasible triangle
+    SlParams sl;
+    double* flag;
 };
 
 // sim_elastic.cu
 void launch_xtilde(Sim* s);
-int elastic_energy_partials(Sim* s, const double* x, double* red);  // returns #partials written
+int elastic_energy_partials(Sim* s, const double* x, double* red, double* flag);  // returns #partials written
+int strain_feasible(Sim* s, const double* x, bool* ok);          // all stretches within the strain limits
+int strain_kappa_update(Sim* s, const double* x, bool* raise);   // kappa_s doubling test; updates the history
 void elastic_grad_hess(Sim* s, const double* x, double* g, bool want_hess);
 void zero_dbc(Sim* s, double* g);
 int dbc_penalty_partials(Sim* s, const double* x, double* red, double* g);  // energy partials (+ gradient if g)

@@ -111,7 +111,7 @@ __global__ void k_kappa_flag(int n, const int* kind, const int4* verts, const do
 // constraint distance is at or below the offset.
 static int eval_energy(Sim* s, const double* x, double* E, bool* ok)
 {
-    const int worst = nblk(s->nv, 256) + nblk(s->nt, 128) + nblk(s->nh, 128) + nblk(s->nrs, 128) + nblk(s->nrh, 128) +
+    const int worst = nblk(s->nv, 256) + 2 * nblk(s->nt, 128) + nblk(s->nh, 128) + nblk(s->nrs, 128) + nblk(s->nrh, 128) +
                       (s->prm.withCollision ? nblk(s->ncon, 128) + nblk(s->nfric, 128) : 0) + 16;
     if ((int)s->red.n < worst + 16) {
         cudaStreamSynchronize(s->stream);
@@ -120,7 +120,7 @@ static int eval_energy(Sim* s, const double* x, double* E, bool* ok)
     double* red = s->red.p;
     double* out = red + s->red.n - 2;  // [E, flag]
     cudaMemsetAsync(out, 0, 2 * sizeof(double), s->stream);
-    int n = elastic_energy_partials(s, x, red);
+    int n = elastic_energy_partials(s, x, red, out + 1);
     n += dbc_penalty_partials(s, x, red + n, nullptr);
     if (s->prm.withCollision) {
         n += contact_energy_partials(s, x, red + n, out + 1);
@@ -190,6 +190,7 @@ int sim_step(Sim* s, StepStats* st)
     StepStats S;
     s->solve_fallbacks = 0;
     s->solve_learned = 0;
+    s->sl_have_prev = false;  // strain history is per step (IMPLICIT_EULER.h:444)
     const SimParams& P = s->prm;
     const int nv = s->nv, n3 = 3 * nv, nd = (int)s->dbc_idx_h.size();
     cudaStream_t str = s->stream;
@@ -298,7 +299,19 @@ int sim_step(Sim* s, StepStats* st)
         // line search (IMPLICIT_EULER.h:9-149)
         cudaMemcpyAsync(s->xprev.p, s->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
         double alpha = 1.0;
-        if (P.withCollision && (rc = ccd_step_size(s, s->xprev.p, s->dir.p, 1.0, &alpha))) return rc;
+        if (s->sl.k0 > 0) {
+            // strain-limit feasibility first (IMPLICIT_EULER.h:74-94): halve until
+            // every stretch is inside the limits
+            for (int k = 0;; ++k) {
+                if (k > 200) return set_error(CIPC_ERR_NOT_CONVERGED, "no strain-feasible step");
+                k_axpby<<<nblk(n3, 256), 256, 0, str>>>(n3, s->xprev.p, alpha, s->dir.p, s->x.p);
+                bool feas = true;
+                if ((rc = strain_feasible(s, s->x.p, &feas))) return rc;
+                if (feas) break;
+                alpha /= 2;
+            }
+        }
+        if (P.withCollision && (rc = ccd_step_size(s, s->xprev.p, s->dir.p, alpha, &alpha))) return rc;
         mark(6);
         const double feasible = alpha;
         double E = Eprev;
@@ -348,6 +361,15 @@ int sim_step(Sim* s, StepStats* st)
             }
         }
         save_prev(s, s->x.p);
+        // strain-limit stiffness update (IMPLICIT_EULER.h:606-645)
+        if (s->sl.k0 > 0) {
+            bool raise = false;
+            if ((rc = strain_kappa_update(s, s->x.p, &raise))) return rc;
+            if (raise && s->sl.k0 < 1e5) {
+                s->sl.k0 *= 2;
+                if ((rc = eval_energy(s, s->x.p, &Eprev, &ok))) return rc;
+            }
+        }
         // convergence (IMPLICIT_EULER.h:647-710)
         L2 = std::sqrt(sum_sq(s, s->dir.p, n3) / (nv - nd)) / P.h;
         ++it;
@@ -538,6 +560,30 @@ extern "C" int cipc_sim_get_kappa(cipc_sim* h, double* kappa2)
     if (int rc = check_sim(h)) return rc;
     kappa2[0] = h->s->kappa;
     kappa2[1] = h->s->kappa_max;
+    return CIPC_OK;
+}
+
+extern "C" int cipc_sim_set_strain_limit(cipc_sim* h, const double* s, const double* s_hat, const double* kappa_s)
+{
+    if (int rc = check_sim(h)) return rc;
+    if (!s || !s_hat || !kappa_s || !(kappa_s[0] >= 0) || !(kappa_s[1] >= 0) ||
+        (kappa_s[0] > 0 && !(s[0] > s_hat[0])) || (kappa_s[1] > 0 && !(s[1] < s_hat[1])))
+        return set_error(CIPC_ERR_INVALID_ARG, "cipc_sim_set_strain_limit: need s[0] > s_hat[0] (and s[1] < s_hat[1])");
+    SlParams& p = h->s->sl;
+    p.s0 = s[0];
+    p.s1 = s[1];
+    p.sh0 = s_hat[0];
+    p.sh1 = s_hat[1];
+    p.k0 = kappa_s[0];
+    p.k1 = kappa_s[1];
+    return CIPC_OK;
+}
+
+extern "C" int cipc_sim_get_strain_limit(cipc_sim* h, double* kappa_s)
+{
+    if (int rc = check_sim(h)) return rc;
+    kappa_s[0] = h->s->sl.k0;
+    kappa_s[1] = h->s->sl.k1;
     return CIPC_OK;
 }
 

@@ -207,6 +207,16 @@ int cipc_sim_destroy(cipc_sim* sim);
 int cipc_sim_init_oipc(cipc_sim* sim, double dhat, double stiff_mult, double* kappa2, double* dhat2);
 int cipc_sim_set_kappa(cipc_sim* sim, double kappa, double kappa_max);
 int cipc_sim_get_kappa(cipc_sim* sim, double* kappa2);
+/* Isotropic strain limiting (Library/FEM/Shell/INEXT.h; the driver's s, sHat and
+ * kappa_s, passed to Advance_One_Step_IE_Hinge, IMPLICIT_EULER.h:162): a barrier
+ * keeps every triangle's stretches (singular values of its deformation) below
+ * s[0], active above s_hat[0] with stiffness h^2 vol kappa_s[0], and above s[1]
+ * when kappa_s[1] > 0.  kappa_s[0] = 0 (the default) turns it off.  kappa_s[0]
+ * doubles (up to 1e5) when a triangle stays within 1e-4 (s[0] - s_hat[0]) of the
+ * limit, and keeps its value across steps (read it back with
+ * cipc_sim_get_strain_limit). */
+int cipc_sim_set_strain_limit(cipc_sim* sim, const double* s, const double* s_hat, const double* kappa_s);
+int cipc_sim_get_strain_limit(cipc_sim* sim, double* kappa_s);
 /* Positions / velocities, host arrays nv x 3 (either may be NULL). */
 int cipc_sim_set_state(cipc_sim* sim, const double* x, const double* v);
 int cipc_sim_get_state(cipc_sim* sim, double* x, double* v);

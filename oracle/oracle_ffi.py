@@ -191,6 +191,17 @@ class Shell:
         d2 = self.L.orc_shell_oipc(self.h, dhat, stiff_mult, _p(k2))
         return k2, d2
 
+    def set_strain_limit(self, s, s_hat, kappa_s):
+        self.L.orc_shell_set_strain_limit.argtypes = [ctypes.c_void_p, _P, _P, _P]
+        self.L.orc_shell_set_strain_limit(self.h, _p(_c(s, np.float64)), _p(_c(s_hat, np.float64)),
+                                          _p(_c(kappa_s, np.float64)))
+
+    def strain_kappa(self):
+        k2 = np.zeros(2)
+        self.L.orc_shell_get_strain_limit.argtypes = [ctypes.c_void_p, _P]
+        self.L.orc_shell_get_strain_limit(self.h, _p(k2))
+        return k2
+
     def constraints(self, x, dhat2, xi, cap=1 << 20):
         out = np.zeros((cap, 6), np.int32)
         n = self.L.orc_shell_constraints(self.h, _p(_c(x, np.float64)), _p(self.dbc), len(self.dbc), dhat2, xi,
@@ -312,3 +323,18 @@ def rod_bending(x9, lsum, Kb, project=True):
     H = np.zeros((9, 9))
     E = lb.orc_rod_bending(_p(x), lsum, Kb, _p(g), _p(H), 1 if project else 0)
     return E, g, H
+
+
+def strain_limit_elem(x9, P, kh, s, s_hat, kappa_s, project=True):
+    """(E, g[9], H[9x9], valid) of the strain-limiting barrier of one triangle;
+    P the inverse rest first fundamental form (p00, p01, p11), kh = h^2 vol."""
+    lb = lib()
+    lb.orc_sl_elem.restype = ctypes.c_double
+    lb.orc_sl_elem.argtypes = [_P, _P, ctypes.c_double, _P, _P, _P, ctypes.c_int, _P, _P, _P]
+    g = np.zeros(9)
+    H = np.zeros((9, 9))
+    ok = np.zeros(1, np.int32)
+    E = lb.orc_sl_elem(_p(_c(x9, np.float64)), _p(_c(P, np.float64)), kh, _p(_c(s, np.float64)),
+                       _p(_c(s_hat, np.float64)), _p(_c(kappa_s, np.float64)), 1 if project else 0, _p(g), _p(H),
+                       _p(ok))
+    return E, g, H, bool(ok[0])

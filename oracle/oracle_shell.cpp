@@ -489,6 +489,47 @@ static double rod_terms(const Shell& S, const double* x, double h, double* g, As
     return E;
 }
 
+extern "C" double orc_sl_elem(const double* x9, const double* P, double kh, const double* s, const double* s_hat,
+                               const double* kappa_s, int project, double* g, double* H, int* valid);
+extern "C" double orc_sl_strain(const double* x9, const double* P);
+
+// strain-limiting barrier over the triangles (INEXT.h:120-466); *valid cleared by
+// an infeasible triangle
+static double strain_terms(const Shell& S, const double* x, double h, double* g, Asm* A, bool* valid)
+{
+    if (!(S.sl_kappa[0] > 0)) return 0;
+    double E = 0;
+    const int nt = (int)S.vol.size();
+    for (int t = 0; t < nt; ++t) {
+        const int* v = &S.tri[3 * t];
+        if (all_dbc(S, v, 3)) continue;
+        double xe[9], ge[9], H[81];
+        gather(x, v, 3, xe);
+        int ok = 1;
+        E += orc_sl_elem(xe, &S.P[3 * t], h * h * S.vol[t], S.sl_s, S.sl_shat, S.sl_kappa, 1, g ? ge : nullptr,
+                         A ? H : nullptr, &ok);
+        if (!ok && valid) *valid = false;
+        if (g) scatter_add(g, v, 3, ge);
+        if (A) A->add_block(v, 3, H);
+    }
+    return E;
+}
+
+// largest stretch per triangle, 1 where all vertices are Dirichlet
+// (Compute_Inextensibility, INEXT.h:72-118)
+static void strains(const Shell& S, const double* x, std::vector<double>& out)
+{
+    const int nt = (int)S.vol.size();
+    out.assign(nt, 1.0);
+    for (int t = 0; t < nt; ++t) {
+        const int* v = &S.tri[3 * t];
+        if (all_dbc(S, v, 3)) continue;
+        double xe[9];
+        gather(x, v, 3, xe);
+        out[t] = orc_sl_strain(xe, &S.P[3 * t]);
+    }
+}
+
 static double elastic_energy(const Shell& S, const double* x, double h)
 {
     double E = 0;
@@ -1344,7 +1385,8 @@ static double total_energy(const Ctx& C, const double* x, const std::vector<Con>
         E += 0.5 * C.stiff * pen;
     }
     bool good = true;
-    if (C.P.withCollision) good = barrier_terms(S, x, cs, C.P.dHat2, C.P.xi, C.kappa, &E, nullptr, nullptr);
+    E += strain_terms(S, x, C.P.h, nullptr, nullptr, &good);
+    if (C.P.withCollision) good = barrier_terms(S, x, cs, C.P.dHat2, C.P.xi, C.kappa, &E, nullptr, nullptr) && good;
     if (C.P.withCollision && C.P.mu > 0) friction_terms(F, x, C.xn, C.P.epsv2 * C.P.h * C.P.h, C.P.mu, &E, nullptr, nullptr);
     if (ok) *ok = good;
     return E;
@@ -1357,6 +1399,7 @@ static void total_grad(const Ctx& C, const double* x, const std::vector<Con>& cs
     int n = 3 * S.nv;
     for (int i = 0; i < n; ++i) g[i] = 0;
     elastic_grad_hess(S, x, C.P.h, g, A);
+    strain_terms(S, x, C.P.h, g, A, nullptr);
     for (int i = 0; i < S.nv; ++i)
         for (int d = 0; d < 3; ++d) g[3 * i + d] += S.mass[i] * (x[3 * i + d] - C.xtilde[3 * i + d]);
     const std::vector<char>& proj = C.proj.empty() ? S.dbc : C.proj;
@@ -1422,7 +1465,7 @@ static void shell_step(Shell& S, const StepParams& P, double* x, double* v, doub
     }
     std::vector<Con> cs, cs_prev;
     std::vector<Fric> F;
-    std::vector<double> dist2_prev;
+    std::vector<double> dist2_prev, strain_prev;
     if (P.withCollision) {
         constraint_set(S, x, P.dHat2, P.xi, cs);
         if (P.mu > 0) friction_basis(x, cs, P.dHat2, P.xi, C.kappa, F);
@@ -1452,7 +1495,18 @@ static void shell_step(Shell& S, const StepParams& P, double* x, double* v, doub
         // line search (IMPLICIT_EULER.h:9-149)
         xprev.assign(x, x + n);
         double alpha = 1.0;
-        if (P.withCollision) alpha = ccd_step_size(S, xprev.data(), sol.data(), 1.0, P.xi);
+        if (S.sl_kappa[0] > 0) {
+            // strain-limit feasibility first (IMPLICIT_EULER.h:74-94)
+            for (;;) {
+                for (int i = 0; i < n; ++i) x[i] = xprev[i] + alpha * sol[i];
+                bool feas = true;
+                strain_terms(S, x, P.h, nullptr, nullptr, &feas);
+                if (feas) break;
+                alpha /= 2;
+            }
+            for (int i = 0; i < n; ++i) x[i] = xprev[i];
+        }
+        if (P.withCollision) alpha = ccd_step_size(S, xprev.data(), sol.data(), alpha, P.xi);
         double feasible = alpha, E;
         bool ok;
         do {
@@ -1489,6 +1543,20 @@ static void shell_step(Shell& S, const StepParams& P, double* x, double* v, doub
         dist2_prev.clear();
         if (!cs.empty()) min_dist2(cs, x, P.xi, &dist2_prev);
         cs_prev = cs;
+        // strain-limit stiffness update (IMPLICIT_EULER.h:606-645)
+        if (S.sl_kappa[0] > 0) {
+            std::vector<double> st;
+            strains(S, x, st);
+            const double thr = 1.0e-4 * (S.sl_s[0] - S.sl_shat[0]);
+            bool up = false;
+            for (size_t i = 0; i < strain_prev.size() && !up; ++i)
+                up = S.sl_s[0] - strain_prev[i] < thr && S.sl_s[0] - st[i] < thr;
+            if (up && S.sl_kappa[0] < 1e5) {
+                S.sl_kappa[0] *= 2;
+                Eprev = total_energy(C, x, cs, F, nullptr);
+            }
+            strain_prev = st;
+        }
         // convergence (IMPLICIT_EULER.h:647-710)
         double ss = 0;
         for (int i = 0; i < n; ++i) ss += sol[i] * sol[i];
@@ -1610,6 +1678,23 @@ void orc_shell_arrays(void* h, int* tri, double* P, double* vol, int* hinge, dou
 double orc_shell_oipc(void* h, double dhat, double stiffMult, double* kappa2)
 {
     return shell_oipc_kappa(*(Shell*)h, dhat, stiffMult, kappa2);
+}
+
+void orc_shell_set_strain_limit(void* h, const double* s, const double* s_hat, const double* kappa_s)
+{
+    Shell* S = (Shell*)h;
+    for (int k = 0; k < 2; ++k) {
+        S->sl_s[k] = s[k];
+        S->sl_shat[k] = s_hat[k];
+        S->sl_kappa[k] = kappa_s[k];
+    }
+}
+
+void orc_shell_get_strain_limit(void* h, double* kappa_s)
+{
+    const Shell* S = (const Shell*)h;
+    kappa_s[0] = S->sl_kappa[0];
+    kappa_s[1] = S->sl_kappa[1];
 }
 
 static void set_dbc(Shell* S, const int* idx, int n)

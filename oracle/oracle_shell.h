@@ -37,6 +37,9 @@ struct Shell {
     // bnode = [shell nodes | rod nodes from codim0 | particles from codim1];
     // the last nrod_e boundary edges are the rod segments
     int codim0 = 0, codim1 = 0, nrod_e = 0;
+    // isotropic strain limiting (INEXT.h): the reference's s, sHat, kappa_s pairs;
+    // off while sl_kappa[0] == 0
+    double sl_s[2] = {1.01, 0}, sl_shat[2] = {1, 1}, sl_kappa[2] = {0, 0};
 };
 
 struct StepParams {
