@@ -182,7 +182,7 @@ class StepParams(ctypes.Structure):
                 ("epsv2", ctypes.c_double), ("fric_iters", ctypes.c_int), ("newton_tol", ctypes.c_double),
                 ("with_collision", ctypes.c_int), ("max_newton_iters", ctypes.c_int), ("precision", ctypes.c_int),
                 ("pcg_tol", ctypes.c_double), ("pcg_max_iters", ctypes.c_int), ("preconditioner", ctypes.c_int),
-                ("forcing", ctypes.c_int)]
+                ("forcing", ctypes.c_int), ("barrier_model", ctypes.c_int)]
 
 
 class StepStats(ctypes.Structure):
@@ -204,7 +204,12 @@ _SIGS.update({
     "cipc_sim_init_oipc": (_c_int, [_vp, _c_dbl, _c_dbl, _vp, _vp]),
     "cipc_sim_set_kappa": (_c_int, [_vp, _c_dbl, _c_dbl]),
     "cipc_sim_get_kappa": (_c_int, [_vp, _vp]),
+    "cipc_sim_init_eipc": (_c_int, [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _vp, _vp]),
     "cipc_sim_set_strain_limit": (_c_int, [_vp, _vp, _vp, _vp]),
+    "cipc_sim_init_dirichlet": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_double, _c_int, _c_int, _vp]),
+    "cipc_sim_step_dirichlet": (_c_int, [_vp, ctypes.c_double]),
+    "cipc_sim_get_dbc": (_c_int, [_vp, _c_int, _vp, _vp, _vp]),
+    "cipc_sim_write_obj": (_c_int, [_vp, ctypes.c_char_p]),
     "cipc_sim_get_strain_limit": (_c_int, [_vp, _vp]),
     "cipc_sim_set_state": (_c_int, [_vp, _vp, _vp]),
     "cipc_sim_get_state": (_c_int, [_vp, _vp, _vp]),
@@ -218,9 +223,9 @@ _SIGS.update({
 
 def make_params(h, dhat2, xi, mu=0.0, epsv2=1e-6, fric_iters=1, newton_tol=1e-2, with_collision=True,
                 max_newton_iters=200, precision=FP64, pcg_tol=1e-6, pcg_max_iters=10000, preconditioner=0,
-                forcing=0):
+                forcing=0, elastic_ipc=False):
     return StepParams(h, dhat2, xi, mu, epsv2, fric_iters, newton_tol, int(bool(with_collision)), max_newton_iters,
-                      precision, pcg_tol, pcg_max_iters, preconditioner, forcing)
+                      precision, pcg_tol, pcg_max_iters, preconditioner, forcing, 1 if elastic_ipc else 0)
 
 
 class CodimDesc(ctypes.Structure):
@@ -275,6 +280,13 @@ class Sim:
         _check(lib().cipc_sim_init_oipc(self.h, dhat, stiff_mult, k2.ctypes.data, ctypes.byref(d2)))
         return k2, d2.value
 
+    def init_eipc(self, E, nu, thickness, dt):
+        """Initialize_EIPC: returns (kappa3, dhat2) and sets the simulation's kappa."""
+        k3 = np.zeros(3)
+        d2 = ctypes.c_double()
+        _check(lib().cipc_sim_init_eipc(self.h, E, nu, thickness, dt, k3.ctypes.data, ctypes.byref(d2)))
+        return k3, d2.value
+
     def set_kappa(self, kappa, kappa_max):
         _check(lib().cipc_sim_set_kappa(self.h, kappa, kappa_max))
 
@@ -282,6 +294,30 @@ class Sim:
         k2 = np.zeros(2)
         _check(lib().cipc_sim_get_kappa(self.h, k2.ctypes.data))
         return k2
+
+    def init_dirichlet(self, rel_min, rel_max, v=(0.0, 0.0, 0.0), rot_center=(0.0, 0.0, 0.0),
+                       rot_axis=(0.0, 1.0, 0.0), ang_vel_deg=0.0, v_begin=0, v_end=-1):
+        """FEM.Init_Dirichlet: appends a moving Dirichlet group; returns its size."""
+        arr = [np.ascontiguousarray(a, np.float64).reshape(3) for a in (rel_min, rel_max, v, rot_center, rot_axis)]
+        added = ctypes.c_int()
+        _check(lib().cipc_sim_init_dirichlet(self.h, *[a.ctypes.data for a in arr], float(ang_vel_deg), int(v_begin),
+                                             int(v_end), ctypes.byref(added)))
+        return added.value
+
+    def step_dirichlet(self, dt):
+        """FEM.Step_Dirichlet on the device."""
+        _check(lib().cipc_sim_step_dirichlet(self.h, float(dt)))
+
+    def dbc(self):
+        n = ctypes.c_int()
+        _check(lib().cipc_sim_get_dbc(self.h, 0, None, None, ctypes.byref(n)))
+        idx = np.zeros(n.value, np.int32)
+        tg = np.zeros((n.value, 3))
+        _check(lib().cipc_sim_get_dbc(self.h, n.value, idx.ctypes.data, tg.ctypes.data, ctypes.byref(n)))
+        return idx, tg
+
+    def write_obj(self, path):
+        _check(lib().cipc_sim_write_obj(self.h, str(path).encode()))
 
     def set_strain_limit(self, s, s_hat, kappa_s):
         """Isotropic strain limiting (the reference's s, sHat, kappa_s pairs)."""

@@ -47,6 +47,20 @@ struct DBuf {
     }
 };
 
+struct Sim;
+// barrier stiffness applied to the constraints: kappa for offset IPC; for elastic
+// IPC the reference's normalised barrier -kappa (d/dhat - 1)^2 ln(d/dhat) on
+// squared distances (Math/BARRIER.h:9-62, elastic branch) is the offset form with
+// kappa / dhat^4
+double barrier_kappa(const Sim* s);
+
+// one Init_Dirichlet group: list entries [begin, end) move by rotation about the
+// axis through center at ang_deg degrees per second, then by velocity v
+struct DbcMotion {
+    int begin, end;
+    double v[3], center[3], axis[3], ang_deg;
+};
+
 struct SimParams {
     double h = 0.04;          // time step
     double dHat2 = 1e-6;      // dhat^2
@@ -62,6 +76,7 @@ struct SimParams {
     int pcg_maxit = 10000;
     int precond = 0;          // 0 block-Jacobi, 1 learned correction (when a model is loaded)
     int forcing = 0;          // 1: inexact Newton (Eisenstat-Walker forcing term)
+    int elastic = 0;          // 1: elastic IPC (no offset, barrier scaled by 1/dhat^4, kappa fixed)
 };
 
 struct StepStats {
@@ -98,6 +113,8 @@ struct Sim {
     std::vector<int> dbc_idx_h;
     DBuf<int> dbc_idx;
     DBuf<double> dbc_tgt;
+    std::vector<DbcMotion> dbc_motion;  // device-side Dirichlet motion groups (ranges of the list above)
+    DBuf<DbcMotion> dbc_motion_d;
     // block sparsity of the elastic part (vertex blocks, 3x3) in ELL form: row i's
     // k-th block is block k * nv + i (k < ell_k), column col[k * nv + i]; padding
     // blocks are zero with the row's own column; nnzb = ell_k * nv

@@ -742,6 +742,11 @@ __global__ void __launch_bounds__(128) k_barrier_cons(BarArgs a, int want_h)
     if (a.red && threadIdx.x == 0) a.red[blockIdx.x] = sh[0];
 }
 
+double barrier_kappa(const Sim* s)
+{
+    return s->prm.elastic ? s->kappa / (s->prm.dHat2 * s->prm.dHat2) : s->kappa;
+}
+
 static BarArgs bar_args(Sim* s, const double* x)
 {
     BarArgs a;
@@ -754,7 +759,7 @@ static BarArgs bar_args(Sim* s, const double* x)
     a.dbc = s->proj.p;  // Hessian rows / columns removed from the Newton system
     a.xi2 = s->prm.xi * s->prm.xi;
     a.shat = s->prm.dHat2 + 2 * sqrt(s->prm.dHat2) * s->prm.xi;
-    a.kappa = s->kappa;
+    a.kappa = barrier_kappa(s);
     a.g = nullptr;
     a.red = nullptr;
     a.flag = nullptr;
@@ -915,7 +920,7 @@ int friction_basis(Sim* s, const double* x)
         return set_error(CIPC_ERR_CUDA, "friction buffers");
     const double shat = s->prm.dHat2 + 2 * sqrt(s->prm.dHat2) * s->prm.xi;
     k_fric_basis<<<nblk(s->nfric, 128), 128, 0, s->stream>>>(s->nfric, s->ckind.p, s->cverts.p, s->cmult.p, x,
-                                                             s->prm.xi * s->prm.xi, shat, s->kappa, s->fkind.p,
+                                                             s->prm.xi * s->prm.xi, shat, barrier_kappa(s), s->fkind.p,
                                                              s->fverts.p, s->fmult.p, s->fw.p, s->fT.p, s->flam.p);
     return CIPC_OK;
 }

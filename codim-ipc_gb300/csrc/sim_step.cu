@@ -21,6 +21,7 @@
 
 #include "../../include/cipc.h"
 #include "cipc_util.h"
+#include "sim_handle.h"
 #include "constraint_eval.cuh"
 #include "sim.h"
 #include "sim_host.h"
@@ -346,8 +347,8 @@ int sim_step(Sim* s, StepStats* st)
             std::fprintf(stderr, "cipc newton %d: step %.3e feasible %.3e trials %d E %.17g dE %.3e gd %d\n", it,
                          2 * alpha, feasible, trials, E, E - Eprev, (int)useGD);
         Eprev = E;
-        // barrier stiffness update (IMPLICIT_EULER.h:566-595)
-        if (s->npcon > 0) {
+        // barrier stiffness update (IMPLICIT_EULER.h:566-595; offset IPC only)
+        if (s->npcon > 0 && !P.elastic) {
             unsigned long long* flag = s->cnt.p + 32;
             cudaMemsetAsync(flag, 0, sizeof(unsigned long long), str);
             k_kappa_flag<<<nblk(s->npcon, 256), 256, 0, str>>>(s->npcon, s->pkind.p, s->pverts.p, s->pd2.p, s->x.p,
@@ -477,15 +478,6 @@ void sim_destroy(Sim* s)
 // ---------------------------------------------------------------------------
 using namespace cipc;
 
-struct cipc_sim {
-    Sim* s;
-};
-
-static int check_sim(cipc_sim* h)
-{
-    if (!h || !h->s) return set_error(CIPC_ERR_INVALID_ARG, "null simulation handle");
-    return CIPC_OK;
-}
 
 extern "C" int cipc_sim_create(int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
                                double thickness, const double* gravity, double bend_stiff_mult, int membrane_model,
@@ -544,6 +536,24 @@ extern "C" int cipc_sim_init_oipc(cipc_sim* h, double dhat, double stiff_mult, d
         kappa2[1] = k2[1];
     }
     if (dhat2) *dhat2 = d2;
+    return CIPC_OK;
+}
+
+extern "C" int cipc_sim_init_eipc(cipc_sim* h, double E, double nu, double thickness, double dt, double* kappa3,
+                                  double* dhat2)
+{
+    if (int rc = check_sim(h)) return rc;
+    if (!(E > 0) || !(nu > -1 && nu < 0.5) || !(thickness > 0) || !(dt > 0))
+        return set_error(CIPC_ERR_INVALID_ARG, "cipc_sim_init_eipc: bad material or step");
+    const double lambda = E * nu / (1 - nu * nu), mu = E / (2 * (1 + nu)), h2 = dt * dt;
+    h->s->kappa = h2 * mu;
+    h->s->kappa_max = h2 * lambda;
+    if (kappa3) {
+        kappa3[0] = h2 * mu;
+        kappa3[1] = h2 * lambda;
+        kappa3[2] = nu;
+    }
+    if (dhat2) *dhat2 = thickness * thickness;
     return CIPC_OK;
 }
 
@@ -617,6 +627,7 @@ extern "C" int cipc_sim_set_dbc(cipc_sim* h, int n, const int* idx, const double
     for (int k = 0; k < n; ++k)
         if (idx[k] < 0 || idx[k] >= s->nv) return set_error(CIPC_ERR_INDEX_RANGE, "cipc_sim_set_dbc: vertex index");
     s->dbc_idx_h.assign(idx, idx + n);
+    s->dbc_motion.clear();  // explicit targets replace any device-side motion
     std::vector<uint8_t> mask(s->nv, 0);
     for (int k = 0; k < n; ++k) mask[idx[k]] = 1;
     cudaError_t e = cudaMemcpyAsync(s->dbc.p, mask.data(), s->nv, cudaMemcpyHostToDevice, s->stream);
@@ -647,6 +658,10 @@ static void to_params(const cipc_step_params* p, SimParams& q)
     q.pcg_maxit = p->pcg_max_iters > 0 ? p->pcg_max_iters : 10000;
     q.precond = p->preconditioner;
     q.forcing = p->forcing;
+    // elastic IPC (Advance_One_Step_IE_Hinge_EIPC): no offset anywhere
+    // (IPC.h:49-51, 752-754, FRICTION.h:28-30)
+    q.elastic = p->barrier_model == CIPC_BARRIER_ELASTIC;
+    if (q.elastic) q.xi = 0;
 }
 
 extern "C" int cipc_sim_step(cipc_sim* h, const cipc_step_params* p, cipc_step_stats* stats)

@@ -38,6 +38,8 @@ extern "C" {
 
 #define CIPC_PRECISION_FP64 0  /* all-FP64, decisions bit-exact with the CPU restatement */
 #define CIPC_PRECISION_MIXED 1 /* FP32 classification / Hessians, FP64 distances and times */
+#define CIPC_BARRIER_OFFSET 0  /* offset IPC (C-IPC): barrier on d^2 - xi^2 */
+#define CIPC_BARRIER_ELASTIC 1 /* elastic IPC: no offset, barrier normalised by dhat */
 
 #define CIPC_MEM_HOST 0
 #define CIPC_MEM_DEVICE 1
@@ -158,6 +160,9 @@ typedef struct cipc_step_params {
     int forcing;           /* 0: every Newton system to pcg_tol; 1: inexact Newton, the
                               Eisenstat-Walker forcing term (choice 2, gamma 0.9, alpha 2)
                               clamped to [pcg_tol, 0.1], pcg_tol once RMS(step)/h < 10 tol */
+    int barrier_model;     /* CIPC_BARRIER_OFFSET (0, Advance_One_Step_IE_Hinge) or
+                              CIPC_BARRIER_ELASTIC (1, Advance_One_Step_IE_Hinge_EIPC:
+                              no offset, normalised barrier, kappa not adapted) */
 } cipc_step_params;
 
 typedef struct cipc_step_stats {
@@ -205,6 +210,11 @@ int cipc_sim_destroy(cipc_sim* sim);
 /* Offset-IPC barrier stiffness; replaces FEM.DiscreteShell.Initialize_OIPC
  * (DISCRETE_SHELL.h:555-577, export :1103).  Writes (kappa, kappa_max) and dhat^2. */
 int cipc_sim_init_oipc(cipc_sim* sim, double dhat, double stiff_mult, double* kappa2, double* dhat2);
+/* Elastic-IPC stiffness; replaces FEM.DiscreteShell.Initialize_EIPC
+ * (DISCRETE_SHELL.h:555-577, export :1102): kappa3 = (h^2 mu, h^2 lambda, nu) of the
+ * plane-stress material, dhat^2 = thickness^2; sets the simulation's kappa. */
+int cipc_sim_init_eipc(cipc_sim* sim, double E, double nu, double thickness, double dt, double* kappa3,
+                       double* dhat2);
 int cipc_sim_set_kappa(cipc_sim* sim, double kappa, double kappa_max);
 int cipc_sim_get_kappa(cipc_sim* sim, double* kappa2);
 /* Isotropic strain limiting (Library/FEM/Shell/INEXT.h; the driver's s, sHat and
@@ -223,6 +233,23 @@ int cipc_sim_get_state(cipc_sim* sim, double* x, double* v);
 /* Dirichlet vertices and their targets for the next step (the DBC storage of the
  * reference, moved by FEM.Step_Dirichlet on the host). */
 int cipc_sim_set_dbc(cipc_sim* sim, int n, const int* idx, const double* targets);
+/* Device-side Dirichlet motion; replaces FEM.Init_Dirichlet / FEM.Step_Dirichlet
+ * (Library/FEM/BOUNDARY_CONDITION.h:16-157).  init: the vertices of [v_begin,
+ * v_end) (v_end < 0: to the last vertex) whose current positions lie in the box
+ * rel_min..rel_max, relative to that range's bounding box, are appended to the
+ * Dirichlet list with their positions as targets, as one motion group (velocity
+ * v; rotation about rot_axis through rot_center at ang_vel_deg degrees per
+ * second); *added = their count.  step: advances every group's targets by dt on
+ * the device (rotation, then translation).  cipc_sim_set_dbc replaces the list
+ * and drops the motions.  get: copies up to cap indices / targets of the list. */
+int cipc_sim_init_dirichlet(cipc_sim* sim, const double* rel_min, const double* rel_max, const double* v,
+                            const double* rot_center, const double* rot_axis, double ang_vel_deg, int v_begin,
+                            int v_end, int* added);
+int cipc_sim_step_dirichlet(cipc_sim* sim, double dt);
+int cipc_sim_get_dbc(cipc_sim* sim, int cap, int* idx, double* targets, int* count);
+/* Writes the current positions and the shell triangles as an OBJ file in the
+ * reference's format (Write_TriMesh_Obj, Library/Utils/MESHIO.h:182-213). */
+int cipc_sim_write_obj(cipc_sim* sim, const char* path);
 /* One time step; replaces Advance_One_Step_IE_Hinge (IMPLICIT_EULER.h:151-902).
  * Returns CIPC_OK, or CIPC_ERR_NOT_CONVERGED when the Newton cap is reached or
  * the Dirichlet motion is blocked by contact (stats->status -1 / -2). */

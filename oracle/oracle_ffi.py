@@ -222,9 +222,10 @@ class Shell:
                                     len(self.dbc))
 
     def step(self, x, v, kappa2, dbc_idx, dbc_tgt, h, dhat2, xi, mu=0.0, epsv2=1e-6, fric_iters=1, tol=1e-2,
-             with_collision=True, max_iter=500):
+             with_collision=True, max_iter=500, elastic_ipc=False):
         """Advances x, v, kappa2 in place; returns (status, stats dict)."""
-        prm = np.array([h, dhat2, xi, mu, epsv2, fric_iters, tol, 1.0 if with_collision else 0.0, max_iter], float)
+        prm = np.array([h, dhat2, xi, mu, epsv2, fric_iters, tol, 1.0 if with_collision else 0.0, max_iter,
+                        1.0 if elastic_ipc else 0.0], float)
         st = np.zeros(4)
         idx = _c(dbc_idx, np.int32)
         tg = _c(dbc_tgt, np.float64)

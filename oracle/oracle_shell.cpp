@@ -1425,9 +1425,14 @@ static void total_grad(const Ctx& C, const double* x, const std::vector<Con>& cs
         }
 }
 
-static void shell_step(Shell& S, const StepParams& P, double* x, double* v, double* kappa, const int* dbc_idx,
+static void shell_step(Shell& S, const StepParams& P_in, double* x, double* v, double* kappa, const int* dbc_idx,
                        const double* dbc_tgt, int ndbc, StepOut& out)
 {
+    StepParams P = P_in;
+    if (P.elastic) P.xi = 0;  // IPC.h:49-51, 752-754, FRICTION.h:28-30
+    // the elastic barrier -k (d/dh - 1)^2 ln(d/dh) on squared distances is the
+    // offset form with k / dh^2 (Math/BARRIER.h:9-62)
+    auto bkappa = [&]() { return P.elastic ? kappa[0] / (P.dHat2 * P.dHat2) : kappa[0]; };
     const int nv = S.nv, n = 3 * nv;
     S.dbc.assign(nv, 0);
     for (int k = 0; k < ndbc; ++k) S.dbc[dbc_idx[k]] = 1;
@@ -1443,7 +1448,7 @@ static void shell_step(Shell& S, const StepParams& P, double* x, double* v, doub
         for (int d = 0; d < 3; ++d) disp[3 * dbc_idx[k] + d] = dbc_tgt[3 * k + d] - x[3 * dbc_idx[k] + d];
     double dbcAlpha = 1;
     if (P.withCollision) dbcAlpha = ccd_step_size(S, x, disp.data(), 1.0, P.xi);
-    Ctx C{&S, P, xt.data(), xn.data(), kappa[0]};
+    Ctx C{&S, P, xt.data(), xn.data(), bkappa()};
     C.dbc_idx = dbc_idx;
     C.dbc_tgt = dbc_tgt;
     C.ndbc = ndbc;
@@ -1524,8 +1529,8 @@ static void shell_step(Shell& S, const StepParams& P, double* x, double* v, doub
             alpha /= 2;
         } while (E > Eprev || !ok);
         Eprev = E;
-        // barrier stiffness update (IMPLICIT_EULER.h:566-595)
-        if (!cs_prev.empty()) {
+        // barrier stiffness update (IMPLICIT_EULER.h:566-595; offset IPC only)
+        if (!cs_prev.empty() && !P.elastic) {
             std::vector<double> cur;
             min_dist2(cs_prev, x, P.xi, &cur);
             bool up = false;
@@ -1764,7 +1769,7 @@ int orc_shell_step(void* h, const double* params, double* x, double* v, double* 
 {
     Shell* S = (Shell*)h;
     StepParams P{params[0], params[1], params[2], params[3], params[4], (int)params[5], params[6], (int)params[7],
-                 (int)params[8]};
+                 (int)params[8], (int)params[9]};
     StepOut o;
     shell_step(*S, P, x, v, kappa2, dbc_idx, dbc_tgt, ndbc, o);
     if (stats) {

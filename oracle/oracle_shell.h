@@ -49,6 +49,7 @@ struct StepParams {
     double tol;           // Newton tolerance (velocity units: RMS step / h)
     int withCollision;
     int maxIter;          // safety cap on Newton iterations
+    int elastic = 0;      // 1: elastic IPC (Advance_One_Step_IE_Hinge_EIPC): no offset, barrier / dhat^4, kappa fixed
 };
 
 }  // namespace orc
