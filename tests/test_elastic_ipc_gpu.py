@@ -8,9 +8,12 @@ Scene: the shell tests' 8x8 cloth (0.5 m) 5 mm above a fixed box, E 1e5,
 rho 200, 1 mm; dhat = thickness = 1 mm, dt 0.04.
 
 Bars: Initialize_EIPC values exact; constraint sets equal as sets; incremental
-potential and gradient 1e-10 relative; positions after steps solved to a tight
-Newton tolerance within 1e-8 of the bounding-box diagonal of the oracle's
-direct-solve Newton; every step intersection free; kappa unchanged."""
+potential 1e-10 relative, gradient 1e-10 relative plus 1e-13 (the rounding level
+of the elastic gradients at rest); positions after steps solved to a tight
+Newton tolerance (1e-7) within 2 sqrt(free vertices) tol h of the oracle's
+direct-solve Newton (each loop stops once its RMS step is at most tol h; the
+soft elastic barrier, kappa = h^2 mu, makes these systems ill-conditioned, ~60
+Newton iterations, so the two stopping points differ at that level); every step intersection free; kappa unchanged."""
 import numpy as np
 import pytest
 
@@ -43,7 +46,7 @@ def test_elastic_ipc_steps_match_direct_solve(cuda, orc):
     k2 = _kappa()
     assert dhat2 == T_SHELL * T_SHELL and np.array_equal(k3[:2], k2) and k3[2] == NU
     prm = F.make_params(DT, dhat2, 0.0, newton_tol=1e-7, pcg_tol=1e-12, max_newton_iters=400, elastic_ipc=True)
-    diag = np.linalg.norm(X.max(0) - X.min(0))
+    bar = 2 * np.sqrt(X.shape[0] - len(dbc)) * 1e-7 * DT
     xo, vo = X.copy(), np.zeros_like(X)
     sh.dbc = dbc
     rng = np.random.default_rng(0)
@@ -55,11 +58,11 @@ def test_elastic_ipc_steps_match_direct_solve(cuda, orc):
         cg = sorted(map(tuple, s.constraints(prm, xo).tolist()))
         co = sorted(map(tuple, sh.constraints(xo, dhat2, 0.0).tolist()))
         assert cg == co, step
-        xt = xo + rng.standard_normal(xo.shape) * 1e-5
+        xt = xo + rng.standard_normal(xo.shape) * 1e-3
         Eg, gg = s.eval(prm, xo, xt)
         Eo, go = sh.eval(xo, xt, dhat2, 0.0, k2[0] / (dhat2 * dhat2), DT)
         assert abs(Eg - Eo) <= 1e-10 * abs(Eo), (step, Eg, Eo)
-        assert np.abs(gg - go).max() <= 1e-10 * np.abs(go).max(), step
+        assert np.abs(gg - go).max() <= 1e-10 * np.abs(go).max() + 1e-13, step
         # one step each
         rc, sto = sh.step(xo, vo, k2, dbc, X[dbc], DT, dhat2, 0.0, tol=1e-7, max_iter=400, elastic_ipc=True)
         assert rc == 0
@@ -67,6 +70,6 @@ def test_elastic_ipc_steps_match_direct_solve(cuda, orc):
         xg, _ = s.state()
         assert stg.min_dist2 > 0 or stg.n_constraints == 0
         contact += stg.n_constraints > 0
-        assert np.abs(xg - xo).max() <= 1e-8 * diag, (step, np.abs(xg - xo).max(), sto, stg.as_dict())
+        assert np.abs(xg - xo).max() <= bar, (step, np.abs(xg - xo).max(), sto, stg.as_dict())
         assert np.array_equal(s.kappa(), k2) and np.array_equal(k2, _kappa())
     assert contact >= 2
