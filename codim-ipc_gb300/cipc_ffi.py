@@ -204,6 +204,8 @@ _SIGS.update({
     "cipc_sim_init_oipc": (_c_int, [_vp, _c_dbl, _c_dbl, _vp, _vp]),
     "cipc_sim_set_kappa": (_c_int, [_vp, _c_dbl, _c_dbl]),
     "cipc_sim_get_kappa": (_c_int, [_vp, _vp]),
+    "cipc_sim_create_full": (_c_int, [_c_int, _vp, _c_int, _vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_double, _vp, ctypes.c_double, _c_int, _vp, _vp, _vp]),
     "cipc_sim_init_eipc": (_c_int, [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _vp, _vp]),
     "cipc_sim_set_strain_limit": (_c_int, [_vp, _vp, _vp, _vp]),
     "cipc_sim_init_dirichlet": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_double, _c_int, _c_int, _vp]),
@@ -235,19 +237,40 @@ class CodimDesc(ctypes.Structure):
                 ("particle_thickness", ctypes.c_double)]
 
 
+class TetDesc(ctypes.Structure):
+    _fields_ = [("n_tets", ctypes.c_int), ("tets", ctypes.c_void_p), ("E", ctypes.c_double), ("nu", ctypes.c_double),
+                ("rho", ctypes.c_double)]
+
+
 class Sim:
     """Owns one cipc_sim handle (device-resident shell scene).
 
     codim (optional): dict(segments=(n,2) ints, rod_E, rod_rho, rod_thickness,
-    rod_bend_mult=1, particles=(m,) ints, particle_rho, particle_thickness)."""
+    rod_bend_mult=1, particles=(m,) ints, particle_rho, particle_thickness).
+    tets (optional): dict(tets=(k,4) ints, E, nu, rho) -- volumetric Neo-Hookean."""
 
     def __init__(self, X, T, rho, E, nu, thickness, gravity=(0.0, -9.81, 0.0), bend_stiff_mult=1.0, nh=True,
-                 codim=None):
+                 codim=None, tets=None):
         X = np.ascontiguousarray(X, np.float64)
         T = np.ascontiguousarray(T, np.int32).reshape(-1, 3)
         g = np.ascontiguousarray(gravity, np.float64)
         h = ctypes.c_void_p()
-        if codim is None:
+        if tets is not None:
+            tt = np.ascontiguousarray(tets["tets"], np.int32).reshape(-1, 4)
+            td = TetDesc(tt.shape[0], tt.ctypes.data, tets["E"], tets["nu"], tets["rho"])
+            cdp = None
+            if codim is not None:
+                seg = np.ascontiguousarray(codim.get("segments", np.zeros((0, 2))), np.int32).reshape(-1, 2)
+                par = np.ascontiguousarray(codim.get("particles", np.zeros(0)), np.int32).reshape(-1)
+                cdp = ctypes.byref(CodimDesc(seg.shape[0], seg.ctypes.data if seg.size else None,
+                                             codim.get("rod_E", 0.0), codim.get("rod_rho", 0.0),
+                                             codim.get("rod_thickness", 0.0), codim.get("rod_bend_mult", 1.0),
+                                             par.shape[0], par.ctypes.data if par.size else None,
+                                             codim.get("particle_rho", 0.0), codim.get("particle_thickness", 0.0)))
+            _check(lib().cipc_sim_create_full(X.shape[0], X.ctypes.data, T.shape[0], T.ctypes.data if T.size else None,
+                                              rho, E, nu, thickness, g.ctypes.data, bend_stiff_mult, 1 if nh else 0,
+                                              cdp, ctypes.byref(td), ctypes.byref(h)))
+        elif codim is None:
             _check(lib().cipc_sim_create(X.shape[0], X.ctypes.data, T.shape[0], T.ctypes.data, rho, E, nu, thickness,
                                          g.ctypes.data, bend_stiff_mult, 1 if nh else 0, ctypes.byref(h)))
         else:

@@ -124,6 +124,11 @@ struct Sim {
     int nrs = 0, nrh = 0;
     DBuf<int> rseg, rhinge, rseg_slot, rhinge_slot;
     DBuf<double> rinfo, rhinfo;
+    // volumetric Neo-Hookean tetrahedra (Dm^-1 row-major, volume, ELL slots)
+    int ntet = 0;
+    double tlam = 0, tmu = 0;
+    DBuf<int> tet, tet_slot;
+    DBuf<double> tDinv, tvol;
     // boundary layout: bnode = [shell | rod nodes from codim0 | particles from codim1],
     // the last nrod_e boundary edges are rod segments
     int codim0 = 0, codim1 = 0, nrod_e = 0;
@@ -171,8 +176,10 @@ struct Sim {
 
 // host-side construction (sim_setup.cpp)
 struct CodimDesc;
+struct TetDesc;
 int sim_create(Sim** out, int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
-               double thickness, const double* gravity, double bendMult, int nh_model, const CodimDesc* cd = nullptr);
+               double thickness, const double* gravity, double bendMult, int nh_model, const CodimDesc* cd = nullptr,
+               const TetDesc* td = nullptr);
 void sim_destroy(Sim* s);
 
 }  // namespace cipc

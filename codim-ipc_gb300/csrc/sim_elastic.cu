@@ -17,6 +17,7 @@
 #include "elements.cuh"
 #include "rod.cuh"
 #include "strain_limit.cuh"
+#include "tet_nh.cuh"
 #include "sim.h"
 #include "sim_kernels.h"
 
@@ -246,6 +247,37 @@ __global__ void __launch_bounds__(128) k_strain_limit(ElasticArgs a, HT* hval)
     if (a.red && threadIdx.x == 0) a.red[blockIdx.x] = s;
 }
 
+// volumetric Neo-Hookean tetrahedra (INC_POTENTIAL.h:97-109, 228-229, 354-364);
+// an inverted tetrahedron (J <= 0) sets *a.flag
+template <typename HT>
+__global__ void __launch_bounds__(128) k_tet_nh(ElasticArgs a, HT* hval)
+{
+    __shared__ double sh[128];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0;
+    if (t < a.ntet) {
+        const int vid[4] = {a.tet[4 * t], a.tet[4 * t + 1], a.tet[4 * t + 2], a.tet[4 * t + 3]};
+        if (!(a.dbc[vid[0]] && a.dbc[vid[1]] && a.dbc[vid[2]] && a.dbc[vid[3]])) {
+            const d3 x[4] = {ld(a.x, vid[0]), ld(a.x, vid[1]), ld(a.x, vid[2]), ld(a.x, vid[3])};
+            const double w = a.h * a.h * a.tvol[t];
+            double g[12];
+            const bool ok = tet_nh_eg(x, a.tDinv + 9 * t, w, a.tlam, a.tmu, e, a.g ? g : nullptr);
+            if (!ok && a.flag) *a.flag = 1.0;
+            if (a.g && ok)
+                for (int v = 0; v < 4; ++v)
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) atomicAdd(a.g + 3 * vid[v] + d, g[3 * v + d]);
+            if (hval && ok) {
+                HT H[12][12];
+                tet_nh_hess<HT>(x, a.tDinv + 9 * t, w, a.tlam, a.tmu, true, H);
+                scatter_blocks<HT>(hval, a.tet_slot + 16 * t, a.proj, vid, 4, &H[0][0], 12);
+            }
+        }
+    }
+    const double s = block_sum(e, sh);
+    if (a.red && threadIdx.x == 0) a.red[blockIdx.x] = s;
+}
+
 // kappa_s update test (IMPLICIT_EULER.h:606-628): a triangle whose largest
 // stretch was within thr of the limit s0 after the previous Newton iteration and
 // still is sets *flag; prev[] takes the current stretches (1 for triangles with
@@ -383,12 +415,20 @@ ElasticArgs elastic_args(Sim* s, const double* x, double* g)
     a.rhinfo = s->rhinfo.p;
     a.sl = s->sl;
     a.flag = nullptr;
+    a.ntet = s->ntet;
+    a.tet = s->tet.p;
+    a.tet_slot = s->tet_slot.p;
+    a.tDinv = s->tDinv.p;
+    a.tvol = s->tvol.p;
+    a.tlam = s->tlam;
+    a.tmu = s->tmu;
     return a;
 }
 
 // Energy partial layout: [inertia | membrane | bending | rod stretching | rod
-// bending | strain limiting (when on)]; returns the partial count.  flag (device
-// double, may be null) is set to 1 by a strain-infeasible triangle.
+// bending | strain limiting (when on) | tetrahedra]; returns the partial count.
+// flag (device double, may be null) is set to 1 by a strain-infeasible triangle
+// or an inverted tetrahedron.
 int elastic_energy_partials(Sim* s, const double* x, double* red, double* flag)
 {
     const int b0 = nblk(s->nv, 256), b1 = nblk(s->nt, 128), b2 = nblk(s->nh, 128);
@@ -404,28 +444,34 @@ int elastic_energy_partials(Sim* s, const double* x, double* red, double* flag)
     a.red = red + b0 + b1 + b2 + b3;
     k_rod_bend<double><<<b4, 128, 0, s->stream>>>(a, nullptr);
     int n = b0 + b1 + b2 + b3 + b4;
+    a.flag = flag;
     if (s->sl.k0 > 0) {
         a.red = red + n;
-        a.flag = flag;
         k_strain_limit<double><<<b1, 128, 0, s->stream>>>(a, nullptr);
         n += b1;
+    }
+    if (s->ntet > 0) {
+        a.red = red + n;
+        k_tet_nh<double><<<nblk(s->ntet, 128), 128, 0, s->stream>>>(a, nullptr);
+        n += nblk(s->ntet, 128);
     }
     return n;
 }
 
-int strain_feasible(Sim* s, const double* x, bool* ok)
+int elastic_feasible(Sim* s, const double* x, bool* ok)
 {
     *ok = true;
-    if (!(s->sl.k0 > 0)) return CIPC_OK;
+    if (!(s->sl.k0 > 0) && s->ntet == 0) return CIPC_OK;
     double* flag = s->red.p + s->red.n - 1;
     cudaMemsetAsync(flag, 0, sizeof(double), s->stream);
     ElasticArgs a = elastic_args(s, x, nullptr);
     a.flag = flag;
-    k_strain_limit<double><<<nblk(s->nt, 128), 128, 0, s->stream>>>(a, nullptr);
+    if (s->sl.k0 > 0) k_strain_limit<double><<<nblk(s->nt, 128), 128, 0, s->stream>>>(a, nullptr);
+    if (s->ntet > 0) k_tet_nh<double><<<nblk(s->ntet, 128), 128, 0, s->stream>>>(a, nullptr);
     double h = 0;
     cudaMemcpyAsync(&h, flag, sizeof(double), cudaMemcpyDeviceToHost, s->stream);
     cudaError_t e = cudaStreamSynchronize(s->stream);
-    if (e != cudaSuccess) return set_cuda_error(e, "strain feasibility");
+    if (e != cudaSuccess) return set_cuda_error(e, "elastic feasibility");
     *ok = h == 0;
     return CIPC_OK;
 }
@@ -463,6 +509,7 @@ void elastic_grad_hess(Sim* s, const double* x, double* g, bool want_hess)
         if (s->nrs) k_rod_spring<float><<<nblk(s->nrs, 128), 128, 0, s->stream>>>(a, hv);
         if (s->nrh) k_rod_bend<float><<<nblk(s->nrh, 128), 128, 0, s->stream>>>(a, hv);
         if (s->sl.k0 > 0) k_strain_limit<float><<<nblk(s->nt, 128), 128, 0, s->stream>>>(a, hv);
+        if (s->ntet > 0) k_tet_nh<float><<<nblk(s->ntet, 128), 128, 0, s->stream>>>(a, hv);
         if (want_hess)
             k_mass_diag<float><<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->mass.p, s->proj.p, s->dbc.p,
                                                                       s->dbc_stiff, s->diag.p, hv);
@@ -473,6 +520,7 @@ void elastic_grad_hess(Sim* s, const double* x, double* g, bool want_hess)
         if (s->nrs) k_rod_spring<double><<<nblk(s->nrs, 128), 128, 0, s->stream>>>(a, hv);
         if (s->nrh) k_rod_bend<double><<<nblk(s->nrh, 128), 128, 0, s->stream>>>(a, hv);
         if (s->sl.k0 > 0) k_strain_limit<double><<<nblk(s->nt, 128), 128, 0, s->stream>>>(a, hv);
+        if (s->ntet > 0) k_tet_nh<double><<<nblk(s->ntet, 128), 128, 0, s->stream>>>(a, hv);
         if (want_hess)
             k_mass_diag<double><<<nblk(s->nv, 256), 256, 0, s->stream>>>(s->nv, s->mass.p, s->proj.p, s->dbc.p,
                                                                        s->dbc_stiff, s->diag.p, hv);

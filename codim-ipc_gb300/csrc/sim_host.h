@@ -18,6 +18,15 @@ struct CodimDesc {
     double part_rho = 0, part_thickness = 0;
 };
 
+// Volumetric tetrahedra (the drivers' add_object_3D: FEM.Compute_Vol_And_Inv_Basis,
+// Library/FEM/DEFORMATION_GRADIENT.h:39-76; lumped mass; Neo-Hookean material with
+// lambda = E nu / ((1 + nu)(1 - 2 nu)), mu = E / (2 (1 + nu))).
+struct TetDesc {
+    int ntet = 0;
+    const int* tet = nullptr;  // 4 vertex indices per tetrahedron
+    double E = 0, nu = 0, rho = 0;
+};
+
 struct HostScene {
     int nv = 0, nh_model = 1;
     std::vector<double> X0, P, vol, hinfo, mass, b;
@@ -34,11 +43,16 @@ struct HostScene {
     // boundary layout of the codimensional primitives (IMPLICIT_EULER.h:242-277):
     // bnode = [shell nodes | rod nodes | particles], bedge = [shell edges | rod segments]
     int codim0 = 0, codim1 = 0, nrod_e = 0;
+    // tetrahedra: vertices (4), rest inverse basis Dm^-1 (9, row-major), volume,
+    // ELL slots (16); their surface triangles lead the contact triangles
+    std::vector<int> tet, tet_slot;
+    std::vector<double> tDinv, tvol;
+    double tlam = 0, tmu = 0;
 };
 
 int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
                      double thickness, const double* gravity, double bendMult, int nh_model,
-                     const CodimDesc* cd = nullptr);
+                     const CodimDesc* cd = nullptr, const TetDesc* td = nullptr);
 double oipc_kappa(const std::vector<double>& mass, double dhat, double stiffMult, double* kappa2);
 int sim_upload(Sim* s, const HostScene& S);
 

@@ -25,14 +25,20 @@ struct ElasticArgs {
     const int *rseg, *rhinge, *rseg_slot, *rhinge_slot;
     const double *rinfo, *rhinfo;
     // strain limiting (on when sl.k0 > 0); flag set to 1 by an infeasible triangle
+    // or tetrahedron
     SlParams sl;
     double* flag;
+    // volumetric Neo-Hookean tetrahedra
+    int ntet;
+    const int *tet, *tet_slot;
+    const double *tDinv, *tvol;
+    double tlam, tmu;
 };
 
 // sim_elastic.cu
 void launch_xtilde(Sim* s);
 int elastic_energy_partials(Sim* s, const double* x, double* red, double* flag);  // returns #partials written
-int strain_feasible(Sim* s, const double* x, bool* ok);          // all stretches within the strain limits
+int elastic_feasible(Sim* s, const double* x, bool* ok);         // stretches within the strain limits, tets not inverted
 int strain_kappa_update(Sim* s, const double* x, bool* raise);   // kappa_s doubling test; updates the history
 void elastic_grad_hess(Sim* s, const double* x, double* g, bool want_hess);
 void zero_dbc(Sim* s, double* g);

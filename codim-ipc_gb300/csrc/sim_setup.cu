@@ -12,6 +12,7 @@
 // (vertex pairs sharing a triangle or a hinge) with per-element slot maps, which
 // is the sort-reduce of the reference's triplet assembly done once per mesh.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdlib>
 #include <map>
@@ -57,9 +58,36 @@ static double rest_dihedral(const double* X0, const double* X1, const double* X2
     return th;
 }
 
-int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
-                     double thickness, const double* gravity, double bendMult, int nh_model, const CodimDesc* cd)
+// surface triangles of a tetrahedral mesh (Find_Surface_TriMesh, MESHIO.h:486-544):
+// the four outward faces (0,2,1), (0,3,2), (0,1,3), (1,2,3) of every tetrahedron
+// keyed as given; a face is on the surface if no rotation of its reverse is a key;
+// output in key order
+static void tet_surface(int ntet, const int* tet, std::vector<int>& out)
 {
+    std::set<std::array<int, 3>> keys;
+    for (int t = 0; t < ntet; ++t) {
+        const int* v = tet + 4 * t;
+        keys.insert({v[0], v[2], v[1]});
+        keys.insert({v[0], v[3], v[2]});
+        keys.insert({v[0], v[1], v[3]});
+        keys.insert({v[1], v[2], v[3]});
+    }
+    for (const auto& k : keys) {
+        if (keys.count({k[2], k[1], k[0]}) || keys.count({k[1], k[0], k[2]}) || keys.count({k[0], k[2], k[1]})) continue;
+        out.insert(out.end(), k.begin(), k.end());
+    }
+}
+
+int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
+                     double thickness, const double* gravity, double bendMult, int nh_model, const CodimDesc* cd,
+                     const TetDesc* td)
+{
+    if (td && td->ntet) {
+        if (td->ntet < 0 || !td->tet || !(td->rho > 0) || !(td->E > 0) || !(td->nu > -1 && td->nu < 0.5))
+            return set_error(CIPC_ERR_INVALID_ARG, "tet setup: null arrays or bad material");
+        for (int i = 0; i < 4 * td->ntet; ++i)
+            if (td->tet[i] < 0 || td->tet[i] >= nv) return set_error(CIPC_ERR_INDEX_RANGE, "tet setup: vertex index out of range");
+    }
     if (cd) {
         if (cd->nseg < 0 || cd->npart < 0 || (cd->nseg && !cd->seg) || (cd->npart && !cd->part))
             return set_error(CIPC_ERR_INVALID_ARG, "codim setup: null arrays or negative counts");
@@ -91,6 +119,11 @@ int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* t
         if (a00 * a11 - a01 * a01 != 0) S.tri.insert(S.tri.end(), tri + 3 * t, tri + 3 * t + 3);
     }
     nt = (int)S.tri.size() / 3;
+    // contact triangles: tetrahedral surface first, then the shell (IMPLICIT_EULER.h:235-241)
+    std::vector<int> ctri;
+    if (td && td->ntet) tet_surface(td->ntet, td->tet, ctri);
+    ctri.insert(ctri.end(), S.tri.begin(), S.tri.end());
+    const int nct = (int)ctri.size() / 3;
     std::map<std::pair<int, int>, int> e2t;
     for (int t = 0; t < nt; ++t) {
         const int* v = &S.tri[3 * t];
@@ -98,8 +131,8 @@ int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* t
     }
     std::set<std::pair<int, int>> es;
     std::vector<char> isb(nv, 0);
-    for (int t = 0; t < nt; ++t) {
-        const int* v = &S.tri[3 * t];
+    for (int t = 0; t < nct; ++t) {
+        const int* v = &ctri[3 * t];
         for (int k = 0; k < 3; ++k) {
             int a = v[k], b = v[(k + 1) % 3];
             if (!es.count({b, a})) es.insert({a, b});
@@ -112,7 +145,7 @@ int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* t
     }
     for (int i = 0; i < nv; ++i)
         if (isb[i]) S.bnode.push_back(i);
-    S.btri = S.tri;
+    S.btri = ctri;
     S.P.resize(3 * nt);
     S.vol.resize(nt);
     S.mass.assign(nv, 0.0);
@@ -163,6 +196,40 @@ int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* t
         v3sub(X1v, X3v, b);
         v3cross(a, b, n2);
         S.hinfo.insert(S.hinfo.end(), {rest_dihedral(X0v, X1v, X2v, X3v), el, (v3norm(n1) + v3norm(n2)) / (el * 6)});
+    }
+    // tetrahedra (DEFORMATION_GRADIENT.h:39-76): Dm = [X1-X0, X2-X0, X3-X0],
+    // vol = det(Dm) / 6, Dm^-1; mass vol rho / 4 per corner
+    if (td && td->ntet) {
+        S.tlam = td->E * td->nu / ((1 + td->nu) * (1 - 2 * td->nu));
+        S.tmu = td->E / (2 * (1 + td->nu));
+        for (int t = 0; t < td->ntet; ++t) {
+            const int* v = td->tet + 4 * t;
+            double D[3][3];
+            for (int k = 0; k < 3; ++k)
+                for (int i = 0; i < 3; ++i) D[i][k] = X[3 * v[k + 1] + i] - X[3 * v[0] + i];
+            const double c00 = D[1][1] * D[2][2] - D[1][2] * D[2][1], c01 = D[1][2] * D[2][0] - D[1][0] * D[2][2],
+                         c02 = D[1][0] * D[2][1] - D[1][1] * D[2][0];
+            const double det = D[0][0] * c00 + D[0][1] * c01 + D[0][2] * c02;
+            if (!(det > 0)) return set_error(CIPC_ERR_INVALID_ARG, "tet setup: tetrahedron %d is degenerate or inverted", t);
+            const double inv[9] = {c00 / det,
+                                   (D[0][2] * D[2][1] - D[0][1] * D[2][2]) / det,
+                                   (D[0][1] * D[1][2] - D[0][2] * D[1][1]) / det,
+                                   c01 / det,
+                                   (D[0][0] * D[2][2] - D[0][2] * D[2][0]) / det,
+                                   (D[0][2] * D[1][0] - D[0][0] * D[1][2]) / det,
+                                   c02 / det,
+                                   (D[0][1] * D[2][0] - D[0][0] * D[2][1]) / det,
+                                   (D[0][0] * D[1][1] - D[0][1] * D[1][0]) / det};
+            S.tet.insert(S.tet.end(), v, v + 4);
+            S.tDinv.insert(S.tDinv.end(), inv, inv + 9);
+            const double vol = det / 6;
+            S.tvol.push_back(vol);
+            const double mp = vol * td->rho / 4;
+            for (int k = 0; k < 4; ++k) {
+                S.mass[v[k]] += mp;
+                for (int d = 0; d < 3; ++d) S.b[3 * v[k] + d] += mp * gravity[d];
+            }
+        }
     }
     S.lam = E * nu / (1 - nu * nu);
     S.mu = E / (2 * (1 + nu));
@@ -242,6 +309,10 @@ int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* t
     for (int e = 0; e < nrh; ++e)
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) adj[S.rhinge[3 * e + a]].push_back(S.rhinge[3 * e + b]);
+    const int ntet = (int)S.tet.size() / 4;
+    for (int e = 0; e < ntet; ++e)
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b) adj[S.tet[4 * e + a]].push_back(S.tet[4 * e + b]);
     int K = 1;
     for (int i = 0; i < nv; ++i) {
         std::sort(adj[i].begin(), adj[i].end());
@@ -279,6 +350,10 @@ int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* t
     for (int e = 0; e < nrh; ++e)
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) S.rhinge_slot[9 * e + 3 * a + b] = slot(S.rhinge[3 * e + a], S.rhinge[3 * e + b]);
+    S.tet_slot.resize(16 * ntet);
+    for (int e = 0; e < ntet; ++e)
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b) S.tet_slot[16 * e + 4 * a + b] = slot(S.tet[4 * e + a], S.tet[4 * e + b]);
     return CIPC_OK;
 }
 
@@ -329,7 +404,11 @@ int sim_upload(Sim* s, const HostScene& S)
     UP(s->hinge_slot, S.hinge_slot)
     UP(s->rseg, S.rseg) UP(s->rhinge, S.rhinge) UP(s->rseg_slot, S.rseg_slot) UP(s->rhinge_slot, S.rhinge_slot)
     UP(s->rinfo, S.rinfo) UP(s->rhinfo, S.rhinfo)
+    UP(s->tet, S.tet) UP(s->tet_slot, S.tet_slot) UP(s->tDinv, S.tDinv) UP(s->tvol, S.tvol)
 #undef UP
+    s->ntet = (int)S.tvol.size();
+    s->tlam = S.tlam;
+    s->tmu = S.tmu;
     s->nrs = (int)S.rseg.size() / 2;
     s->nrh = (int)S.rhinge.size() / 3;
     s->codim0 = S.codim0;
@@ -355,10 +434,11 @@ int sim_upload(Sim* s, const HostScene& S)
 }
 
 int sim_create(Sim** out, int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
-               double thickness, const double* gravity, double bendMult, int nh_model, const CodimDesc* cd)
+               double thickness, const double* gravity, double bendMult, int nh_model, const CodimDesc* cd,
+               const TetDesc* td)
 {
     HostScene S;
-    int rc = build_host_scene(S, nv, X, nt, tri, rho, E, nu, thickness, gravity, bendMult, nh_model, cd);
+    int rc = build_host_scene(S, nv, X, nt, tri, rho, E, nu, thickness, gravity, bendMult, nh_model, cd, td);
     if (rc != CIPC_OK) return rc;
     rc = ensure_device();
     if (rc != CIPC_OK) return rc;

@@ -113,6 +113,7 @@ __global__ void k_kappa_flag(int n, const int* kind, const int4* verts, const do
 static int eval_energy(Sim* s, const double* x, double* E, bool* ok)
 {
     const int worst = nblk(s->nv, 256) + 2 * nblk(s->nt, 128) + nblk(s->nh, 128) + nblk(s->nrs, 128) + nblk(s->nrh, 128) +
+                      nblk(s->ntet, 128) +
                       (s->prm.withCollision ? nblk(s->ncon, 128) + nblk(s->nfric, 128) : 0) + 16;
     if ((int)s->red.n < worst + 16) {
         cudaStreamSynchronize(s->stream);
@@ -300,14 +301,14 @@ int sim_step(Sim* s, StepStats* st)
         // line search (IMPLICIT_EULER.h:9-149)
         cudaMemcpyAsync(s->xprev.p, s->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
         double alpha = 1.0;
-        if (s->sl.k0 > 0) {
-            // strain-limit feasibility first (IMPLICIT_EULER.h:74-94): halve until
-            // every stretch is inside the limits
+        if (s->sl.k0 > 0 || s->ntet > 0) {
+            // elastic feasibility first (IMPLICIT_EULER.h:74-94): halve until every
+            // stretch is inside the limits and no tetrahedron is inverted
             for (int k = 0;; ++k) {
-                if (k > 200) return set_error(CIPC_ERR_NOT_CONVERGED, "no strain-feasible step");
+                if (k > 200) return set_error(CIPC_ERR_NOT_CONVERGED, "no feasible step");
                 k_axpby<<<nblk(n3, 256), 256, 0, str>>>(n3, s->xprev.p, alpha, s->dir.p, s->x.p);
                 bool feas = true;
-                if ((rc = strain_feasible(s, s->x.p, &feas))) return rc;
+                if ((rc = elastic_feasible(s, s->x.p, &feas))) return rc;
                 if (feas) break;
                 alpha /= 2;
             }
@@ -448,12 +449,12 @@ void sim_destroy(Sim* s)
     pcg_release(s);
     for (DBuf<int>* b : {&s->tri, &s->hinge, &s->bnode, &s->bedge, &s->btri, &s->dbc_idx, &s->col,
                          &s->diag, &s->tri_slot, &s->hinge_slot, &s->ckind, &s->cmult, &s->fkind, &s->fmult,
-                         &s->rseg, &s->rhinge, &s->rseg_slot, &s->rhinge_slot,
+                         &s->rseg, &s->rhinge, &s->rseg_slot, &s->rhinge_slot, &s->tet, &s->tet_slot,
                          &s->pkind})
         b->release();
     for (DBuf<double>* b : {&s->P, &s->vol, &s->hinfo, &s->mass, &s->b, &s->X0, &s->dbc_tgt, &s->x, &s->xn, &s->xt,
                             &s->v, &s->g, &s->dir, &s->xprev, &s->rhs, &s->disp, &s->fw, &s->fT, &s->flam, &s->pdiag,
-                            &s->red, &s->pd2, &s->rinfo, &s->rhinfo})
+                            &s->red, &s->pd2, &s->rinfo, &s->rhinfo, &s->tDinv, &s->tvol, &s->sl_prev})
         b->release();
     s->dbc.release();
     s->proj.release();
@@ -511,6 +512,42 @@ extern "C" int cipc_sim_create_codim(int nv, const double* X, int nt, const int*
     cd.part_thickness = codim->particle_thickness;
     Sim* s = nullptr;
     int rc = sim_create(&s, nv, X, nt, tri, rho, E, nu, thickness, gravity, bend_stiff_mult, membrane_model, &cd);
+    if (rc) return rc;
+    *out = new cipc_sim{s};
+    return CIPC_OK;
+}
+
+extern "C" int cipc_sim_create_full(int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
+                                    double thickness, const double* gravity, double bend_stiff_mult,
+                                    int membrane_model, const cipc_codim_desc* codim, const cipc_tet_desc* tets,
+                                    cipc_sim** out)
+{
+    if (!out || !gravity) return set_error(CIPC_ERR_INVALID_ARG, "cipc_sim_create_full: null argument");
+    if (nv >= (1 << 21) - 1) return set_error(CIPC_ERR_INVALID_ARG, "cipc_sim_create_full: at most 2^21-2 vertices");
+    CodimDesc cd;
+    if (codim) {
+        cd.nseg = codim->n_segments;
+        cd.seg = codim->segments;
+        cd.rod_E = codim->rod_E;
+        cd.rod_rho = codim->rod_rho;
+        cd.rod_thickness = codim->rod_thickness;
+        cd.rod_bend_mult = codim->rod_bend_mult;
+        cd.npart = codim->n_particles;
+        cd.part = codim->particles;
+        cd.part_rho = codim->particle_rho;
+        cd.part_thickness = codim->particle_thickness;
+    }
+    TetDesc td;
+    if (tets) {
+        td.ntet = tets->n_tets;
+        td.tet = tets->tets;
+        td.E = tets->E;
+        td.nu = tets->nu;
+        td.rho = tets->rho;
+    }
+    Sim* s = nullptr;
+    int rc = sim_create(&s, nv, X, nt, tri, rho, E, nu, thickness, gravity, bend_stiff_mult, membrane_model,
+                        codim ? &cd : nullptr, tets ? &td : nullptr);
     if (rc) return rc;
     *out = new cipc_sim{s};
     return CIPC_OK;

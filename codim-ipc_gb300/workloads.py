@@ -336,3 +336,28 @@ def stacked_shells(n=180, layers=8, size=1.0, gap=5e-3, jitter=1e-3, plate_n=21,
     dbc = np.arange(offs[layers], X.shape[0], dtype=np.int32)
     top = np.arange(offs[layers + 1], X.shape[0], dtype=np.int32)
     return X, T, dbc, top
+
+
+def tet_box(n=3, size=0.1, center=(0.0, 0.0, 0.0)):
+    """Cube (edge `size`) of n^3 cells, each split into 6 tetrahedra around its
+    main diagonal (Kuhn subdivision, conforming across cells), all positively
+    oriented.  Returns X ((n+1)^3, 3) and tets (6 n^3, 4)."""
+    import itertools
+    c = np.asarray(center, float)
+    h = size / n
+    idx = lambda i, j, k: (i * (n + 1) + j) * (n + 1) + k
+    X = np.array([[i * h, j * h, k * h] for i in range(n + 1) for j in range(n + 1) for k in range(n + 1)])
+    X += c - size / 2
+    tets = []
+    for i, j, k in itertools.product(range(n), range(n), range(n)):
+        for perm in itertools.permutations(range(3)):
+            p = [i, j, k]
+            v = [idx(*p)]
+            for ax in perm:
+                p[ax] += 1
+                v.append(idx(*p))
+            a, b, cc, d = (X[q] for q in v)
+            if np.linalg.det(np.column_stack([b - a, cc - a, d - a])) < 0:
+                v[1], v[2] = v[2], v[1]
+            tets.append(v)
+    return X, np.array(tets, np.int32)

@@ -206,6 +206,21 @@ typedef struct cipc_codim_desc {
 int cipc_sim_create_codim(int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
                           double thickness, const double* gravity, double bend_stiff_mult, int membrane_model,
                           const cipc_codim_desc* codim, cipc_sim** out);
+/* Volumetric tetrahedra (the drivers' add_object_3D + initialize of a tet mesh:
+ * FEM.Compute_Vol_And_Inv_Basis, DEFORMATION_GRADIENT.h:39-76; lumped mass;
+ * Neo-Hookean material, NEOHOOKEAN.h, in the step via INC_POTENTIAL.h:97-109,
+ * 228-229, 354-364).  Their surface triangles (Find_Surface_TriMesh,
+ * MESHIO.h:486-544) take part in contact ahead of the shell triangles
+ * (IMPLICIT_EULER.h:235-241).  Tetrahedra must be positively oriented. */
+typedef struct cipc_tet_desc {
+    int n_tets;
+    const int32_t* tets; /* 4 vertex indices per tetrahedron */
+    double E, nu, rho;
+} cipc_tet_desc;
+/* Shell + optional codimensional parts + optional tetrahedra (either may be NULL). */
+int cipc_sim_create_full(int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
+                         double thickness, const double* gravity, double bend_stiff_mult, int membrane_model,
+                         const cipc_codim_desc* codim, const cipc_tet_desc* tets, cipc_sim** out);
 int cipc_sim_destroy(cipc_sim* sim);
 /* Offset-IPC barrier stiffness; replaces FEM.DiscreteShell.Initialize_OIPC
  * (DISCRETE_SHELL.h:555-577, export :1103).  Writes (kappa, kappa_max) and dhat^2. */

@@ -24,7 +24,7 @@ REF_ROOT = os.environ.get("CIPC_REFERENCE_ROOT", "/root/reference")
 
 def build_oracle(force=False):
     out = os.path.join(HERE, "liboracle.so")
-    srcs = [os.path.join(HERE, f) for f in ("oracle_math.cpp", "oracle_api.cpp", "oracle_shell.cpp", "oracle_learned.cpp", "oracle_rod.cpp", "oracle_sl.cpp")]
+    srcs = [os.path.join(HERE, f) for f in ("oracle_math.cpp", "oracle_api.cpp", "oracle_shell.cpp", "oracle_learned.cpp", "oracle_rod.cpp", "oracle_sl.cpp", "oracle_tet.cpp")]
     srcs = [s for s in srcs if os.path.exists(s)]
     deps = srcs + [os.path.join(HERE, f) for f in os.listdir(HERE) if f.endswith(".h")]
     if not force and os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):

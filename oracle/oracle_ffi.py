@@ -125,7 +125,8 @@ def set_threads(n):
 class Shell:
     """The oracle's shell scene and time step (oracle_shell.cpp)."""
 
-    def __init__(self, X, T, rho, E, nu, thickness, gravity=(0.0, -9.81, 0.0), bend_mult=1.0, nh=True, codim=None):
+    def __init__(self, X, T, rho, E, nu, thickness, gravity=(0.0, -9.81, 0.0), bend_mult=1.0, nh=True, codim=None,
+                 tets=None):
         L = lib()
         L.orc_shell_create.restype = _P
         L.orc_shell_create.argtypes = [ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_double, ctypes.c_double,
@@ -149,7 +150,23 @@ class Shell:
         T = _c(T, np.int32)
         g = _c(gravity, np.float64)
         T = T.reshape(-1, 3)
-        if codim is None:
+        if tets is not None:
+            L.orc_shell_create_full.restype = _P
+            L.orc_shell_create_full.argtypes = [ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_double, ctypes.c_double,
+                                                ctypes.c_double, ctypes.c_double, _P, ctypes.c_double, ctypes.c_int,
+                                                ctypes.c_int, _P, ctypes.c_int, _P, _P, ctypes.c_int, _P, _P]
+            cd = codim or {}
+            seg = _c(cd.get("segments", np.zeros((0, 2))), np.int32).reshape(-1, 2)
+            par = _c(cd.get("particles", np.zeros(0)), np.int32).reshape(-1)
+            prm = np.array([cd.get("rod_E", 0.0), cd.get("rod_rho", 0.0), cd.get("rod_thickness", 0.0),
+                            cd.get("rod_bend_mult", 1.0), cd.get("particle_rho", 0.0), cd.get("particle_thickness", 0.0)])
+            tt = _c(tets["tets"], np.int32).reshape(-1, 4)
+            tm = np.array([tets["E"], tets["nu"], tets["rho"]], float)
+            self.h = L.orc_shell_create_full(self.X.shape[0], _p(self.X), T.shape[0], _p(T), rho, E, nu, thickness,
+                                             _p(g), bend_mult, 1 if nh else 0, seg.shape[0], _p(seg), par.shape[0],
+                                             _p(par), _p(prm) if codim is not None else None, tt.shape[0], _p(tt),
+                                             _p(tm))
+        elif codim is None:
             self.h = L.orc_shell_create(self.X.shape[0], _p(self.X), T.shape[0], _p(T), rho, E, nu, thickness, _p(g),
                                         bend_mult, 1 if nh else 0)
         else:
@@ -338,4 +355,17 @@ def strain_limit_elem(x9, P, kh, s, s_hat, kappa_s, project=True):
     E = lb.orc_sl_elem(_p(_c(x9, np.float64)), _p(_c(P, np.float64)), kh, _p(_c(s, np.float64)),
                        _p(_c(s_hat, np.float64)), _p(_c(kappa_s, np.float64)), 1 if project else 0, _p(g), _p(H),
                        _p(ok))
+    return E, g, H, bool(ok[0])
+
+
+def tet_nh_elem(x12, Dinv, w, lam, mu, project=True):
+    """(E, g[12], H[12x12], valid) of one Neo-Hookean tetrahedron, w = h^2 vol."""
+    lb = lib()
+    lb.orc_tet_nh.restype = ctypes.c_double
+    lb.orc_tet_nh.argtypes = [_P, _P, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, _P, _P, _P]
+    g = np.zeros(12)
+    H = np.zeros((12, 12))
+    ok = np.zeros(1, np.int32)
+    E = lb.orc_tet_nh(_p(_c(x12, np.float64)), _p(_c(Dinv, np.float64)), w, lam, mu, 1 if project else 0, _p(g),
+                      _p(H), _p(ok))
     return E, g, H, bool(ok[0])

@@ -14,6 +14,7 @@
 #include <omp.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -244,8 +245,29 @@ static void bending_grad_d(const double* x, double thetabar, double c, double* g
 // :131-216 (hinge stencils and rest data), MESHIO.h:728-767 (surface primitives),
 // DISCRETE_SHELL.h:555-577 (offset-IPC stiffness).
 // ---------------------------------------------------------------------------
+// surface triangles of a tetrahedral mesh (Find_Surface_TriMesh, MESHIO.h:486-544):
+// the outward faces (0,2,1), (0,3,2), (0,1,3), (1,2,3) of every tetrahedron as
+// keys; a key without a reversed twin (in any rotation) is on the surface; key order
+static std::vector<int> tet_surface(int ntet, const int* tet)
+{
+    std::set<std::array<int, 3>> keys;
+    for (int t = 0; t < ntet; ++t) {
+        const int* v = tet + 4 * t;
+        keys.insert({v[0], v[2], v[1]});
+        keys.insert({v[0], v[3], v[2]});
+        keys.insert({v[0], v[1], v[3]});
+        keys.insert({v[1], v[2], v[3]});
+    }
+    std::vector<int> out;
+    for (const auto& k : keys)
+        if (!keys.count({k[2], k[1], k[0]}) && !keys.count({k[1], k[0], k[2]}) && !keys.count({k[0], k[2], k[1]}))
+            out.insert(out.end(), k.begin(), k.end());
+    return out;
+}
+
 static void shell_init(Shell& S, int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
-                       double thickness, const double* gravity, double bendMult, int nh_model)
+                       double thickness, const double* gravity, double bendMult, int nh_model, int ntet = 0,
+                       const int* tets = nullptr)
 {
     S.nv = nv;
     S.X0.assign(X, X + 3 * nv);
@@ -267,12 +289,15 @@ static void shell_init(Shell& S, int nv, const double* X, int nt, const int* tri
         e2t[{v[1], v[2]}] = t;
         e2t[{v[2], v[0]}] = t;
     }
-    // surface primitives: an edge keeps the orientation of its first occurrence
+    // surface primitives over the tetrahedral surface then the shell
+    // (IMPLICIT_EULER.h:235-241): an edge keeps the orientation of its first occurrence
+    std::vector<int> ctri = tet_surface(ntet, tets);
+    ctri.insert(ctri.end(), S.tri.begin(), S.tri.end());
     std::set<std::pair<int, int>> es;
     std::vector<char> isb(nv, 0);
     S.btri.clear();
-    for (int t = 0; t < nt; ++t) {
-        const int* v = &S.tri[3 * t];
+    for (int t = 0; t < (int)ctri.size() / 3; ++t) {
+        const int* v = &ctri[3 * t];
         for (int k = 0; k < 3; ++k) S.btri.push_back(v[k]);
         for (int k = 0; k < 3; ++k) {
             int a = v[k], b = v[(k + 1) % 3];
@@ -487,6 +512,61 @@ static double rod_terms(const Shell& S, const double* x, double h, double* g, As
         if (A) A->add_block(v, 3, H);
     }
     return E;
+}
+
+extern "C" double orc_tet_nh(const double* x12, const double* Dinv, double w, double lam, double mu, int project,
+                              double* g, double* H, int* valid);
+
+// volumetric Neo-Hookean tetrahedra (INC_POTENTIAL.h:97-109, 228-229, 354-364);
+// *valid cleared by an inverted tetrahedron
+static double tet_terms(const Shell& S, const double* x, double h, double* g, Asm* A, bool* valid)
+{
+    double E = 0;
+    const int nt = (int)S.tvol.size();
+    for (int t = 0; t < nt; ++t) {
+        const int* v = &S.tet[4 * t];
+        if (all_dbc(S, v, 4)) continue;
+        double xe[12], ge[12], H[144];
+        gather(x, v, 4, xe);
+        int ok = 1;
+        E += orc_tet_nh(xe, &S.tDinv[9 * t], h * h * S.tvol[t], S.tlam, S.tmu, 1, g ? ge : nullptr, A ? H : nullptr,
+                        &ok);
+        if (!ok && valid) *valid = false;
+        if (g) scatter_add(g, v, 4, ge);
+        if (A && ok) A->add_block(v, 4, H);
+    }
+    return E;
+}
+
+// tetrahedra (DEFORMATION_GRADIENT.h:39-76): Dm^-1, vol = det Dm / 6, mass vol rho / 4
+static void tet_init(Shell& S, const double* X, int ntet, const int* tets, double E, double nu, double rho,
+                     const double* gravity)
+{
+    S.tlam = E * nu / ((1 + nu) * (1 - 2 * nu));
+    S.tmu = E / (2 * (1 + nu));
+    for (int t = 0; t < ntet; ++t) {
+        const int* v = tets + 4 * t;
+        double D[3][3];
+        for (int k = 0; k < 3; ++k)
+            for (int i = 0; i < 3; ++i) D[i][k] = X[3 * v[k + 1] + i] - X[3 * v[0] + i];
+        const double c00 = D[1][1] * D[2][2] - D[1][2] * D[2][1], c01 = D[1][2] * D[2][0] - D[1][0] * D[2][2],
+                     c02 = D[1][0] * D[2][1] - D[1][1] * D[2][0];
+        const double det = D[0][0] * c00 + D[0][1] * c01 + D[0][2] * c02;
+        const double inv[9] = {c00 / det, (D[0][2] * D[2][1] - D[0][1] * D[2][2]) / det,
+                               (D[0][1] * D[1][2] - D[0][2] * D[1][1]) / det, c01 / det,
+                               (D[0][0] * D[2][2] - D[0][2] * D[2][0]) / det,
+                               (D[0][2] * D[1][0] - D[0][0] * D[1][2]) / det, c02 / det,
+                               (D[0][1] * D[2][0] - D[0][0] * D[2][1]) / det,
+                               (D[0][0] * D[1][1] - D[0][1] * D[1][0]) / det};
+        S.tet.insert(S.tet.end(), v, v + 4);
+        S.tDinv.insert(S.tDinv.end(), inv, inv + 9);
+        S.tvol.push_back(det / 6);
+        const double mp = det / 6 * rho / 4;
+        for (int k = 0; k < 4; ++k) {
+            S.mass[v[k]] += mp;
+            for (int d = 0; d < 3; ++d) S.b[3 * v[k] + d] += mp * gravity[d];
+        }
+    }
 }
 
 extern "C" double orc_sl_elem(const double* x9, const double* P, double kh, const double* s, const double* s_hat,
@@ -1386,6 +1466,7 @@ static double total_energy(const Ctx& C, const double* x, const std::vector<Con>
     }
     bool good = true;
     E += strain_terms(S, x, C.P.h, nullptr, nullptr, &good);
+    E += tet_terms(S, x, C.P.h, nullptr, nullptr, &good);
     if (C.P.withCollision) good = barrier_terms(S, x, cs, C.P.dHat2, C.P.xi, C.kappa, &E, nullptr, nullptr) && good;
     if (C.P.withCollision && C.P.mu > 0) friction_terms(F, x, C.xn, C.P.epsv2 * C.P.h * C.P.h, C.P.mu, &E, nullptr, nullptr);
     if (ok) *ok = good;
@@ -1400,6 +1481,7 @@ static void total_grad(const Ctx& C, const double* x, const std::vector<Con>& cs
     for (int i = 0; i < n; ++i) g[i] = 0;
     elastic_grad_hess(S, x, C.P.h, g, A);
     strain_terms(S, x, C.P.h, g, A, nullptr);
+    tet_terms(S, x, C.P.h, g, A, nullptr);
     for (int i = 0; i < S.nv; ++i)
         for (int d = 0; d < 3; ++d) g[3 * i + d] += S.mass[i] * (x[3 * i + d] - C.xtilde[3 * i + d]);
     const std::vector<char>& proj = C.proj.empty() ? S.dbc : C.proj;
@@ -1500,12 +1582,13 @@ static void shell_step(Shell& S, const StepParams& P_in, double* x, double* v, d
         // line search (IMPLICIT_EULER.h:9-149)
         xprev.assign(x, x + n);
         double alpha = 1.0;
-        if (S.sl_kappa[0] > 0) {
-            // strain-limit feasibility first (IMPLICIT_EULER.h:74-94)
+        if (S.sl_kappa[0] > 0 || !S.tvol.empty()) {
+            // elastic feasibility first (IMPLICIT_EULER.h:74-94)
             for (;;) {
                 for (int i = 0; i < n; ++i) x[i] = xprev[i] + alpha * sol[i];
                 bool feas = true;
                 strain_terms(S, x, P.h, nullptr, nullptr, &feas);
+                tet_terms(S, x, P.h, nullptr, nullptr, &feas);
                 if (feas) break;
                 alpha /= 2;
             }
@@ -1645,6 +1728,20 @@ void* orc_shell_create_codim(int nv, const double* X, int nt, const int* tri, do
     Shell* S = new Shell();
     shell_init(*S, nv, X, nt, tri, rho, E, nu, thickness, gravity, bendMult, nh_model);
     codim_init(*S, X, nseg, seg, codim[0], codim[1], codim[2], codim[3], npart, part, codim[4], codim[5], gravity);
+    return S;
+}
+
+// shell + optional codimensional parts (codim null: none) + tetrahedra with
+// material tetmat = (E, nu, rho)
+void* orc_shell_create_full(int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
+                            double thickness, const double* gravity, double bendMult, int nh_model, int nseg,
+                            const int* seg, int npart, const int* part, const double* codim, int ntet,
+                            const int* tets, const double* tetmat)
+{
+    Shell* S = new Shell();
+    shell_init(*S, nv, X, nt, tri, rho, E, nu, thickness, gravity, bendMult, nh_model, ntet, tets);
+    if (codim) codim_init(*S, X, nseg, seg, codim[0], codim[1], codim[2], codim[3], npart, part, codim[4], codim[5], gravity);
+    if (ntet) tet_init(*S, X, ntet, tets, tetmat[0], tetmat[1], tetmat[2], gravity);
     return S;
 }
 

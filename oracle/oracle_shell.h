@@ -40,6 +40,10 @@ struct Shell {
     // isotropic strain limiting (INEXT.h): the reference's s, sHat, kappa_s pairs;
     // off while sl_kappa[0] == 0
     double sl_s[2] = {1.01, 0}, sl_shat[2] = {1, 1}, sl_kappa[2] = {0, 0};
+    // volumetric Neo-Hookean tetrahedra: vertices (4), Dm^-1 (9, row-major), volume
+    std::vector<int> tet;
+    std::vector<double> tDinv, tvol;
+    double tlam = 0, tmu = 0;
 };
 
 struct StepParams {
