@@ -191,13 +191,20 @@ __global__ void k_lp_feat(LpSys<VT, CT> S, const float* Dn, const int* ncnt, con
 }
 
 
-// P = Cm E Cm^T with Cm = [[e0,0,0],[o3,e1,0],[o4,o5,e2]], e_a = exp(0.5 clamp(o_a, -8, 8))
+// P = Cm E Cm^T with Cm = [[e0,0,0],[l3,e1,0],[l4,l5,e2]], e_a = exp(0.5 clamp(o_a, -2, 2)),
+// l_a = clamp(o_a, -1, 1): the correction can rescale a block by at most e^2 and
+// shear it by a bounded amount, so no network output makes PCG arbitrarily worse
+// than block Jacobi
+constexpr float kLpDiagClamp = 2.f, kLpOffClamp = 1.f;
 __device__ __forceinline__ void lp_block(const float* o, const float* E, float* P, float* Cout)
 {
     float e[3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) e[a] = expf(0.5f * fminf(8.f, fmaxf(-8.f, o[a])));
-    const float C[9] = {e[0], 0.f, 0.f, o[3], e[1], 0.f, o[4], o[5], e[2]};
+    for (int a = 0; a < 3; ++a) e[a] = expf(0.5f * fminf(kLpDiagClamp, fmaxf(-kLpDiagClamp, o[a])));
+    const float l3 = fminf(kLpOffClamp, fmaxf(-kLpOffClamp, o[3]));
+    const float l4 = fminf(kLpOffClamp, fmaxf(-kLpOffClamp, o[4]));
+    const float l5 = fminf(kLpOffClamp, fmaxf(-kLpOffClamp, o[5]));
+    const float C[9] = {e[0], 0.f, 0.f, l3, e[1], 0.f, l4, l5, e[2]};
     float CE[9];
 #pragma unroll
     for (int r = 0; r < 3; ++r)
@@ -470,10 +477,11 @@ __global__ void k_lp_out_bwd(int nv, const float* o, const float* E, const float
     for (int x = 0; x < 3; ++x)
         for (int y = 0; y < 3; ++y) dC[3 * x + y] = S[3 * x] * CE[y] + S[3 * x + 1] * CE[3 + y] + S[3 * x + 2] * CE[6 + y];
     float* d = dout + (size_t)kLpOut * i;
-    for (int q = 0; q < 3; ++q) d[q] = (oo[q] > -8.f && oo[q] < 8.f) ? dC[4 * q] * 0.5f * C[4 * q] : 0.f;
-    d[3] = dC[3];
-    d[4] = dC[6];
-    d[5] = dC[7];
+    for (int q = 0; q < 3; ++q)
+        d[q] = (oo[q] > -kLpDiagClamp && oo[q] < kLpDiagClamp) ? dC[4 * q] * 0.5f * C[4 * q] : 0.f;
+    d[3] = fabsf(oo[3]) < kLpOffClamp ? dC[3] : 0.f;
+    d[4] = fabsf(oo[4]) < kLpOffClamp ? dC[6] : 0.f;
+    d[5] = fabsf(oo[5]) < kLpOffClamp ? dC[7] : 0.f;
 }
 
 // din_i (+)= W^T dout_i, W (Ho x Hi)
@@ -753,10 +761,11 @@ __global__ void k_lp_out_bwd_G(int nv, const float* o, const float* E, const flo
     for (int x = 0; x < 3; ++x)
         for (int y = 0; y < 3; ++y) dC[3 * x + y] = S[3 * x] * CE[y] + S[3 * x + 1] * CE[3 + y] + S[3 * x + 2] * CE[6 + y];
     float* d = dout + (size_t)kLpOut * i;
-    for (int q = 0; q < 3; ++q) d[q] = (oo[q] > -8.f && oo[q] < 8.f) ? dC[4 * q] * 0.5f * C[4 * q] : 0.f;
-    d[3] = dC[3];
-    d[4] = dC[6];
-    d[5] = dC[7];
+    for (int q = 0; q < 3; ++q)
+        d[q] = (oo[q] > -kLpDiagClamp && oo[q] < kLpDiagClamp) ? dC[4 * q] * 0.5f * C[4 * q] : 0.f;
+    d[3] = fabsf(oo[3]) < kLpOffClamp ? dC[3] : 0.f;
+    d[4] = fabsf(oo[4]) < kLpOffClamp ? dC[6] : 0.f;
+    d[5] = fabsf(oo[5]) < kLpOffClamp ? dC[7] : 0.f;
 }
 
 template <typename T>

@@ -40,7 +40,7 @@ static const int kNeedScratch = 1000;
 // an enormous step (the step-size search then halves its trial step) or
 // primitives far larger than the cells
 static const int kSpanTooLarge = 1001;
-static const unsigned long long kMaxGridEntries = 1ull << 27;
+static const unsigned long long kMaxGridEntries = 1ull << 25;
 
 // ---------------------------------------------------------------------------
 // exclusive scan of int counts (three-phase block scan, recursive over blocks)

@@ -14,7 +14,7 @@
 //   h0 = relu(W0 x + b0)
 //   layer l: g_i = sum_j a_ij h_j / s_i ; c_i = mean over constraints touching
 //     i of the constraint's mean h ; h <- relu(A h + B g + C c + b) + h
-//   o = Wo h + bo (6) ; e_a = exp(0.5 clamp(o_a, -8, 8))
+//   o = Wo h + bo (6) ; e_a = exp(0.5 clamp(o_a, -2, 2)), l_a = clamp(o_a, -1, 1)
 //   Cm = [[e0,0,0],[o3,e1,0],[o4,o5,e2]] ; P_i = Cm D_i^-1 Cm^T ; z_i = P_i r_i
 // With Wo = 0, bo = 0 (the initial state) P_i = D_i^-1: plain block Jacobi.
 // Loss of one (H, r, p) triple, p = H^-1 r, kind 0:  L = 1 - (z.r)^2 / ((z.Hz)(r.p)),
@@ -225,8 +225,10 @@ void gather_con(const Graph& G, const Prep& P, int H, const std::vector<double>&
 void precond_block(const double* o, const double* E, double* Pm, double* Cm)
 {
     double e[3];
-    for (int a = 0; a < 3; ++a) e[a] = std::exp(0.5 * std::fmin(8.0, std::fmax(-8.0, o[a])));
-    const double C[9] = {e[0], 0, 0, o[3], e[1], 0, o[4], o[5], e[2]};
+    for (int a = 0; a < 3; ++a) e[a] = std::exp(0.5 * std::fmin(2.0, std::fmax(-2.0, o[a])));
+    double l[3];
+    for (int a = 0; a < 3; ++a) l[a] = std::fmin(1.0, std::fmax(-1.0, o[3 + a]));
+    const double C[9] = {e[0], 0, 0, l[0], e[1], 0, l[1], l[2], e[2]};
     double CE[9];
     for (int r = 0; r < 3; ++r)
         for (int q = 0; q < 3; ++q) CE[3 * r + q] = C[3 * r] * E[q] + C[3 * r + 1] * E[3 + q] + C[3 * r + 2] * E[6 + q];
@@ -459,12 +461,12 @@ double loss_grad(const Net& N, const Graph& G, const Prep& P, const double* r, c
             for (int y = 0; y < 3; ++y) dC[3 * x + y] = S[3 * x] * CE[y] + S[3 * x + 1] * CE[3 + y] + S[3 * x + 2] * CE[6 + y];
         double* d = &dout[(size_t)O * i];
         for (int q = 0; q < 3; ++q) {
-            const bool in = o[q] > -8.0 && o[q] < 8.0;
+            const bool in = o[q] > -2.0 && o[q] < 2.0;
             d[q] = in ? dC[4 * q] * 0.5 * C[4 * q] : 0.0;
         }
-        d[3] = dC[3];
-        d[4] = dC[6];
-        d[5] = dC[7];
+        d[3] = std::fabs(o[3]) < 1.0 ? dC[3] : 0.0;
+        d[4] = std::fabs(o[4]) < 1.0 ? dC[6] : 0.0;
+        d[5] = std::fabs(o[5]) < 1.0 ? dC[7] : 0.0;
     }
     wgrad(nv, O, H, dout, A.h[L], gWo, gbo);
     std::vector<double> dh((size_t)H * nv, 0);
