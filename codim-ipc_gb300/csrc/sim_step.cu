@@ -272,7 +272,10 @@ int sim_step(Sim* s, StepStats* st)
         if (useGD) {
             cudaMemcpyAsync(s->dir.p, s->rhs.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
         } else {
-            if (P.forcing) {
+            // the forcing term is not combined with the learned correction: its
+            // early-stopped solves (trained on tight ones) gave directions of
+            // ~100 m/s and Newton loops of 50+ iterations on the cloth-on-sphere scene
+            if (P.forcing && !(P.precond == 1 && s->learned)) {
                 const double gn = std::sqrt(sum_sq(s, s->rhs.p, n3));
                 double eta = 0.1;
                 if (gnorm_prev > 0) {

@@ -159,7 +159,8 @@ typedef struct cipc_step_params {
     int preconditioner;    /* 0 block-Jacobi, 1 learned correction when a model is set */
     int forcing;           /* 0: every Newton system to pcg_tol; 1: inexact Newton, the
                               Eisenstat-Walker forcing term (choice 2, gamma 0.9, alpha 2)
-                              clamped to [pcg_tol, 0.1], pcg_tol once RMS(step)/h < 10 tol */
+                              clamped to [pcg_tol, 0.1], pcg_tol once RMS(step)/h < 10 tol;
+                              ignored while the learned preconditioner is in use */
     int barrier_model;     /* CIPC_BARRIER_OFFSET (0, Advance_One_Step_IE_Hinge) or
                               CIPC_BARRIER_ELASTIC (1, Advance_One_Step_IE_Hinge_EIPC:
                               no offset, normalised barrier, kappa not adapted) */

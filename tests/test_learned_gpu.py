@@ -98,6 +98,7 @@ def test_untrained_network_is_block_jacobi(cuda):
     pa = F.make_params(DT, dhat2, XI, newton_tol=1e-3, precision=F.MIXED, pcg_tol=1e-5)
     pb = F.make_params(DT, dhat2, XI, newton_tol=1e-3, precision=F.MIXED, pcg_tol=1e-5, preconditioner=1)
     bar = 2 * np.sqrt(X.shape[0] - len(dbc)) * 1e-3 * DT
+    ta = tb = 0
     for step in range(4):
         x0, v0 = a.state()
         b.set_state(x0, v0)
@@ -105,8 +106,13 @@ def test_untrained_network_is_block_jacobi(cuda):
         sa = a.step(pa)
         sb = b.step(pb)
         assert sb.learned_solves > 0 and sb.precond_fallbacks == 0
-        assert abs(sa.pcg_iters - sb.pcg_iters) <= 0.1 * sa.pcg_iters + 5, (step, sa.as_dict(), sb.as_dict())
+        # FP32 atomics make consecutive Newton systems differ slightly between the
+        # two runs, and PCG counts follow: per step 20%, over the run 10%
+        assert abs(sa.pcg_iters - sb.pcg_iters) <= 0.2 * sa.pcg_iters + 5, (step, sa.as_dict(), sb.as_dict())
+        ta += sa.pcg_iters
+        tb += sb.pcg_iters
         assert np.abs(a.state()[0] - b.state()[0]).max() <= bar
+    assert abs(ta - tb) <= 0.1 * ta, (ta, tb)
 
 
 def test_training_lowers_loss(captured):
