@@ -136,8 +136,11 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p)
 // arrived.  acc[(epoch + 2) % 3] held the totals of reduction epoch - 1, which
 // every block has read before arriving here, so block 0 clears it for reduction
 // epoch + 2.  Returns false if the wait gave up (err set; the kernel returns).
-template <int N>
-__device__ __forceinline__ bool grid_allreduce(double (&v)[N], PcgScalars* d, unsigned int& epoch)
+// Warp-level sums run in the solver's precision AT (FP32 shuffles and adds in the
+// FP32 solver: this part's FP64 work otherwise competes for GB300's narrow FP64
+// pipe); block and grid sums are FP64.  The totals land in out.
+template <int N, typename AT>
+__device__ __forceinline__ bool grid_allreduce(const AT (&v)[N], double (&out)[N], PcgScalars* d, unsigned int& epoch)
 {
     static_assert(N >= 1 && N <= 4, "reduction width");
     __shared__ double sh[N][kPcgThreads / 32];
@@ -146,10 +149,10 @@ __device__ __forceinline__ bool grid_allreduce(double (&v)[N], PcgScalars* d, un
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < N; ++k) {
-        double a = v[k];
+        AT a = v[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-        if (lane == 0) sh[k][wid] = a;
+        if (lane == 0) sh[k][wid] = (double)a;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -187,7 +190,7 @@ __device__ __forceinline__ bool grid_allreduce(double (&v)[N], PcgScalars* d, un
     ++epoch;
     if (!ok) return false;
 #pragma unroll
-    for (int k = 0; k < N; ++k) v[k] = res[k];
+    for (int k = 0; k < N; ++k) out[k] = res[k];
     return true;
 }
 
@@ -210,7 +213,7 @@ __device__ __forceinline__ void precond_vertex(const PT* __restrict__ pinv, int 
 // them into q; returns the lane's share of x_c . H_c x_c.  All 4 lanes of the
 // group must call this together (gmask = the group's lanes, gbase = its first).
 template <int NV, typename VT, typename XT, typename G>
-__device__ __forceinline__ double con_apply_lane(const VT* __restrict__ H, size_t hs, int4 iv, int k, unsigned gmask,
+__device__ __forceinline__ XT con_apply_lane(const VT* __restrict__ H, size_t hs, int4 iv, int k, unsigned gmask,
                                                  int gbase, const G& pget, XT* q)
 {
     constexpr int M = 3 * NV;
@@ -224,8 +227,8 @@ __device__ __forceinline__ double con_apply_lane(const VT* __restrict__ H, size_
     for (int j = 0; j < NV; ++j)
 #pragma unroll
         for (int t = 0; t < 3; ++t) xs[3 * j + t] = __shfl_sync(gmask, xk[t], gbase + j);
-    if (!own) return 0.0;
-    double s = 0;
+    if (!own) return XT(0);
+    XT s = 0;
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
         const int p = 3 * k + r;
@@ -236,7 +239,7 @@ __device__ __forceinline__ double con_apply_lane(const VT* __restrict__ H, size_
             const int h = i * M - (i * (i - 1)) / 2 + (j - i);
             y += (XT)__ldg(H + (size_t)h * hs) * xs[m];
         }
-        s += (double)xk[r] * (double)y;
+        s += xk[r] * y;
         if (y != XT(0)) atomicAdd(q + 3 * me + r, y);
     }
     return s;
@@ -245,7 +248,7 @@ __device__ __forceinline__ double con_apply_lane(const VT* __restrict__ H, size_
 // apply phase: q_e, q_c = H p_k (p_k formed on the fly and stored for the owned
 // rows); returns this thread's share of (p_k, H p_k)
 template <typename VT, typename XT, typename PT>
-__device__ __forceinline__ double apply_phase(const PcgArgs<VT, XT, PT>& a, bool first, XT beta, XT* pk,
+__device__ __forceinline__ XT apply_phase(const PcgArgs<VT, XT, PT>& a, bool first, XT beta, XT* pk,
                                               const XT* pold)
 {
     const XT* z = a.z;
@@ -256,7 +259,7 @@ __device__ __forceinline__ double apply_phase(const PcgArgs<VT, XT, PT>& a, bool
     const int nrow = 3 * a.nv, ncon = a.ncon, nfric = a.nfric;
     const int cbeg = (nrow + 3) & ~3, cend = cbeg + 4 * ncon;
     const int total = cend + nfric;
-    double v = 0;
+    XT v = 0;  // this thread's share, in the solver's precision; block sums are FP64
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < total; w += gridDim.x * blockDim.x) {
         if (w < nrow) {
             // one scalar row of the elastic 3x3 block rows per thread: row 3i + r
@@ -274,7 +277,7 @@ __device__ __forceinline__ double apply_phase(const PcgArgs<VT, XT, PT>& a, bool
             const XT pw = pget(w);
             pk[w] = pw;
             a.qe[w] = acc;
-            v += (double)pw * (double)acc;
+            v += pw * acc;
         } else if (w < cbeg) {
             continue;
         } else if (w < cend) {
@@ -295,23 +298,24 @@ __device__ __forceinline__ double apply_phase(const PcgArgs<VT, XT, PT>& a, bool
             const int cnv = con_nv(a.fkind[c]);
             const int4 iv = a.fverts[c];
             const int id[4] = {iv.x, iv.y, iv.z, iv.w};
-            double s0 = 0, s1 = 0, s2 = 0;
+            XT s0 = 0, s1 = 0, s2 = 0;
             for (int q = 0; q < cnv; ++q) {
                 if (a.proj[id[q]]) continue;
-                const double wq = a.fw[4 * c + q];
-                s0 += wq * (double)pget(3 * id[q]);
-                s1 += wq * (double)pget(3 * id[q] + 1);
-                s2 += wq * (double)pget(3 * id[q] + 2);
+                const XT wq = (XT)a.fw[4 * c + q];
+                s0 += wq * pget(3 * id[q]);
+                s1 += wq * pget(3 * id[q] + 1);
+                s2 += wq * pget(3 * id[q] + 2);
             }
-            const double* T = a.fT + 6 * (size_t)c;
-            const double t0 = T[0] * s0 + T[1] * s1 + T[2] * s2, t1 = T[3] * s0 + T[4] * s1 + T[5] * s2;
-            const double m00 = a.fM[3 * c], m01 = a.fM[3 * c + 1], m11 = a.fM[3 * c + 2];
-            const double u0 = m00 * t0 + m01 * t1, u1 = m01 * t0 + m11 * t1;
+            const double* Td = a.fT + 6 * (size_t)c;
+            const XT T[6] = {(XT)Td[0], (XT)Td[1], (XT)Td[2], (XT)Td[3], (XT)Td[4], (XT)Td[5]};
+            const XT t0 = T[0] * s0 + T[1] * s1 + T[2] * s2, t1 = T[3] * s0 + T[4] * s1 + T[5] * s2;
+            const XT m00 = (XT)a.fM[3 * c], m01 = (XT)a.fM[3 * c + 1], m11 = (XT)a.fM[3 * c + 2];
+            const XT u0 = m00 * t0 + m01 * t1, u1 = m01 * t0 + m11 * t1;
             v += t0 * u0 + t1 * u1;
-            const double o0 = T[0] * u0 + T[3] * u1, o1 = T[1] * u0 + T[4] * u1, o2 = T[2] * u0 + T[5] * u1;
+            const XT o0 = T[0] * u0 + T[3] * u1, o1 = T[1] * u0 + T[4] * u1, o2 = T[2] * u0 + T[5] * u1;
             for (int q = 0; q < cnv; ++q) {
                 if (a.proj[id[q]]) continue;
-                const double wq = a.fw[4 * c + q];
+                const XT wq = (XT)a.fw[4 * c + q];
                 atomicAdd(a.qc + 3 * id[q], (XT)(wq * o0));
                 atomicAdd(a.qc + 3 * id[q] + 1, (XT)(wq * o1));
                 atomicAdd(a.qc + 3 * id[q] + 2, (XT)(wq * o2));
@@ -348,7 +352,7 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
                 v[1] += (double)r[c] * (double)r[c];
             }
         }
-        if (!grid_allreduce<2>(v, d, epoch)) return;
+        if (!grid_allreduce<2>(v, v, d, epoch)) return;
         tot[0] = v[0];
         tot[1] = v[1];
     }
@@ -375,17 +379,18 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
         const XT beta = first ? XT(0) : (XT)(rz / rz_prev);
         XT* pk = (k & 1) ? a.P1 : a.P0;
         const XT* pold = (k & 1) ? a.P0 : a.P1;
-        double va[1] = {apply_phase<VT, XT, PT>(a, first, beta, pk, pold)};
+        const XT va[1] = {apply_phase<VT, XT, PT>(a, first, beta, pk, pold)};
+        double vd[1];
         lap(0);
-        if (!grid_allreduce<1>(va, d, epoch)) return;
+        if (!grid_allreduce<1>(va, vd, d, epoch)) return;
         lap(1);
-        pq = va[0];
+        pq = vd[0];
         if (!(pq > 0 && pq < INFINITY)) {
             done = (pq == pq) ? 3 : 2;
             break;
         }
         const XT alpha = (XT)(rz / pq);
-        double vb[2] = {0, 0};
+        XT rz_t = 0, rr_t = 0;
         for (int i = gtid; i < a.nv; i += gstride) {
             XT r[3], z[3];
 #pragma unroll
@@ -400,12 +405,14 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 a.z[3 * i + c] = z[c];
-                vb[0] += (double)r[c] * (double)z[c];
-                vb[1] += (double)r[c] * (double)r[c];
+                rz_t += r[c] * z[c];
+                rr_t += r[c] * r[c];
             }
         }
+        const XT vb_t[2] = {rz_t, rr_t};
+        double vb[2];
         lap(3);
-        if (!grid_allreduce<2>(vb, d, epoch)) return;
+        if (!grid_allreduce<2>(vb_t, vb, d, epoch)) return;
         lap(4);
         tot[0] = vb[0];
         tot[1] = vb[1];
