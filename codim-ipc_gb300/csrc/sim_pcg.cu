@@ -66,8 +66,21 @@ __device__ __forceinline__ unsigned long long gtimer()
     return t;
 }
 
+// (z, p) pairs: iteration k reads z_k and p_{k-1} of a scalar row with one load
+template <typename XT>
+struct Pair;
+template <>
+struct Pair<float> {
+    using T = float2;
+};
+template <>
+struct Pair<double> {
+    using T = double2;
+};
+
 template <typename VT, typename XT, typename PT>
 struct PcgArgs {
+    using XT2 = typename Pair<XT>::T;
     int nv, ell_k;
     const int* col;
     const VT* val;
@@ -85,9 +98,7 @@ struct PcgArgs {
     const XT* b;
     XT* x;
     XT* r;
-    XT* z;
-    XT* P0;
-    XT* P1;
+    XT2* zp[2];  // iteration k reads zp[k % 2] = (z_k, p_{k-1}); writes p_k and z_{k+1} into zp[(k + 1) % 2]
     XT* qe;
     XT* qc;
     PcgScalars* d;
@@ -248,11 +259,16 @@ __device__ __forceinline__ XT con_apply_lane(const VT* __restrict__ H, size_t hs
 // apply phase: q_e, q_c = H p_k (p_k formed on the fly and stored for the owned
 // rows); returns this thread's share of (p_k, H p_k)
 template <typename VT, typename XT, typename PT>
-__device__ __forceinline__ XT apply_phase(const PcgArgs<VT, XT, PT>& a, bool first, XT beta, XT* pk,
-                                              const XT* pold)
+__device__ __forceinline__ XT apply_phase(const PcgArgs<VT, XT, PT>& a, XT beta,
+                                              const typename PcgArgs<VT, XT, PT>::XT2* zp,
+                                              typename PcgArgs<VT, XT, PT>::XT2* zp_next)
 {
-    const XT* z = a.z;
-    auto pget = [&](int j) -> XT { return first ? ldcg(z + j) : ldcg(z + j) + beta * ldcg(pold + j); };
+    // p_k = z_k + beta p_{k-1} (beta = 0 in the first iteration, where p_{-1} is
+    // never written: the pair's second half is ignored then)
+    auto pget = [&](int j) -> XT {
+        const auto v = ldcg(zp + j);
+        return beta == XT(0) ? v.x : v.x + beta * v.y;
+    };
     // work items: elastic scalar rows, then 4 lanes per contact constraint
     // (starting 4-aligned, so a constraint's lanes are 4 aligned lanes of one warp:
     // the grid stride is a multiple of 32), then friction constraints
@@ -275,7 +291,7 @@ __device__ __forceinline__ XT apply_phase(const PcgArgs<VT, XT, PT>& a, bool fir
                        (XT)__ldg(B + 2) * pget(3 * j + 2);
             }
             const XT pw = pget(w);
-            pk[w] = pw;
+            zp_next[w].y = pw;
             a.qe[w] = acc;
             v += pw * acc;
         } else if (w < cbeg) {
@@ -347,7 +363,7 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
             precond_vertex<XT, PT>(a.pinv, i, r, z);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                a.z[3 * i + c] = z[c];
+                a.zp[0][3 * i + c].x = z[c];
                 v[0] += (double)r[c] * (double)z[c];
                 v[1] += (double)r[c] * (double)r[c];
             }
@@ -377,9 +393,9 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
         }
         const bool first = (k == 0);
         const XT beta = first ? XT(0) : (XT)(rz / rz_prev);
-        XT* pk = (k & 1) ? a.P1 : a.P0;
-        const XT* pold = (k & 1) ? a.P0 : a.P1;
-        const XT va[1] = {apply_phase<VT, XT, PT>(a, first, beta, pk, pold)};
+        const auto* zp = a.zp[k & 1];
+        auto* zp_next = a.zp[(k + 1) & 1];
+        const XT va[1] = {apply_phase<VT, XT, PT>(a, beta, zp, zp_next)};
         double vd[1];
         lap(0);
         if (!grid_allreduce<1>(va, vd, d, epoch)) return;
@@ -396,7 +412,7 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const int j = 3 * i + c;
-                a.x[j] = ldcg(a.x + j) + alpha * ldcg(pk + j);
+                a.x[j] = ldcg(a.x + j) + alpha * ldcg(&zp_next[j].y);
                 r[c] = ldcg(a.r + j) - alpha * (ldcg(a.qe + j) + ldcg(a.qc + j));
                 a.r[j] = r[c];
                 a.qc[j] = 0;
@@ -404,7 +420,7 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
             precond_vertex<XT, PT>(a.pinv, i, r, z);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                a.z[3 * i + c] = z[c];
+                zp_next[3 * i + c].x = z[c];
                 rz_t += r[c] * z[c];
                 rr_t += r[c] * r[c];
             }
@@ -438,7 +454,7 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
 // ---------------------------------------------------------------------------
 namespace {
 
-constexpr int kVecs = 8;  // r, z, P0, P1, q_e, q_c, and b, x of the FP32 inner solve
+constexpr int kVecs = 9;  // r, (z, p) pairs x 2 (two vectors each), q_e, q_c, and b, x of the FP32 inner solve
 
 struct PcgState {
     DBuf<char> vec;              // kVecs vectors of 3 nv entries
@@ -536,11 +552,10 @@ int solve(Sim* s, const XT* b, XT* x, double tol, int maxit, int* iters, double*
     a.b = b;
     a.x = x;
     a.r = vecp(0);
-    a.z = vecp(1);
-    a.P0 = vecp(2);
-    a.P1 = vecp(3);
-    a.qe = vecp(4);
-    a.qc = vecp(5);
+    a.zp[0] = reinterpret_cast<typename PcgArgs<VT, XT, PT>::XT2*>(vecp(1));  // pairs span vectors 1-2
+    a.zp[1] = reinterpret_cast<typename PcgArgs<VT, XT, PT>::XT2*>(vecp(3));  // and 3-4
+    a.qe = vecp(5);
+    a.qc = vecp(6);
     a.d = st->dsc.p;
     a.tol = tol;
     a.maxit = maxit;
@@ -592,8 +607,8 @@ int pcg_fp32_io(Sim* s, float** b, float** x)
     int rc = state(s, &st);
     if (rc || (rc = ensure_vectors(s, st, sizeof(float)))) return rc;
     const size_t vbytes = ((3 * (size_t)s->nv * sizeof(float) + 255) & ~(size_t)255);
-    *b = reinterpret_cast<float*>(st->vec.p + 6 * vbytes);
-    *x = reinterpret_cast<float*>(st->vec.p + 7 * vbytes);
+    *b = reinterpret_cast<float*>(st->vec.p + 7 * vbytes);
+    *x = reinterpret_cast<float*>(st->vec.p + 8 * vbytes);
     return CIPC_OK;
 }
 
