@@ -338,7 +338,47 @@ struct CsArgs {
     double dHat, dh2;
     Grid G;
     ConSink S;
+    // FP32 boxes (lo xyz, hi xyz) of the boundary triangles and edges, rounded
+    // outward, and dHat rounded up: a conservative prefilter in front of the
+    // FP64 box test (see box_apart)
+    const float* tbox;
+    const float* ebox;
+    float dHat_f;
 };
+
+// FP32 boxes of n items of nvi vertices: lo rounded down, hi rounded up, so each
+// box contains the FP64 box of the item
+__global__ void k_item_boxes(int n, int nvi, const int* verts, const double* x, float* box)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (int k = 0; k < nvi; ++k) {
+        const int v = verts[nvi * t + k];
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = fmin(mn[d], x[3 * v + d]);
+            mx[d] = fmax(mx[d], x[3 * v + d]);
+        }
+    }
+    for (int d = 0; d < 3; ++d) {
+        box[6 * t + d] = __double2float_rd(mn[d]);
+        box[6 * t + 3 + d] = __double2float_ru(mx[d]);
+    }
+}
+
+// True only if the FP64 box test (any coordinate gap between the two boxes above
+// dHat) rejects the pair too: a, b contain the FP64 boxes, the rounded-down
+// difference bounds the real gap from below, and a gap above dHat rounded up to
+// float exceeds dHat by at least one float ulp, far more than the FP64 rounding of
+// the gap.  Candidates it keeps go through the unchanged FP64 tests, so the
+// constraint set is the same.
+__device__ __forceinline__ bool box_apart(const float* a, const float* b, float dh)
+{
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        if (__fsub_rd(a[k], b[3 + k]) > dh || __fsub_rd(b[k], a[3 + k]) > dh) return true;
+    return false;
+}
 
 __device__ __forceinline__ bool any_gt3(d3 a, double d) { return a.x > d || a.y > d || a.z > d; }
 __device__ __forceinline__ d3 vmin3(d3 a, d3 b) { return mk(fmin(a.x, b.x), fmin(a.y, b.y), fmin(a.z, b.z)); }
@@ -377,7 +417,10 @@ __global__ void k_cs_pt(CsArgs a)
     qh[0] = cellc(p.x + a.dHat, a.G.inv);
     qh[1] = cellc(p.y + a.dHat, a.G.inv);
     qh[2] = cellc(p.z + a.dHat, a.G.inv);
+    const float pb[6] = {__double2float_rd(p.x), __double2float_rd(p.y), __double2float_rd(p.z),
+                         __double2float_ru(p.x), __double2float_ru(p.y), __double2float_ru(p.z)};
     grid_query(a.G, ql, qh, [&](int t) {
+        if (box_apart(pb, a.tbox + 6 * (size_t)t, a.dHat_f)) return;
         const int t0i = a.btri[3 * t], t1i = a.btri[3 * t + 1], t2i = a.btri[3 * t + 2];
         if (vI == t0i || vI == t1i || vI == t2i) return;
         if (a.dbc[vI] && a.dbc[t0i] && a.dbc[t1i] && a.dbc[t2i]) return;
@@ -410,8 +453,12 @@ __global__ void k_cs_ee(CsArgs a)
     qh[0] = cellc(mxa.x + a.dHat, a.G.inv);
     qh[1] = cellc(mxa.y + a.dHat, a.G.inv);
     qh[2] = cellc(mxa.z + a.dHat, a.G.inv);
+    float eb[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) eb[k] = a.ebox[6 * (size_t)eI + k];
     grid_query(a.G, ql, qh, [&](int eJ) {
         if (eJ <= eI) return;
+        if (box_apart(eb, a.ebox + 6 * (size_t)eJ, a.dHat_f)) return;
         const int b0 = a.bedge[2 * eJ], b1 = a.bedge[2 * eJ + 1];
         if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
         if (a.dbc[a0] && a.dbc[a1] && a.dbc[b0] && a.dbc[b1]) return;
@@ -549,6 +596,14 @@ __global__ void k_cs_codim_pp(CsArgs a, int sv_begin)
     });
 }
 
+// smallest float not below v (host)
+static float float_up(double v)
+{
+    float f = (float)v;
+    if ((double)f < v) f = std::nextafter(f, INFINITY);
+    return f;
+}
+
 int build_constraints(Sim* s, const double* x)
 {
     cudaStream_t st = s->stream;
@@ -562,12 +617,18 @@ int build_constraints(Sim* s, const double* x)
         // merge table: 4x the list capacity, power of two
         unsigned tsz = 1024;
         while (tsz < 4u * (unsigned)s->cap_con) tsz <<= 1;
-        const size_t need = grid_bytes(std::max(std::max(s->nbt, s->nbe), s->nbn), 16) + (size_t)tsz * 12 + (1 << 20);
+        const size_t need = grid_bytes(std::max(std::max(s->nbt, s->nbe), s->nbn), 16) + (size_t)tsz * 12 +
+                            24 * ((size_t)s->nbt + s->nbe) + (1 << 20);
         int rc = ensure_scratch(s, need);
         if (rc) return rc;
         Arena ar{s->scratch.p, s->scratch.n};
         unsigned long long* tkeys = ar.take<unsigned long long>(tsz);
         int* tcount = ar.take<int>(tsz);
+        float* tbox = ar.take<float>(6 * (size_t)s->nbt + 6);
+        float* ebox = ar.take<float>(6 * (size_t)s->nbe + 6);
+        if (ar.used > ar.cap) return set_error(CIPC_ERR_CUDA, "constraint scratch");
+        if (s->nbt) k_item_boxes<<<nblk(s->nbt, 256), 256, 0, st>>>(s->nbt, 3, s->btri.p, x, tbox);
+        if (s->nbe) k_item_boxes<<<nblk(s->nbe, 256), 256, 0, st>>>(s->nbe, 2, s->bedge.p, x, ebox);
         cudaMemsetAsync(tkeys, 0xFF, sizeof(unsigned long long) * tsz, st);
         cudaMemsetAsync(tcount, 0, sizeof(int) * tsz, st);
         cudaMemsetAsync(s->cnt.p, 0, 8 * sizeof(unsigned long long), st);
@@ -580,7 +641,8 @@ int build_constraints(Sim* s, const double* x)
             continue;
         }
         if (rc) return rc;
-        CsArgs a{s->nbn, s->nbe, s->bnode.p, s->bedge.p, s->btri.p, x, s->X0.p, s->dbc.p, dHat, dHat * dHat, G, S};
+        CsArgs a{s->nbn, s->nbe, s->bnode.p, s->bedge.p, s->btri.p, x, s->X0.p, s->dbc.p, dHat, dHat * dHat, G, S,
+                 tbox, ebox, float_up(dHat)};
         k_cs_pt<<<nblk(s->nbn, 128), 128, 0, st>>>(a);
         ar.used = mark;
         rc = static_grid(build_grid(s, ar, s->nbe, 2, s->bedge.p, x, nullptr, 0, G));
@@ -1103,7 +1165,35 @@ struct CcdCand {
     int4* pidx;
     int cap;
     unsigned long long* counter;  // [0] count, [1] overflow
+    // FP32 boxes over {x, x + p} of the boundary triangles and edges (outward
+    // rounded) and xi rounded up: the conservative prefilter of the FP64 swept-box
+    // test (box_apart)
+    const float* tbox;
+    const float* ebox;
+    float xi_f;
 };
+
+// FP32 boxes of n items over their vertices at x and at x + p (the FP64 sums the
+// swept-box test forms), rounded outward
+__global__ void k_item_swept_boxes(int n, int nvi, const int* verts, const double* x, const double* p, float* box)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (int k = 0; k < nvi; ++k) {
+        const int v = verts[nvi * t + k];
+        const d3 a = ld(x, v), b = a + ld(p, v);
+        const double av[3] = {a.x, a.y, a.z}, bv[3] = {b.x, b.y, b.z};
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = fmin(mn[d], fmin(av[d], bv[d]));
+            mx[d] = fmax(mx[d], fmax(av[d], bv[d]));
+        }
+    }
+    for (int d = 0; d < 3; ++d) {
+        box[6 * t + d] = __double2float_rd(mn[d]);
+        box[6 * t + 3 + d] = __double2float_ru(mx[d]);
+    }
+}
 
 __device__ __forceinline__ void add_pair(const CcdCand& c, int tp, int a, int b, int d, int e)
 {
@@ -1131,7 +1221,12 @@ __global__ void k_ccd_pt(CcdCand c)
     qh[0] = cellc(mx.x + c.xi, c.G.inv);
     qh[1] = cellc(mx.y + c.xi, c.G.inv);
     qh[2] = cellc(mx.z + c.xi, c.G.inv);
+    const d3 pf = p + dp;
+    const float pb[6] = {__double2float_rd(fmin(p.x, pf.x)), __double2float_rd(fmin(p.y, pf.y)),
+                         __double2float_rd(fmin(p.z, pf.z)), __double2float_ru(fmax(p.x, pf.x)),
+                         __double2float_ru(fmax(p.y, pf.y)), __double2float_ru(fmax(p.z, pf.z))};
     grid_query(c.G, ql, qh, [&](int t) {
+        if (box_apart(pb, c.tbox + 6 * (size_t)t, c.xi_f)) return;
         const int t0i = c.btri[3 * t], t1i = c.btri[3 * t + 1], t2i = c.btri[3 * t + 2];
         if (vI == t0i || vI == t1i || vI == t2i) return;
         if (c.dbc[vI] && c.dbc[t0i] && c.dbc[t1i] && c.dbc[t2i]) return;
@@ -1161,8 +1256,12 @@ __global__ void k_ccd_ee(CcdCand c)
     qh[0] = cellc(mx.x + c.xi, c.G.inv);
     qh[1] = cellc(mx.y + c.xi, c.G.inv);
     qh[2] = cellc(mx.z + c.xi, c.G.inv);
+    float eb[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) eb[k] = c.ebox[6 * (size_t)eI + k];
     grid_query(c.G, ql, qh, [&](int eJ) {
         if (eJ <= eI) return;
+        if (box_apart(eb, c.ebox + 6 * (size_t)eJ, c.xi_f)) return;
         const int b0 = c.bedge[2 * eJ], b1 = c.bedge[2 * eJ + 1];
         if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
         if (c.dbc[a0] && c.dbc[a1] && c.dbc[b0] && c.dbc[b1]) return;
@@ -1239,7 +1338,8 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
     int cap = std::max(4096, 8 * (s->nbn + s->nbe));
     int shrink = 0;
     for (int attempt = 0; attempt < 8; ++attempt) {
-        const size_t need = grid_bytes(std::max(std::max(s->nbt, s->nbe), s->nbn), 32) + (size_t)cap * (16 + 1 + 8 + 1) + (1 << 20);
+        const size_t need = grid_bytes(std::max(std::max(s->nbt, s->nbe), s->nbn), 32) + (size_t)cap * (16 + 1 + 8 + 1) +
+                            24 * ((size_t)s->nbt + s->nbe) + (1 << 20);
         int rc = ensure_scratch(s, need);
         if (rc) return rc;
         Arena ar{s->scratch.p, s->scratch.n};
@@ -1249,6 +1349,11 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         uint8_t* hit = ar.take<uint8_t>(cap);
         unsigned long long* ctr = ar.take<unsigned long long>(8);
         double* amin = ar.take<double>(1);
+        float* tbox = ar.take<float>(6 * (size_t)s->nbt + 6);
+        float* ebox = ar.take<float>(6 * (size_t)s->nbe + 6);
+        if (ar.used > ar.cap) return set_error(CIPC_ERR_CUDA, "CCD scratch");
+        if (s->nbt) k_item_swept_boxes<<<nblk(s->nbt, 256), 256, 0, st>>>(s->nbt, 3, s->btri.p, x, p, tbox);
+        if (s->nbe) k_item_swept_boxes<<<nblk(s->nbe, 256), 256, 0, st>>>(s->nbe, 2, s->bedge.p, x, p, ebox);
         cudaMemsetAsync(ctr, 0, 8 * sizeof(unsigned long long), st);
         size_t mark = ar.used;
         Grid G;
@@ -1265,7 +1370,7 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         }
         if (rc) return rc;
         CcdCand c{s->bnode.p, s->bedge.p, s->btri.p, s->nbn, s->nbe, x, p, alpha, s->prm.xi, s->dbc.p, G,
-                  ptype, pidx, cap, ctr};
+                  ptype, pidx, cap, ctr, tbox, ebox, float_up(s->prm.xi)};
         k_ccd_pt<<<nblk(s->nbn, 128), 128, 0, st>>>(c);
         ar.used = mark;
         rc = build_grid(s, ar, s->nbe, 2, s->bedge.p, x, p, alpha, G);
