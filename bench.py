@@ -347,6 +347,26 @@ def scene_runs(args):
     return out
 
 
+def trace_scene(args):
+    """Steps the cloth-on-rotating-sphere scene (args.trace_scene x args.trace_scene
+    cloth) for args.trace_steps steps and prints each step's statistics (no JSON
+    line): the workload of the committed time-step profiles."""
+    import cipc_ffi as F
+    import workloads
+
+    X, T, dbc, c = workloads.cloth_on_sphere(n=args.trace_scene)
+    prec = F.MIXED if args.trace_precision == "mixed" else F.FP64
+    s = F.Sim(X, T, 200.0, 1e5, 0.3, 1e-3)
+    _, dhat2 = s.init_oipc(1e-3)
+    prm = F.make_params(0.02, dhat2, 5e-4, mu=0.4, epsv2=1e-6, fric_iters=1, newton_tol=1e-3, precision=prec,
+                        pcg_tol=1e-4)
+    for k in range(args.trace_steps):
+        s.set_dbc(dbc, workloads.rotate_y(X[dbc], c, 2.0 * 0.02 * (k + 1)))
+        st = s.step(prm, allow=(F.CIPC_ERR_NOT_CONVERGED,))
+        print("step", k, st.as_dict(), flush=True)
+    s.close()
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -514,11 +534,17 @@ def main():
     ap.add_argument("--ts-steps", type=int, default=6, help="measured steps per variant")
     ap.add_argument("--ts-epochs", type=int, default=20, help="training epochs of the learned correction")
     ap.add_argument("--no-scenes", action="store_true", help="skip the cube / codimensional / stacked-shell scenes")
+    ap.add_argument("--trace-scene", type=int, default=0,
+                    help="only step the cloth-on-sphere scene at this resolution (profiling workload)")
+    ap.add_argument("--trace-steps", type=int, default=12)
+    ap.add_argument("--trace-precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--c1-steps", type=int, default=50, help="steps of the cloth-on-cube scene")
     ap.add_argument("--c1-cpu-steps", type=int, default=8, help="cloth-on-cube steps run by the CPU oracle")
     ap.add_argument("--sc-steps", type=int, default=6, help="steps of the codimensional and stacked scenes")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.trace_scene > 0:
+        trace_scene(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
