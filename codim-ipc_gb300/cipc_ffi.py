@@ -204,6 +204,7 @@ _SIGS.update({
     "cipc_sim_init_oipc": (_c_int, [_vp, _c_dbl, _c_dbl, _vp, _vp]),
     "cipc_sim_set_kappa": (_c_int, [_vp, _c_dbl, _c_dbl]),
     "cipc_sim_get_kappa": (_c_int, [_vp, _vp]),
+    "cipc_sim_step_split": (_c_int, [_vp, _vp, _vp]),
     "cipc_sim_create_full": (_c_int, [_c_int, _vp, _c_int, _vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double, _vp, ctypes.c_double, _c_int, _vp, _vp, _vp]),
     "cipc_sim_init_eipc": (_c_int, [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _vp, _vp]),
@@ -372,6 +373,13 @@ class Sim:
     def step(self, params, allow=()):
         st = StepStats()
         rc = lib().cipc_sim_step(self.h, ctypes.byref(params), ctypes.byref(st))
+        _check(rc, allow)
+        return st
+
+    def step_split(self, params, allow=()):
+        """Advance_One_Step_SIE_Hinge: elastodynamic substep, then the projection."""
+        st = StepStats()
+        rc = lib().cipc_sim_step_split(self.h, ctypes.byref(params), ctypes.byref(st))
         _check(rc, allow)
         return st
 

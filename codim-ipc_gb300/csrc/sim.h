@@ -100,6 +100,8 @@ struct Sim {
     double cell = 1;  // broad-phase cell size (mean rest edge length)
     double kappa = 1, kappa_max = 100;
     SlParams sl;              // strain limiting (kappa_s doubles during steps, like kappa)
+    int elastic_off = 0;      // energies without membrane, bending, rods, tets (split stepper projection)
+    DBuf<double> xsplit;      // split stepper: positions at the start of the step
     DBuf<double> sl_prev;     // per-triangle largest stretch after the previous Newton iteration
     bool sl_have_prev = false;
     int trace = 0;    // CIPC_TRACE set: one stderr line per Newton iteration and refinement pass
@@ -181,5 +183,7 @@ int sim_create(Sim** out, int nv, const double* X, int nt, const int* tri, doubl
                double thickness, const double* gravity, double bendMult, int nh_model, const CodimDesc* cd = nullptr,
                const TetDesc* td = nullptr);
 void sim_destroy(Sim* s);
+int sim_step(Sim* s, StepStats* st);
+int sim_step_split(Sim* s, StepStats* st);
 
 }  // namespace cipc

@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(128) k_membrane(ElasticArgs a, HT* hval)
     __shared__ double sh[128];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     double e = 0;
-    if (t < a.nt) {
+    if (t < a.nt && !a.skip_membrane) {
         const int vid[3] = {a.tri[3 * t], a.tri[3 * t + 1], a.tri[3 * t + 2]};
         if (!(a.dbc[vid[0]] && a.dbc[vid[1]] && a.dbc[vid[2]])) {
             const d3 x[3] = {ld(a.x, vid[0]), ld(a.x, vid[1]), ld(a.x, vid[2])};
@@ -422,6 +422,14 @@ ElasticArgs elastic_args(Sim* s, const double* x, double* g)
     a.tvol = s->tvol.p;
     a.tlam = s->tlam;
     a.tmu = s->tmu;
+    a.skip_membrane = 0;
+    if (s->elastic_off) {
+        a.skip_membrane = 1;
+        a.nh = 0;
+        a.nrs = 0;
+        a.nrh = 0;
+        a.ntet = 0;
+    }
     return a;
 }
 

@@ -28,6 +28,9 @@ struct ElasticArgs {
     // or tetrahedron
     SlParams sl;
     double* flag;
+    // membrane off (the split stepper's projection substep keeps only inertia,
+    // strain limiting and contact)
+    int skip_membrane;
     // volumetric Neo-Hookean tetrahedra
     int ntet;
     const int *tet, *tet_slot;

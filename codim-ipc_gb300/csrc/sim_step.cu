@@ -445,6 +445,192 @@ int sim_step(Sim* s, StepStats* st)
     return rc;
 }
 
+// Split stepper (Advance_One_Step_SIE_Discrete_Shell, SPLITTING_IE.h:362-729):
+// an elastodynamic implicit-Euler substep without contact and without strain
+// limiting gives x'; a projection substep then minimises, from x^n,
+//   1/2 (x - x')^T M (x - x') + strain-limit barrier + contact barrier
+//   + lagged friction (+ Dirichlet penalty)
+// (Compute_SLP_Energy, :7-69) with its own Dirichlet handling (DBC_Info_Init
+// :218-301: the Dirichlet vertices move by the largest strain-feasible fraction of
+// their motion; if that is not all of it, a penalty of stiffness 1e8 pulls them,
+// doubled up to 1e10 while progress < 99%, DBC_Dual_Update :303-360) and line
+// search (CCD bound, then halving on infeasible strain, non-positive distance or
+// no decrease).
+int sim_step_split(Sim* s, StepStats* st)
+{
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
+    SimParams& P = s->prm;
+    const int nv = s->nv, n3 = 3 * nv, nd = (int)s->dbc_idx_h.size();
+    cudaStream_t str = s->stream;
+    int rc = CIPC_OK;
+    if (s->xsplit.alloc(n3) != cudaSuccess) return set_error(CIPC_ERR_CUDA, "split stepper buffer");
+    cudaMemcpyAsync(s->xsplit.p, s->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
+    // elastodynamic substep: no contact, no strain limiting
+    StepStats S1;
+    {
+        const SlParams sl = s->sl;
+        const int wc = P.withCollision;
+        s->sl.k0 = s->sl.k1 = 0;
+        P.withCollision = 0;
+        rc = sim_step(s, &S1);
+        s->sl = sl;
+        P.withCollision = wc;
+        if (rc != CIPC_OK && rc != CIPC_ERR_NOT_CONVERGED) return rc;
+    }
+    // projection substep from x^n towards x'
+    StepStats S;
+    S.pcg_iters = S1.pcg_iters;
+    S.line_search_trials = S1.line_search_trials;
+    cudaMemcpyAsync(s->xt.p, s->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);  // x'
+    cudaMemcpyAsync(s->x.p, s->xsplit.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
+    cudaMemcpyAsync(s->xn.p, s->xsplit.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
+    s->elastic_off = 1;
+    struct Restore {
+        Sim* s;
+        ~Restore() { s->elastic_off = 0; }
+    } restore{s};
+    s->solve_fallbacks = 0;
+    s->solve_learned = 0;
+    s->dbc_stiff = 0;
+    double dbcPenaltyXn = 0;
+    cudaMemcpyAsync(s->proj.p, s->dbc.p, nv, cudaMemcpyDeviceToDevice, str);
+    if (nd > 0) {
+        cudaMemsetAsync(s->disp.p, 0, sizeof(double) * n3, str);
+        k_dbc_disp<<<nblk(nd, 128), 128, 0, str>>>(nd, s->dbc_idx.p, s->dbc_tgt.p, s->x.p, s->disp.p);
+        cudaMemsetAsync(s->dbc_fixed.p, 0, nv, str);
+        k_dbc_fixed<<<nblk(nd, 128), 128, 0, str>>>(nd, s->dbc_idx.p, s->disp.p, s->dbc_fixed.p);
+        double dbcAlpha = 1.0;
+        if (s->sl.k0 > 0) {
+            for (int k = 0;; ++k) {
+                if (k > 200) return set_error(CIPC_ERR_NOT_CONVERGED, "no strain-feasible Dirichlet motion");
+                k_axpby<<<nblk(n3, 256), 256, 0, str>>>(n3, s->xsplit.p, dbcAlpha, s->disp.p, s->x.p);
+                bool feas = true;
+                if ((rc = elastic_feasible(s, s->x.p, &feas))) return rc;
+                if (feas) break;
+                dbcAlpha /= 2;
+            }
+            cudaMemcpyAsync(s->x.p, s->xsplit.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
+        }
+        if (dbcAlpha == 1.0) {
+            k_dbc_apply<<<nblk(nd, 128), 128, 0, str>>>(nd, s->dbc_idx.p, s->dbc_tgt.p, s->x.p);
+        } else {
+            s->dbc_stiff = 1e8;
+            dbcPenaltyXn = dbc_dist2(s, s->xn.p);
+            cudaMemcpyAsync(s->proj.p, s->dbc_fixed.p, nv, cudaMemcpyDeviceToDevice, str);
+            S.status = 1;
+        }
+    }
+    s->ncon = s->nfric = s->npcon = 0;
+    if (P.withCollision) {
+        if ((rc = build_constraints(s, s->x.p))) return rc;
+        if (P.mu > 0 && (rc = friction_basis(s, s->x.p))) return rc;
+    }
+    double Eprev;
+    bool ok;
+    if ((rc = eval_energy(s, s->x.p, &Eprev, &ok))) return rc;
+    if (!ok) return set_error(CIPC_ERR_NONPOSITIVE_DISTANCE, "split step: the start of the projection is infeasible");
+    std::deque<double> res;
+    bool useGD = false;
+    double L2 = 0;
+    int it = 0;
+    s->solve_tol = 0;
+    do {
+        if (it >= P.maxIter) {
+            S.status = -1;
+            rc = set_error(CIPC_ERR_NOT_CONVERGED, "Newton iteration cap %d reached", P.maxIter);
+            break;
+        }
+        eval_grad_hess(s, s->x.p, s->g.p, !useGD);
+        k_neg<<<nblk(n3, 256), 256, 0, str>>>(n3, s->g.p, s->rhs.p);
+        if (useGD) {
+            cudaMemcpyAsync(s->dir.p, s->rhs.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
+        } else {
+            int pit = 0;
+            const int lr = linear_solve(s, s->rhs.p, s->dir.p, &pit);
+            S.pcg_iters += pit;
+            if (lr == CIPC_ERR_NAN) {
+                useGD = true;
+                cudaMemcpyAsync(s->dir.p, s->rhs.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
+            } else if (lr != CIPC_OK && lr != CIPC_ERR_NOT_CONVERGED) {
+                return lr;
+            }
+        }
+        cudaMemcpyAsync(s->xprev.p, s->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
+        double alpha = 1.0, feasible = 0, E = Eprev;
+        if (P.withCollision && (rc = ccd_step_size(s, s->xprev.p, s->dir.p, 1.0, &alpha))) return rc;
+        bool valid = true;
+        int trials = 0;
+        do {
+            if (++trials > 200) {
+                S.status = -3;
+                return set_error(CIPC_ERR_NOT_CONVERGED, "line search did not find a decrease");
+            }
+            k_axpby<<<nblk(n3, 256), 256, 0, str>>>(n3, s->xprev.p, alpha, s->dir.p, s->x.p);
+            if ((rc = elastic_feasible(s, s->x.p, &valid))) return rc;
+            if (valid) {
+                if (feasible == 0) feasible = alpha;
+                if (P.withCollision) {
+                    if ((rc = build_constraints(s, s->x.p))) return rc;
+                    if (s->ncon > 0) {
+                        double md;
+                        if ((rc = min_d2(s, s->x.p, &md))) return rc;
+                        if (md <= 0) {
+                            alpha /= 2;
+                            valid = false;
+                            feasible = 0;
+                            continue;
+                        }
+                    }
+                }
+                bool eok;
+                if ((rc = eval_energy(s, s->x.p, &E, &eok))) return rc;
+                valid = valid && eok;
+            }
+            alpha /= 2;
+        } while (E > Eprev || !valid);
+        S.line_search_trials += trials;
+        Eprev = E;
+        L2 = std::sqrt(sum_sq(s, s->dir.p, n3) / (nv - nd)) / P.h;
+        ++it;
+        res.push_back(L2);
+        if (res.size() > 3) res.pop_front();
+        L2 = *std::max_element(res.begin(), res.end());
+        if (useGD) L2 = P.tol * 10;
+        if (alpha * 2 < 1e-6 && feasible > 1e-6) useGD = true;
+        else useGD = false;
+        if (s->trace)
+            std::fprintf(stderr, "cipc split %d: step %.3e feasible %.3e L2 %.3e dbc_stiff %.3g ncon %d\n", it,
+                         2 * alpha, feasible, L2, s->dbc_stiff, s->ncon);
+        if (s->dbc_stiff != 0) {
+            const double progress = 1 - std::sqrt(dbc_dist2(s, s->x.p) / dbcPenaltyXn);
+            if (progress < 0.99) {
+                if (L2 < P.tol * 10 && s->dbc_stiff < 1e10) {
+                    s->dbc_stiff *= 2;
+                    if ((rc = eval_energy(s, s->x.p, &Eprev, &ok))) return rc;
+                }
+                L2 = P.tol * 10;
+            } else {
+                s->dbc_stiff = 0;
+                cudaMemcpyAsync(s->proj.p, s->dbc.p, nv, cudaMemcpyDeviceToDevice, str);
+                if ((rc = eval_energy(s, s->x.p, &Eprev, &ok))) return rc;
+            }
+        }
+    } while (res.size() < 3 || L2 > P.tol);
+    k_velocity<<<nblk(n3, 256), 256, 0, str>>>(n3, s->x.p, s->xsplit.p, P.h, s->v.p);
+    S.newton_iters = S1.newton_iters + it;
+    S.n_constraints = s->ncon;
+    if (s->ncon > 0) min_d2(s, s->x.p, &S.min_dist2);
+    S.kappa = s->kappa;
+    cudaError_t e = cudaStreamSynchronize(str);
+    if (e != cudaSuccess) return set_cuda_error(e, "split step");
+    S.ms = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+    S.precond_fallbacks = s->solve_fallbacks;
+    S.learned_solves = s->solve_learned;
+    *st = S;
+    return rc;
+}
+
 void sim_destroy(Sim* s)
 {
     if (!s) return;
@@ -457,7 +643,7 @@ void sim_destroy(Sim* s)
         b->release();
     for (DBuf<double>* b : {&s->P, &s->vol, &s->hinfo, &s->mass, &s->b, &s->X0, &s->dbc_tgt, &s->x, &s->xn, &s->xt,
                             &s->v, &s->g, &s->dir, &s->xprev, &s->rhs, &s->disp, &s->fw, &s->fT, &s->flam, &s->pdiag,
-                            &s->red, &s->pd2, &s->rinfo, &s->rhinfo, &s->tDinv, &s->tvol, &s->sl_prev})
+                            &s->red, &s->pd2, &s->rinfo, &s->rhinfo, &s->tDinv, &s->tvol, &s->sl_prev, &s->xsplit})
         b->release();
     s->dbc.release();
     s->proj.release();
@@ -704,7 +890,7 @@ static void to_params(const cipc_step_params* p, SimParams& q)
     if (q.elastic) q.xi = 0;
 }
 
-extern "C" int cipc_sim_step(cipc_sim* h, const cipc_step_params* p, cipc_step_stats* stats)
+static int step_entry(cipc_sim* h, const cipc_step_params* p, cipc_step_stats* stats, bool split)
 {
     if (int rc = check_sim(h)) return rc;
     if (!p || !(p->h > 0) || !(p->dhat2 > 0) || !(p->xi >= 0) || !(p->newton_tol > 0) ||
@@ -715,7 +901,7 @@ extern "C" int cipc_sim_step(cipc_sim* h, const cipc_step_params* p, cipc_step_s
     to_params(p, s->prm);
     if (old_prec != s->prm.precision) s->hval.alloc(9 * sizeof(double) * (size_t)s->nnzb);
     StepStats S;
-    const int rc = sim_step(s, &S);
+    const int rc = split ? sim_step_split(s, &S) : sim_step(s, &S);
     if (stats) {
         stats->newton_iters = S.newton_iters;
         stats->pcg_iters = S.pcg_iters;
@@ -729,6 +915,16 @@ extern "C" int cipc_sim_step(cipc_sim* h, const cipc_step_params* p, cipc_step_s
         stats->learned_solves = S.learned_solves;
     }
     return rc;
+}
+
+extern "C" int cipc_sim_step(cipc_sim* h, const cipc_step_params* p, cipc_step_stats* stats)
+{
+    return step_entry(h, p, stats, false);
+}
+
+extern "C" int cipc_sim_step_split(cipc_sim* h, const cipc_step_params* p, cipc_step_stats* stats)
+{
+    return step_entry(h, p, stats, true);
 }
 
 extern "C" int cipc_sim_constraints(cipc_sim* h, const cipc_step_params* p, const double* x, int cap, int* out6,

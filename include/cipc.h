@@ -270,6 +270,12 @@ int cipc_sim_write_obj(cipc_sim* sim, const char* path);
  * Returns CIPC_OK, or CIPC_ERR_NOT_CONVERGED when the Newton cap is reached or
  * the Dirichlet motion is blocked by contact (stats->status -1 / -2). */
 int cipc_sim_step(cipc_sim* sim, const cipc_step_params* params, cipc_step_stats* stats);
+/* Split stepper; replaces Advance_One_Step_SIE_Hinge (SPLITTING_IE.h:362-729,
+ * export DISCRETE_SHELL.h:1115): an implicit-Euler substep without contact and
+ * strain limiting, then a projection substep minimising 1/2 |x - x'|_M^2 + strain
+ * barrier + contact barrier + friction from x^n.  stats->newton_iters counts both
+ * substeps' Newton iterations. */
+int cipc_sim_step_split(cipc_sim* sim, const cipc_step_params* params, cipc_step_stats* stats);
 /* Parity entry points: the constraint set at x (rows of kind, v0..v3, multiplicity;
  * kinds 0 PP 1 PE 2 PT 3 EE 4 mollified EE 5 mollified PE 6 mollified PP), the
  * incremental potential and its gradient at x for a given x~, and the

@@ -250,6 +250,20 @@ class Shell:
         rc = self.L.orc_shell_step(self.h, _p(prm), _p(x), _p(v), _p(kappa2), _p(idx), _p(tg), len(idx), _p(st))
         return rc, dict(newton_iters=int(st[0]), n_constraints=int(st[1]), min_dist2=st[2], gd_iters=int(st[3]))
 
+    def step_split(self, x, v, kappa2, dbc_idx, dbc_tgt, h, dhat2, xi, mu=0.0, epsv2=1e-6, fric_iters=1, tol=1e-2,
+             with_collision=True, max_iter=500, elastic_ipc=False):
+        """Split stepper (elastodynamic substep, then the projection); as step."""
+        prm = np.array([h, dhat2, xi, mu, epsv2, fric_iters, tol, 1.0 if with_collision else 0.0, max_iter,
+                        1.0 if elastic_ipc else 0.0], float)
+        st = np.zeros(4)
+        idx = _c(dbc_idx, np.int32)
+        tg = _c(dbc_tgt, np.float64)
+        self.dbc = idx
+        self.L.orc_shell_step_split.restype = ctypes.c_int
+        self.L.orc_shell_step_split.argtypes = self.L.orc_shell_step.argtypes
+        rc = self.L.orc_shell_step_split(self.h, _p(prm), _p(x), _p(v), _p(kappa2), _p(idx), _p(tg), len(idx), _p(st))
+        return rc, dict(newton_iters=int(st[0]), n_constraints=int(st[1]), min_dist2=st[2], gd_iters=int(st[3]))
+
 
 def num_threads():
     return lib().orc_num_threads()

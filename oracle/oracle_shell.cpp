@@ -1427,6 +1427,7 @@ struct Ctx {
     const double* dbc_tgt = nullptr;
     int ndbc = 0;
     std::vector<char> proj;  // rows / columns projected out of the Newton system
+    bool slp = false;        // split stepper projection: no membrane, bending, rods, tets
 };
 
 static double dbc_dist2(const Ctx& C, const double* x)
@@ -1444,7 +1445,7 @@ static double total_energy(const Ctx& C, const double* x, const std::vector<Con>
                            bool* ok)
 {
     const Shell& S = *C.S;
-    double E = elastic_energy(S, x, C.P.h);
+    double E = C.slp ? 0.0 : elastic_energy(S, x, C.P.h);
     double ine = 0;
     for (int i = 0; i < S.nv; ++i)
         for (int d = 0; d < 3; ++d) {
@@ -1466,7 +1467,7 @@ static double total_energy(const Ctx& C, const double* x, const std::vector<Con>
     }
     bool good = true;
     E += strain_terms(S, x, C.P.h, nullptr, nullptr, &good);
-    E += tet_terms(S, x, C.P.h, nullptr, nullptr, &good);
+    if (!C.slp) E += tet_terms(S, x, C.P.h, nullptr, nullptr, &good);
     if (C.P.withCollision) good = barrier_terms(S, x, cs, C.P.dHat2, C.P.xi, C.kappa, &E, nullptr, nullptr) && good;
     if (C.P.withCollision && C.P.mu > 0) friction_terms(F, x, C.xn, C.P.epsv2 * C.P.h * C.P.h, C.P.mu, &E, nullptr, nullptr);
     if (ok) *ok = good;
@@ -1479,9 +1480,9 @@ static void total_grad(const Ctx& C, const double* x, const std::vector<Con>& cs
     const Shell& S = *C.S;
     int n = 3 * S.nv;
     for (int i = 0; i < n; ++i) g[i] = 0;
-    elastic_grad_hess(S, x, C.P.h, g, A);
+    if (!C.slp) elastic_grad_hess(S, x, C.P.h, g, A);
     strain_terms(S, x, C.P.h, g, A, nullptr);
-    tet_terms(S, x, C.P.h, g, A, nullptr);
+    if (!C.slp) tet_terms(S, x, C.P.h, g, A, nullptr);
     for (int i = 0; i < S.nv; ++i)
         for (int d = 0; d < 3; ++d) g[3 * i + d] += S.mass[i] * (x[3 * i + d] - C.xtilde[3 * i + d]);
     const std::vector<char>& proj = C.proj.empty() ? S.dbc : C.proj;
@@ -1703,6 +1704,156 @@ static void shell_step(Shell& S, const StepParams& P_in, double* x, double* v, d
     out.min_dist2 = cs.empty() ? 0 : min_dist2(cs, x, P.xi, nullptr);
 }
 
+// Split stepper (Advance_One_Step_SIE_Discrete_Shell, SPLITTING_IE.h:362-729):
+// implicit-Euler substep without contact and strain limiting (x'), then from x^n
+// the projection minimising 1/2 |x - x'|_M^2 + strain barrier + contact barrier +
+// friction (+ Dirichlet penalty, Compute_SLP_Energy :7-69), with DBC_Info_Init
+// (:218-301) and DBC_Dual_Update (:303-360).
+static void shell_step_split(Shell& S, const StepParams& P_in, double* x, double* v, double* kappa,
+                             const int* dbc_idx, const double* dbc_tgt, int ndbc, StepOut& out)
+{
+    const int nv = S.nv, n = 3 * nv;
+    std::vector<double> xs(x, x + n);
+    StepOut o1;
+    {
+        StepParams P1 = P_in;
+        P1.withCollision = 0;
+        const double k0 = S.sl_kappa[0], k1 = S.sl_kappa[1];
+        S.sl_kappa[0] = S.sl_kappa[1] = 0;
+        shell_step(S, P1, x, v, kappa, dbc_idx, dbc_tgt, ndbc, o1);
+        S.sl_kappa[0] = k0;
+        S.sl_kappa[1] = k1;
+    }
+    StepParams P = P_in;
+    if (P.elastic) P.xi = 0;
+    std::vector<double> xprim(x, x + n);
+    for (int i = 0; i < n; ++i) x[i] = xs[i];
+    const double bk = P.elastic ? kappa[0] / (P.dHat2 * P.dHat2) : kappa[0];
+    Ctx C{&S, P, xprim.data(), xs.data(), bk};
+    C.slp = true;
+    C.dbc_idx = dbc_idx;
+    C.dbc_tgt = dbc_tgt;
+    C.ndbc = ndbc;
+    C.proj = S.dbc;
+    std::vector<double> disp(n, 0.0);
+    for (int k = 0; k < ndbc; ++k)
+        for (int d = 0; d < 3; ++d) disp[3 * dbc_idx[k] + d] = dbc_tgt[3 * k + d] - x[3 * dbc_idx[k] + d];
+    double dbcAlpha = 1, penaltyXn = 0;
+    if (S.sl_kappa[0] > 0) {
+        std::vector<double> xt(n);
+        for (;;) {
+            for (int i = 0; i < n; ++i) xt[i] = xs[i] + dbcAlpha * disp[i];
+            bool feas = true;
+            strain_terms(S, xt.data(), P.h, nullptr, nullptr, &feas);
+            if (feas) break;
+            dbcAlpha /= 2;
+        }
+    }
+    if (dbcAlpha == 1) {
+        for (int k = 0; k < ndbc; ++k)
+            for (int d = 0; d < 3; ++d) x[3 * dbc_idx[k] + d] = dbc_tgt[3 * k + d];
+    } else {
+        C.stiff = 1e8;
+        penaltyXn = dbc_dist2(C, xs.data());
+        C.proj.assign(nv, 0);
+        for (int k = 0; k < ndbc; ++k) {
+            const int vv = dbc_idx[k];
+            C.proj[vv] = (disp[3 * vv] == 0 && disp[3 * vv + 1] == 0 && disp[3 * vv + 2] == 0) ? 1 : 0;
+        }
+    }
+    std::vector<Con> cs;
+    std::vector<Fric> F;
+    if (P.withCollision) {
+        constraint_set(S, x, P.dHat2, P.xi, cs);
+        if (P.mu > 0) friction_basis(x, cs, P.dHat2, P.xi, C.kappa, F);
+    }
+    bool ok;
+    double Eprev = total_energy(C, x, cs, F, &ok);
+    if (!ok) {
+        out.status = -3;
+        return;
+    }
+    std::deque<double> res;
+    bool useGD = false;
+    std::vector<double> g(n), sol(n), rhs(n), xprev(n);
+    int it = 0;
+    double L2 = 0;
+    do {
+        if (it >= P.maxIter) {
+            out.status = -1;
+            break;
+        }
+        Asm A;
+        A.dbc = &C.proj;
+        total_grad(C, x, cs, F, g.data(), useGD ? nullptr : &A);
+        for (int i = 0; i < n; ++i) rhs[i] = -g[i];
+        if (useGD) sol = rhs;
+        else if (!skyline_solve(n, A.t, rhs.data(), sol.data())) {
+            useGD = true;
+            sol = rhs;
+            ++out.gd_iters;
+        }
+        xprev.assign(x, x + n);
+        double alpha = 1.0, feasible = 0, E = Eprev;
+        if (P.withCollision) alpha = ccd_step_size(S, xprev.data(), sol.data(), 1.0, P.xi);
+        bool valid = true;
+        int trials = 0;
+        do {
+            if (++trials > 200) {
+                out.status = -3;
+                return;
+            }
+            for (int i = 0; i < n; ++i) x[i] = xprev[i] + alpha * sol[i];
+            valid = true;
+            strain_terms(S, x, P.h, nullptr, nullptr, &valid);
+            if (valid) {
+                if (feasible == 0) feasible = alpha;
+                if (P.withCollision) {
+                    constraint_set(S, x, P.dHat2, P.xi, cs);
+                    if (!cs.empty() && min_dist2(cs, x, P.xi, nullptr) <= 0) {
+                        alpha /= 2;
+                        valid = false;
+                        feasible = 0;
+                        continue;
+                    }
+                }
+                bool eok;
+                E = total_energy(C, x, cs, F, &eok);
+                valid = valid && eok;
+            }
+            alpha /= 2;
+        } while (E > Eprev || !valid);
+        Eprev = E;
+        double ss = 0;
+        for (int i = 0; i < n; ++i) ss += sol[i] * sol[i];
+        L2 = std::sqrt(ss / (nv - ndbc)) / P.h;
+        ++it;
+        res.push_back(L2);
+        if (res.size() > 3) res.pop_front();
+        L2 = *std::max_element(res.begin(), res.end());
+        if (useGD) L2 = P.tol * 10;
+        useGD = alpha * 2 < 1e-6 && feasible > 1e-6;
+        if (C.stiff != 0) {
+            const double progress = 1 - std::sqrt(dbc_dist2(C, x) / penaltyXn);
+            if (progress < 0.99) {
+                if (L2 < P.tol * 10 && C.stiff < 1e10) {
+                    C.stiff *= 2;
+                    Eprev = total_energy(C, x, cs, F, nullptr);
+                }
+                L2 = P.tol * 10;
+            } else {
+                C.stiff = 0;
+                C.proj = S.dbc;
+                Eprev = total_energy(C, x, cs, F, nullptr);
+            }
+        }
+    } while (res.size() < 3 || L2 > P.tol);
+    for (int i = 0; i < n; ++i) v[i] = (x[i] - xs[i]) / P.h;
+    out.pn_iters = o1.pn_iters + it;
+    out.n_constraints = (int)cs.size();
+    out.min_dist2 = cs.empty() ? 0 : min_dist2(cs, x, P.xi, nullptr);
+}
+
 }  // namespace orc
 
 // ---------------------------------------------------------------------------
@@ -1869,6 +2020,23 @@ int orc_shell_step(void* h, const double* params, double* x, double* v, double* 
                  (int)params[8], (int)params[9]};
     StepOut o;
     shell_step(*S, P, x, v, kappa2, dbc_idx, dbc_tgt, ndbc, o);
+    if (stats) {
+        stats[0] = o.pn_iters;
+        stats[1] = o.n_constraints;
+        stats[2] = o.min_dist2;
+        stats[3] = o.gd_iters;
+    }
+    return o.status;
+}
+
+int orc_shell_step_split(void* h, const double* params, double* x, double* v, double* kappa2, const int* dbc_idx,
+                   const double* dbc_tgt, int ndbc, double* stats)
+{
+    Shell* S = (Shell*)h;
+    StepParams P{params[0], params[1], params[2], params[3], params[4], (int)params[5], params[6], (int)params[7],
+                 (int)params[8], (int)params[9]};
+    StepOut o;
+    shell_step_split(*S, P, x, v, kappa2, dbc_idx, dbc_tgt, ndbc, o);
     if (stats) {
         stats[0] = o.pn_iters;
         stats[1] = o.n_constraints;

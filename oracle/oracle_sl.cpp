@@ -79,19 +79,39 @@ double orc_sl_elem(const double* x9, const double* P, double kh, const double* s
             f[3 + i] += c[1][v] * x9[3 * v + i];
         }
     }
-    D2<6> fd[6];
-    for (int k = 0; k < 6; ++k) fd[k] = seed<6>(f[k], k);
+    // At equal singular values (e.g. a triangle at rest) the singular values are
+    // not differentiable one by one, although the energy is: there the value and
+    // derivatives are the mean of two evaluations at F +- eps e00 (eps = 1e-6 |F|),
+    // which split them (error O(eps^2))
+    const double c00 = f[0] * f[0] + f[1] * f[1] + f[2] * f[2], c01 = f[0] * f[3] + f[1] * f[4] + f[2] * f[5];
+    const double c11 = f[3] * f[3] + f[4] * f[4] + f[5] * f[5];
+    const double m = 0.5 * (c00 + c11), dd = 0.5 * (c00 - c11), r = std::sqrt(dd * dd + c01 * c01);
+    const bool degenerate = !(r > 1e-6 * m);
+    const double eps = 1e-6 * std::sqrt(c00 + c11);
+    const int nev = degenerate ? 2 : 1;
+    double Ev = 0, gF[6] = {0, 0, 0, 0, 0, 0}, HFs[36];
+    for (int k = 0; k < 36; ++k) HFs[k] = 0;
     bool ok = true;
-    const D2<6> E = energy_F(fd, s, s_hat, kappa_s, kh, &ok);
+    for (int e = 0; e < nev; ++e) {
+        double fe[6];
+        for (int k = 0; k < 6; ++k) fe[k] = f[k];
+        if (degenerate) fe[0] += (e == 0 ? eps : -eps);
+        D2<6> fd[6];
+        for (int k = 0; k < 6; ++k) fd[k] = seed<6>(fe[k], k);
+        const D2<6> E = energy_F(fd, s, s_hat, kappa_s, kh, &ok);
+        Ev += E.v.v / nev;
+        for (int k = 0; k < 6; ++k) gF[k] += E.v.d[k] / nev;
+        for (int a = 0; a < 6; ++a)
+            for (int b = 0; b < 6; ++b) HFs[6 * a + b] += 0.5 * (E.d[a].d[b] + E.d[b].d[a]) / nev;
+    }
     if (valid) *valid = ok ? 1 : 0;
     if (g) {
         for (int v = 0; v < 3; ++v)
-            for (int i = 0; i < 3; ++i) g[3 * v + i] = c[0][v] * E.v.d[i] + c[1][v] * E.v.d[3 + i];
+            for (int i = 0; i < 3; ++i) g[3 * v + i] = c[0][v] * gF[i] + c[1][v] * gF[3 + i];
     }
     if (H) {
         double HF[36];
-        for (int a = 0; a < 6; ++a)
-            for (int b = 0; b < 6; ++b) HF[6 * a + b] = 0.5 * (E.d[a].d[b] + E.d[b].d[a]);
+        for (int k = 0; k < 36; ++k) HF[k] = HFs[k];
         if (project) orc::make_pd(6, HF);
         for (int v = 0; v < 3; ++v)
             for (int i = 0; i < 3; ++i)
@@ -103,7 +123,7 @@ double orc_sl_elem(const double* x9, const double* P, double kh, const double* s
                         H[9 * (3 * v + i) + 3 * w + j] = t;
                     }
     }
-    return E.v.v;
+    return Ev;
 }
 
 // largest stretch of one triangle (the reference's Compute_Inextensibility)
