@@ -31,8 +31,11 @@ T barrier(const T& s, double lim, double hat)
 }
 
 // f[0..2] column 0 of F, f[3..5] column 1
+// sv0: the singular values that decide feasibility and which terms are active
+// (those of the unperturbed F, also when f is split at equal singular values)
 template <typename T>
-T energy_F(const T* f, const double* s, const double* sh, const double* ks, double kh, bool* valid)
+T energy_F(const T* f, const double* sv0, const double* s, const double* sh, const double* ks, double kh,
+           bool* valid)
 {
     const T c00 = f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
     const T c01 = f[0] * f[3] + f[1] * f[4] + f[2] * f[5];
@@ -42,7 +45,7 @@ T energy_F(const T* f, const double* s, const double* sh, const double* ks, doub
     const T sig[2] = {sq_root(m + r), sq_root(m - r)};
     T E = C<T>(0.0);
     for (int i = 0; i < 2; ++i) {
-        const double sv = value(sig[i]);
+        const double sv = sv0[i];
         if (sv >= s[0]) *valid = false;
         else if (sv > sh[0]) E = E + C<T>(kh * ks[0]) * barrier(sig[i], s[0], sh[0]);
         if (ks[1] > 0) {
@@ -79,15 +82,16 @@ double orc_sl_elem(const double* x9, const double* P, double kh, const double* s
             f[3 + i] += c[1][v] * x9[3 * v + i];
         }
     }
-    // At equal singular values (e.g. a triangle at rest) the singular values are
-    // not differentiable one by one, although the energy is: there the value and
-    // derivatives are the mean of two evaluations at F +- eps e00 (eps = 1e-6 |F|),
-    // which split them (error O(eps^2))
+    // At (numerically) equal singular values, e.g. a triangle at rest, the
+    // singular values are not differentiable one by one, although the energy is:
+    // there the value and derivatives are the mean of two evaluations at
+    // F +- eps e00 (eps = 1e-7 |F|), which split them (error O(eps^2))
     const double c00 = f[0] * f[0] + f[1] * f[1] + f[2] * f[2], c01 = f[0] * f[3] + f[1] * f[4] + f[2] * f[5];
     const double c11 = f[3] * f[3] + f[4] * f[4] + f[5] * f[5];
     const double m = 0.5 * (c00 + c11), dd = 0.5 * (c00 - c11), r = std::sqrt(dd * dd + c01 * c01);
-    const bool degenerate = !(r > 1e-6 * m);
-    const double eps = 1e-6 * std::sqrt(c00 + c11);
+    const bool degenerate = !(r > 1e-14 * m);
+    const double eps = 1e-7 * std::sqrt(c00 + c11);
+    const double sv0[2] = {std::sqrt(m + r), std::sqrt(m - r)};
     const int nev = degenerate ? 2 : 1;
     double Ev = 0, gF[6] = {0, 0, 0, 0, 0, 0}, HFs[36];
     for (int k = 0; k < 36; ++k) HFs[k] = 0;
@@ -98,7 +102,7 @@ double orc_sl_elem(const double* x9, const double* P, double kh, const double* s
         if (degenerate) fe[0] += (e == 0 ? eps : -eps);
         D2<6> fd[6];
         for (int k = 0; k < 6; ++k) fd[k] = seed<6>(fe[k], k);
-        const D2<6> E = energy_F(fd, s, s_hat, kappa_s, kh, &ok);
+        const D2<6> E = energy_F(fd, sv0, s, s_hat, kappa_s, kh, &ok);
         Ev += E.v.v / nev;
         for (int k = 0; k < 6; ++k) gF[k] += E.v.d[k] / nev;
         for (int a = 0; a < 6; ++a)
