@@ -171,7 +171,7 @@ struct Sim {
     void* learned = nullptr;
     void* capture = nullptr;
     int solve_fallbacks = 0, solve_learned = 0;  // counts of the current step
-    int bj_last_iters = 0;                       // iterations of the latest converged solve (0: no block-Jacobi solve yet)
+    int bj_last_iters = 0;                       // iterations of the step's latest block-Jacobi solve (0: none yet)
     double solve_tol = 0;                        // relative tolerance of the next linear solve (0: prm.pcg_tol)
     std::vector<double> host_mass;
 };

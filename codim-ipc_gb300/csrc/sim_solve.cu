@@ -332,14 +332,14 @@ static int solve_with_precond(Sim* s, const double* rhs, double* sol, int* iters
 
 int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
 {
-    // The learned correction is used once a block-Jacobi solve has set the
-    // yardstick, and not after it has stalled twice in this step.  It stalls when
-    // it needs more than three times the iterations of the latest converged solve
-    // (block Jacobi or learned; at least 100 — consecutive Newton systems differ
-    // in difficulty by up to ~2x, and as contacts build up the count drifts
-    // upward, which a yardstick fixed at the first block-Jacobi solve would
-    // mistake for a stall), breaks down or yields NaN; block Jacobi then solves
-    // the same system, so a poor network costs at most ~4x a plain solve.
+    // The learned correction is used once a block-Jacobi solve of this time step
+    // (its first) has set the yardstick, and not after it has stalled twice in
+    // the step.  It stalls when it needs more than three times the iterations of
+    // the latest block-Jacobi solve (at least 100; consecutive Newton systems of
+    // a step differ in difficulty by up to ~2x, while across steps the count
+    // drifts upward as contacts build up, hence the per-step yardstick), breaks
+    // down or yields NaN; block Jacobi then solves the same system, so a poor
+    // network costs at most ~4x a plain solve.
     bool learned = false;
     if (s->prm.precond == 1 && s->learned && s->bj_last_iters > 0 && s->solve_fallbacks < 2)
         learned = lp_precond(s, static_cast<LpModel*>(s->learned)) == CIPC_OK;
@@ -352,7 +352,6 @@ int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
     total += it;
     if (learned) {
         ++s->solve_learned;
-        if (rc == CIPC_OK) s->bj_last_iters = std::max(1, it);
         if (rc == CIPC_ERR_NOT_CONVERGED || rc == CIPC_ERR_NAN) {
             // the learned preconditioner stalled or broke down: plain block Jacobi
             // solves the same system (and is the yardstick for the network)

@@ -192,6 +192,7 @@ int sim_step(Sim* s, StepStats* st)
     StepStats S;
     s->solve_fallbacks = 0;
     s->solve_learned = 0;
+    s->bj_last_iters = 0;  // the step's first solve is block Jacobi: a fresh yardstick
     s->sl_have_prev = false;  // strain history is per step (IMPLICIT_EULER.h:444)
     const SimParams& P = s->prm;
     const int nv = s->nv, n3 = 3 * nv, nd = (int)s->dbc_idx_h.size();
@@ -492,6 +493,7 @@ int sim_step_split(Sim* s, StepStats* st)
     } restore{s};
     s->solve_fallbacks = 0;
     s->solve_learned = 0;
+    s->bj_last_iters = 0;
     s->dbc_stiff = 0;
     double dbcPenaltyXn = 0;
     cudaMemcpyAsync(s->proj.p, s->dbc.p, nv, cudaMemcpyDeviceToDevice, str);
