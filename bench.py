@@ -492,7 +492,7 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": round(value, 2), "unit": "Mpairs/s", "n_gpus": ws, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64" if prec == F.MIXED else "f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f32+float-float" if prec == F.MIXED else "f64", "data": "synthetic",
             "config": {"workload": "ACCD time of impact, %d seeded contact pairs per GPU (PT/EE/PE/PP 40/40/10/10)"
                                    % n, "pairs_per_gpu": n, "precision": args.precision, "eta": ETA, "xi": XI,
                        "l2": "inputs (%.2f GB) larger than L2; no flush" % (ccd_bytes / 1e9)},
@@ -501,9 +501,13 @@ def run_ours(args):
             "gpu_launches": args.steps,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
-                         "kernel": "k_accd<%sPol>" % ("Mixed" if prec == F.MIXED else "Exact"),
+                         "kernel": "k_accd_mixed" if prec == F.MIXED else "k_accd<ExactPol>",
                          "peak_source": peak_kind,
-                         "note": "ACCD is FP64-pipe bound on this part; bytes are the algorithmic minimum"},
+                         "note": ("ACCD is instruction-issue bound (FP32 and integer pipes: float-float "
+                                  "distances, ~3.4 distance evaluations per pair), not HBM bound; bytes are the "
+                                  "algorithmic minimum, read once" if prec == F.MIXED else
+                                  "ACCD in FP64 is FP64-pipe bound on this part (1/64 of the FP32 rate); bytes "
+                                  "are the algorithmic minimum, read once")},
             "clocks": clk,
             "variants": variants,
             "cpu_baseline": cpu,
