@@ -272,13 +272,13 @@ CIPC_HD int barrier_one(const BarrierArgs& a, int64_t i)
     if (!(s > 0) || s >= a.shat) {
         a.E[i] = 0;
         for (int k = 0; k < 12; ++k) gout[k] = 0;
-        const int m = 3 * nv;
-        for (int k = 0; k < m * (m + 1) / 2; ++k) hout[k] = 0;
+        for (int k = 0; k < 78; ++k) hout[k] = 0;
         return (s > 0) ? 0 : 1;
     }
     double bv, bg, bh;
     barrier3(s, a.shat, a.kappa, bv, bg, bh);
     for (int k = 3 * nv; k < 12; ++k) gout[k] = 0;
+    for (int k = 3 * nv * (3 * nv + 1) / 2; k < 78; ++k) hout[k] = 0;  // unused tail of PP / PE records
     switch (tp) {
         case kPP: pair_body<HT, kPP>(a, i, xv, bv, bg, bh, gout, hout); break;
         case kPE: pair_body<HT, kPE>(a, i, xv, bv, bg, bh, gout, hout); break;

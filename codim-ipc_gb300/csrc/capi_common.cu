@@ -34,6 +34,21 @@ int ensure_device()
         cudaGetLastError();
         return set_error(CIPC_ERR_NO_DEVICE, "no CUDA device available (%s)", cudaGetErrorString(e));
     }
+    // Host-buffer calls stage their inputs in stream-ordered allocations; the
+    // default pool would hand that memory back to the driver at every
+    // synchronisation and map it again on the next call (milliseconds for the
+    // ~2 GB of a 10M-pair pass), so up to 8 GiB of freed blocks stay reserved.
+    static bool pool_set[64] = {false};
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && !pool_set[dev]) {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t keep = 8ull << 30;
+            if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) == cudaSuccess)
+                pool_set[dev] = true;
+        }
+        cudaGetLastError();
+    }
     return CIPC_OK;
 }
 

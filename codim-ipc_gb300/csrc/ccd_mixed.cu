@@ -4,10 +4,13 @@
 // FP64 arithmetic in the loop, on a part whose FP64 pipe issues 1/64 of the FP32
 // rate (the previous form of this kernel, FP64 distance numerators, kept the FP64
 // pipe 87% busy with the FP32 pipe at 1.5%):
-//   * The inputs are split into float-float values (ff.cuh) by integer operations
-//     on their bit patterns; a pair is carried by its translation-free difference
-//     vectors r(s) = r(0) + s dr, affine in time and evaluated in float-float from
-//     the t = 0 values (no accumulated position updates).
+//   * A pair is carried by its translation-free difference vectors r(s) = r(0) +
+//     s dr, affine in time.  The 18 differences (positions and displacements) are
+//     the only FP64 operations: one subtraction each, exact for nearby vertices
+//     (Sterbenz), so precision does not depend on where the scene sits; they are
+//     then split into float-float values (ff.cuh) by integer operations on their
+//     bit patterns, and r(s) is evaluated in float-float from the t = 0 values (no
+//     accumulated position updates).
 //   * Each pair is rescaled by a power of two (exact) so that its largest
 //     difference component is ~1: ACCD's step and stopping test are invariant under
 //     a common scaling of positions, displacements and xi, and the FP32 ratios
@@ -224,17 +227,17 @@ struct MixedState {
     int64_t adv;
 };
 
+__device__ __forceinline__ ff3 ffd(d3 a) { return ff3{ff_from_double(a.x), ff_from_double(a.y), ff_from_double(a.z)}; }
 __device__ __forceinline__ float f3_norm(f3 a) { return sqrtf(fdot(a, a)); }
 __device__ __forceinline__ float amax3(const ff3& v)
 {
     return fmaxf(fmaxf(fabsf(v.x.hi), fabsf(v.y.hi)), fabsf(v.z.hi));
 }
 
-// Sets up pair pid from its vertices (positions v, displacements dv, as
-// float-float).  Returns 0 when the pair needs stepping, otherwise writes the
+// Sets up pair pid from its vertices (positions v, displacements dv).  Returns 0 when the pair needs stepping, otherwise writes the
 // pair's result and returns 1 (no motion).
 __device__ __forceinline__ int mixed_init(const CcdArgs& a, const ff& th_ff, float oneme, int64_t pid, int tp,
-                                          const ff3 (&v)[4], const ff3 (&dv)[4], MixedState& S)
+                                          const d3 (&v)[4], const d3 (&dv)[4], MixedState& S)
 {
     S.tp = tp;
     const ff3 z3 = ff3{ffv(0.f), ffv(0.f), ffv(0.f)};
@@ -246,17 +249,17 @@ __device__ __forceinline__ int mixed_init(const CcdArgs& a, const ff& th_ff, flo
     float maxDisp;
     switch (tp) {
         case kPP: {
-            L.r0[0] = ff3_sub(v[0], v[1]);
-            L.dr[0] = ff3_sub(dv[0], dv[1]);
+            L.r0[0] = ffd(v[0] - v[1]);
+            L.dr[0] = ffd(dv[0] - dv[1]);
             L.r0[1] = L.r0[2] = L.dr[1] = L.dr[2] = z3;
             maxDisp = f3_norm(hi3(L.dr[0]));
             break;
         }
         case kPE: {
-            L.r0[0] = ff3_sub(v[0], v[1]);
-            L.dr[0] = ff3_sub(dv[0], dv[1]);
-            L.r0[1] = ff3_sub(v[2], v[1]);
-            L.dr[1] = ff3_sub(dv[2], dv[1]);
+            L.r0[0] = ffd(v[0] - v[1]);
+            L.dr[0] = ffd(dv[0] - dv[1]);
+            L.r0[1] = ffd(v[2] - v[1]);
+            L.dr[1] = ffd(dv[2] - dv[1]);
             L.r0[2] = L.dr[2] = z3;
             const f3 B0 = hi3(L.dr[0]), B2 = hi3(L.dr[1]);
             const float third = 1.f / 3.f;
@@ -265,24 +268,24 @@ __device__ __forceinline__ int mixed_init(const CcdArgs& a, const ff& th_ff, flo
             break;
         }
         case kPT: {
-            L.r0[0] = ff3_sub(v[0], v[1]);
-            L.dr[0] = ff3_sub(dv[0], dv[1]);
-            L.r0[1] = ff3_sub(v[2], v[1]);
-            L.dr[1] = ff3_sub(dv[2], dv[1]);
-            L.r0[2] = ff3_sub(v[3], v[1]);
-            L.dr[2] = ff3_sub(dv[3], dv[1]);
+            L.r0[0] = ffd(v[0] - v[1]);
+            L.dr[0] = ffd(dv[0] - dv[1]);
+            L.r0[1] = ffd(v[2] - v[1]);
+            L.dr[1] = ffd(dv[2] - dv[1]);
+            L.r0[2] = ffd(v[3] - v[1]);
+            L.dr[2] = ffd(dv[3] - dv[1]);
             const f3 D0 = hi3(L.dr[0]), D2 = hi3(L.dr[1]), D3 = hi3(L.dr[2]);
             const f3 M = f3{0.25f * (D0.x + D2.x + D3.x), 0.25f * (D0.y + D2.y + D3.y), 0.25f * (D0.z + D2.z + D3.z)};
             maxDisp = f3_norm(D0 - M) + fmaxf(fmaxf(f3_norm(M), f3_norm(D2 - M)), f3_norm(D3 - M));
             break;
         }
         default: {
-            L.r0[0] = ff3_sub(v[1], v[0]);
-            L.dr[0] = ff3_sub(dv[1], dv[0]);
-            L.r0[1] = ff3_sub(v[3], v[2]);
-            L.dr[1] = ff3_sub(dv[3], dv[2]);
-            L.r0[2] = ff3_sub(v[0], v[2]);
-            L.dr[2] = ff3_sub(dv[0], dv[2]);
+            L.r0[0] = ffd(v[1] - v[0]);
+            L.dr[0] = ffd(dv[1] - dv[0]);
+            L.r0[1] = ffd(v[3] - v[2]);
+            L.dr[1] = ffd(dv[3] - dv[2]);
+            L.r0[2] = ffd(v[0] - v[2]);
+            L.dr[2] = ffd(dv[0] - dv[2]);
             // relative to eb0: ea0 moves by A0 = w rate, ea1 by A0 + u rate, eb1 by v rate
             const f3 A0 = hi3(L.dr[2]), A1 = hi3(L.dr[2]) + hi3(L.dr[0]), A3 = hi3(L.dr[1]);
             const f3 M = f3{0.25f * (A0.x + A1.x + A3.x), 0.25f * (A0.y + A1.y + A3.y), 0.25f * (A0.z + A1.z + A3.z)};
@@ -432,20 +435,17 @@ __global__ void __launch_bounds__(kAccdThreads) k_accd_mixed(CcdArgs a)
             } else {
                 cp_async_wait_all();
                 const int nv = pair_nv(tq);
-                const ff3 z3 = ff3{ffv(0.f), ffv(0.f), ffv(0.f)};
-                ff3 v[4], dv[4];
+                d3 v[4], dv[4];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     if (k < nv) {
                         const double* px = slot + (3 * k) * kAccdThreads + tid;
                         const double* pd = slot + (12 + 3 * k) * kAccdThreads + tid;
-                        v[k] = ff3{ff_from_double(px[0]), ff_from_double(px[kAccdThreads]),
-                                   ff_from_double(px[2 * kAccdThreads])};
-                        dv[k] = ff3{ff_from_double(pd[0]), ff_from_double(pd[kAccdThreads]),
-                                    ff_from_double(pd[2 * kAccdThreads])};
+                        v[k] = d3{px[0], px[kAccdThreads], px[2 * kAccdThreads]};
+                        dv[k] = d3{pd[0], pd[kAccdThreads], pd[2 * kAccdThreads]};
                     } else {
-                        v[k] = z3;
-                        dv[k] = z3;
+                        v[k] = mk(0, 0, 0);
+                        dv[k] = mk(0, 0, 0);
                     }
                 }
                 if (mixed_init(a, th_ff, oneme, q, tq, v, dv, S) == 0) pid = q;

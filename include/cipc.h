@@ -115,7 +115,7 @@ int cipc_ccd_pairs_noalloc(int64_t n_pairs, const uint8_t* type, const int32_t* 
  * |ea x eb|^2 < 1e-3 |ea_rest|^2 |eb_rest|^2 (EDGE_EDGE_MOLLIFIER.h:582-591).
  * Outputs: energy[i]; grad[12*i + k] (first 3*nv used, rest zero); hess[78*i + k] =
  * upper triangle of the (3nv x 3nv) Hessian packed row by row (first
- * 3nv(3nv+1)/2 used), doubles for CIPC_PRECISION_FP64 and floats for
+ * 3nv(3nv+1)/2 used, rest zero), doubles for CIPC_PRECISION_FP64 and floats for
  * CIPC_PRECISION_MIXED.  Pairs with s >= shat are inactive (all zeros).  Pairs
  * with s <= 0 are counted in *n_nonpositive (optional) and make the call return
  * CIPC_ERR_NONPOSITIVE_DISTANCE (the reference exits there, IPC.h:773-776).

@@ -65,6 +65,23 @@ def test_ccd_mixed_against_fp64_oracle(cuda, orc):
     assert rel.max() <= 1e-2, rel.max()
 
 
+@pytest.mark.parametrize("precision", [F.FP64, F.MIXED])
+def test_ccd_scale_invariant(cuda, precision):
+    # ACCD's steps and stopping test are invariant under a common scaling of
+    # positions, displacements and xi; by a power of two every rounding scales
+    # exactly, so the answers must be bit-identical (the mixed kernel's float-float
+    # split and per-pair rescaling included) at scales far from the unit cube
+    w = workloads.contact_pairs(100_000, seed=8, mix=(0.25, 0.25, 0.25, 0.25))
+    toc0, hit0, st, _ = _gpu_ccd(w, precision)
+    assert st == 0 and 0 < hit0.sum() < hit0.size
+    for k in (-40, 40):
+        ws = dict(w, x=w["x"] * 2.0 ** k, dx=w["dx"] * 2.0 ** k)
+        toc, hit, st, _ = _gpu_ccd(ws, precision, th=TH * 2.0 ** k)
+        assert st == 0
+        assert np.array_equal(hit, hit0), k
+        assert np.array_equal(toc.view(np.uint64), toc0.view(np.uint64)), k
+
+
 def test_ccd_device_memory_matches_host(cuda):
     import torch
     w = workloads.contact_pairs(50_000, seed=4)
