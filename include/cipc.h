@@ -37,7 +37,9 @@ extern "C" {
 #define CIPC_ERR_INDEX_RANGE 8
 
 #define CIPC_PRECISION_FP64 0  /* all-FP64, decisions bit-exact with the CPU restatement */
-#define CIPC_PRECISION_MIXED 1 /* FP32 classification / Hessians, FP64 distances and times */
+#define CIPC_PRECISION_MIXED 1 /* FP32 classification and Hessians; barrier distances FP64; CCD   \
+                                  distances and times in float-float (FP32 pairs, ~47 bits) from \
+                                  FP64 vertex differences */
 #define CIPC_BARRIER_OFFSET 0  /* offset IPC (C-IPC): barrier on d^2 - xi^2 */
 #define CIPC_BARRIER_ELASTIC 1 /* elastic IPC: no offset, barrier normalised by dhat */
 
@@ -69,6 +71,9 @@ int cipc_device_count(void);
  * iteration cap (2^20 steps) — they are reported as no hit; with any overflow the
  * call returns CIPC_ERR_ITER_CAP.  Pairs with an index outside [0, n_verts) or a
  * type above 3 are not evaluated and make the call return CIPC_ERR_INDEX_RANGE.
+ * With CIPC_MEM_HOST the inputs are staged in stream-ordered allocations and
+ * the call returns after the results are back; n_pairs above 2.5M are streamed
+ * in chunks (records in, results out) around the kernel on internal streams.
  */
 int cipc_ccd_pairs(int64_t n_pairs, const uint8_t* type, const int32_t* idx, int64_t n_verts,
                    const double* x, const double* dx, double eta, double thickness, double toc_in,
