@@ -12,7 +12,8 @@ def _declared():
     names = []
     for h in os.listdir(os.path.join(ROOT, "include")):
         if h.endswith(".h"):
-            src = open(os.path.join(ROOT, "include", h)).read()
+            with open(os.path.join(ROOT, "include", h)) as f:
+                src = f.read()
             src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
             names += re.findall(r"\b(cipc_\w+)\s*\(", src)
     return sorted(set(names))

@@ -49,7 +49,7 @@ def _rank_main(rank, ws, port, out):
 def test_two_replicas_max_over_ranks():
     ws = 2
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_rank_main, args=(ws, port, out), nprocs=ws, join=True)
         res = dict(out)

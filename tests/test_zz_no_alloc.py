@@ -21,7 +21,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def test_noalloc_source_has_no_allocation_calls():
     """The no-allocation translation unit names no allocating CUDA call outside comments."""
-    src = open(os.path.join(ROOT, "codim-ipc_gb300", "csrc", "capi_noalloc.cu")).read()
+    with open(os.path.join(ROOT, "codim-ipc_gb300", "csrc", "capi_noalloc.cu")) as f:
+        src = f.read()
     code = re.sub(r"//[^\n]*", "", re.sub(r"/\*.*?\*/", "", src, flags=re.S))
     for name in ("cudaMalloc", "cudaFree", "cudaHostAlloc", "cudaMallocHost", "cudaMallocManaged", "new ",
                  "malloc(", "std::vector"):
