@@ -8,8 +8,10 @@
 ``oracle/_ref/libcipc_ref.so`` when the Codim-IPC sources are available.  The
 reference as a whole needs Eigen, Boost, SuiteSparse and Kokkos and cannot be
 built here, but its symbolic-toolbox derivative routines (``g_PT``, ``H_PT``,
-``g_EE``, ``H_EE``, ``g_PE3D``, ``H_PE3D``, ``g_EECN2``, ``H_EECN2``) and its
-barrier functions are plain scalar C++.  They are cut out of the headers where
+``g_EE``, ``H_EE``, ``g_PE3D``, ``H_PE3D``, ``g_EECN2``, ``H_EECN2``, the rod's
+``g_MS``/``H_MS``/``g_RB``/``H_RB``), its contact barrier functions and its
+strain-limiting barrier (``f/g/h_sl_u``, ``f/g/h_sl_l`` of INEXT.h) are plain
+scalar C++.  They are cut out of the headers where
 they lie and piped straight into g++ (nothing is written to disk but the .so),
 so the oracle's own derivation can be pinned against them.
 """
@@ -52,12 +54,18 @@ _REF_FUNCS = [
     ("Library/FEM/Shell/Rod/MASS_SPRING_DERIVATIVES.h", "H_MS"),
     ("Library/FEM/Shell/Rod/ROD_BENDING_DERIVATIVES.h", "g_RB"),
     ("Library/FEM/Shell/Rod/ROD_BENDING_DERIVATIVES.h", "H_RB"),
+    ("Library/FEM/Shell/INEXT.h", "f_sl_u"),
+    ("Library/FEM/Shell/INEXT.h", "g_sl_u"),
+    ("Library/FEM/Shell/INEXT.h", "h_sl_u"),
+    ("Library/FEM/Shell/INEXT.h", "f_sl_l"),
+    ("Library/FEM/Shell/INEXT.h", "g_sl_l"),
+    ("Library/FEM/Shell/INEXT.h", "h_sl_l"),
 ]
 
 
 def _extract(text, name):
     """Return `template <...> ... name(...) { ... }` cut from text by brace matching."""
-    m = re.search(r"template\s*<[^>]*>\s*(?:inline\s+)?void\s+" + re.escape(name) + r"\s*\(", text)
+    m = re.search(r"template\s*<[^>]*>\s*(?:inline\s+)?(?:void|T)\s+" + re.escape(name) + r"\s*\(", text)
     if not m:
         raise RuntimeError("function %s not found" % name)
     start = m.start()
@@ -112,6 +120,10 @@ def build_ref(force=False):
                  "void ref_H_MS(double k, double l, const double* x, double* H) { ref::H_MS<double>(k, l, %s, H); }\n"
                  "void ref_g_RB(const double* x, double* g) { ref::g_RB<double>(%s, g); }\n"
                  "void ref_H_RB(const double* x, double* H) { ref::H_RB<double>(%s, H); }\n"
+                 "void ref_sl(double s, double slim, double shat, double* out) {\n"
+                 "  out[0] = ref::f_sl_u<double>(s, slim, shat); out[1] = ref::g_sl_u<double>(s, slim, shat);\n"
+                 "  out[2] = ref::h_sl_u<double>(s, slim, shat); out[3] = ref::f_sl_l<double>(s, slim, shat);\n"
+                 "  out[4] = ref::g_sl_l<double>(s, slim, shat); out[5] = ref::h_sl_l<double>(s, slim, shat); }\n"
                  "}\n" % (args12, args12, args12, args12, args9, args9, args12, args12, args6, args6, args9, args9))
     src = "".join(parts)
     cmd = ["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-x", "c++", "-", "-o", out]

@@ -357,6 +357,15 @@ def rod_bending(x9, lsum, Kb, project=True):
     return E, g, H
 
 
+def sl_barrier(s, lim, hat):
+    """(value, d/ds, d2/ds2) of the strain-limiting barrier of one singular value."""
+    lb = lib()
+    lb.orc_sl_barrier.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, _P]
+    out = np.zeros(3)
+    lb.orc_sl_barrier(s, lim, hat, _p(out))
+    return out
+
+
 def strain_limit_elem(x9, P, kh, s, s_hat, kappa_s, project=True):
     """(E, g[9], H[9x9], valid) of the strain-limiting barrier of one triangle;
     P the inverse rest first fundamental form (p00, p01, p11), kh = h^2 vol."""

@@ -130,6 +130,19 @@ double orc_sl_elem(const double* x9, const double* P, double kh, const double* s
     return Ev;
 }
 
+// The barrier of one singular value s against the limit lim with activation
+// threshold hat (upper: hat < s < lim; lower: lim < s < hat): out = value,
+// first and second derivative in s, by the same dual numbers as the element.
+void orc_sl_barrier(double s, double lim, double hat, double* out)
+{
+    using namespace orc_sl;
+    const D2<1> sd = seed<1>(s, 0);
+    const D2<1> f = barrier(sd, lim, hat);
+    out[0] = f.v.v;
+    out[1] = f.v.d[0];
+    out[2] = f.d[0].d[0];
+}
+
 // largest stretch of one triangle (the reference's Compute_Inextensibility)
 double orc_sl_strain(const double* x9, const double* P)
 {

@@ -1,8 +1,8 @@
 """Generates tests/golden/reference_derivs.npz from the reference's own code.
 
 The reference's symbolic-toolbox derivative routines (g_PT/H_PT, g_EE/H_EE,
-g_PE3D/H_PE3D, g_EECN2/H_EECN2, the rod's g_MS/H_MS and g_RB/H_RB) and its
-barrier functions are compiled from the
+g_PE3D/H_PE3D, g_EECN2/H_EECN2, the rod's g_MS/H_MS and g_RB/H_RB), its contact
+barrier functions and its strain-limiting barrier (INEXT.h) are compiled from the
 Codim-IPC sources by ``oracle/build.py:build_ref`` into
 ``oracle/_ref/libcipc_ref.so``; this script evaluates them on seeded inputs and
 stores inputs and outputs, so that the oracle and the CUDA kernels can be
@@ -10,7 +10,8 @@ checked against the reference on machines without its sources.
 
 Inputs: 48 random vertex sets per kind (standard normal coordinates) plus the
 fixed vertex set of the reference's derivTest_EECross / derivTest_e
-(EDGE_EDGE_MOLLIFIER.h:384-438), and barrier arguments spanning 1e-12..1.
+(EDGE_EDGE_MOLLIFIER.h:384-438), barrier arguments spanning 1e-12..1, and
+strain-limit triples (s, limit, threshold) on both sides of 1.
 Run:  python tests/golden/make_golden.py
 """
 import ctypes
@@ -89,6 +90,27 @@ def main():
         L.ref_H_RB(xx.ctypes.data, h.ctypes.data)
         GB[i], HB[i] = g, h.reshape(9, 9)
     out.update(x_RB=XB, g_RB=GB, H_RB=HB)
+    # strain-limiting barrier of one singular value (INEXT.h f/g/h_sl_u for the
+    # upper limit, f/g/h_sl_l for the lower), from its own seeded stream so the
+    # arrays above are unchanged
+    L.ref_sl.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, P]
+    rs = np.random.default_rng(20240601)
+    rows = []
+    for _ in range(48):
+        slim = 1.0 + 10.0 ** rs.uniform(-3, -0.5)
+        shat = 1.0 + (slim - 1.0) * rs.uniform(0.0, 0.9)
+        sv = shat + (slim - shat) * rs.uniform(0.02, 0.98)
+        o = np.zeros(6)
+        L.ref_sl(sv, slim, shat, o.ctypes.data)
+        rows.append([0, sv, slim, shat, o[0], o[1], o[2]])
+    for _ in range(48):
+        slim = 1.0 - 10.0 ** rs.uniform(-3, -0.5)
+        shat = 1.0 - (1.0 - slim) * rs.uniform(0.0, 0.9)
+        sv = shat - (shat - slim) * rs.uniform(0.02, 0.98)
+        o = np.zeros(6)
+        L.ref_sl(sv, slim, shat, o.ctypes.data)
+        rows.append([1, sv, slim, shat, o[3], o[4], o[5]])
+    out["strain_barrier"] = np.array(rows)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_derivs.npz")
     np.savez_compressed(dst, **out)
     print("wrote", dst, os.path.getsize(dst), "bytes")

@@ -35,6 +35,18 @@ def test_barrier_matches_reference(orc):
             assert abs(mine - ref) <= 1e-12 * max(abs(ref), 1e-300)
 
 
+def test_strain_barrier_matches_reference(orc):
+    # the strain-limiting barrier of one singular value against the reference's
+    # f/g/h_sl_u (upper limit) and f/g/h_sl_l (lower limit) of INEXT.h, C2 form
+    z = np.load(GOLD)
+    rows = z["strain_barrier"]
+    assert set(rows[:, 0]) == {0.0, 1.0}
+    for _, sv, slim, shat, f, g, h in rows:
+        out = orc.sl_barrier(sv, slim, shat)
+        for mine, ref in zip(out, (f, g, h)):
+            assert abs(mine - ref) <= 1e-13 * max(abs(ref), 1e-300), (sv, slim, shat, mine, ref)
+
+
 def _fd_grad(f, x, eps):
     g = np.zeros_like(x)
     for i in range(x.size):
