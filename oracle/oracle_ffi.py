@@ -357,6 +357,15 @@ def rod_bending(x9, lsum, Kb, project=True):
     return E, g, H
 
 
+def friction_scalars(x2, eh):
+    """(f0, f1 / |u|, f2 term) of the friction mollifier at squared slip x2, eh = epsv h."""
+    lb = lib()
+    lb.orc_friction_scalars.argtypes = [ctypes.c_double, ctypes.c_double, _P]
+    out = np.zeros(3)
+    lb.orc_friction_scalars(x2, eh, _p(out))
+    return out
+
+
 def sl_barrier(s, lim, hat):
     """(value, d/ds, d2/ds2) of the strain-limiting barrier of one singular value."""
     lb = lib()

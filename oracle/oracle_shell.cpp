@@ -1139,6 +1139,14 @@ static double f1_div(double x2, double eh)
     if (x2 >= eh * eh) return 1 / std::sqrt(x2);
     return (-std::sqrt(x2) + 2.0 * eh) / (eh * eh);
 }
+// the three friction mollifier scalars for the golden-vector checks:
+// out = (f0, f1 / |u|, f2 term) at squared relative slip x2, eh = epsv h
+extern "C" void orc_friction_scalars(double x2, double eh, double* out)
+{
+    out[0] = f0_sf(x2, eh);
+    out[1] = f1_div(x2, eh);
+    out[2] = -1 / (eh * eh);
+}
 
 static void friction_terms(const std::vector<Fric>& F, const double* x, const double* xn, double epsvh2, double mu,
                            double* E, double* g, Asm* A)

@@ -2,7 +2,8 @@
 
 The reference's symbolic-toolbox derivative routines (g_PT/H_PT, g_EE/H_EE,
 g_PE3D/H_PE3D, g_EECN2/H_EECN2, the rod's g_MS/H_MS and g_RB/H_RB), its contact
-barrier functions and its strain-limiting barrier (INEXT.h) are compiled from the
+barrier functions, its strain-limiting barrier (INEXT.h) and its friction
+mollifier (FRICTION_UTILS.h) are compiled from the
 Codim-IPC sources by ``oracle/build.py:build_ref`` into
 ``oracle/_ref/libcipc_ref.so``; this script evaluates them on seeded inputs and
 stores inputs and outputs, so that the oracle and the CUDA kernels can be
@@ -11,7 +12,8 @@ checked against the reference on machines without its sources.
 Inputs: 48 random vertex sets per kind (standard normal coordinates) plus the
 fixed vertex set of the reference's derivTest_EECross / derivTest_e
 (EDGE_EDGE_MOLLIFIER.h:384-438), barrier arguments spanning 1e-12..1, and
-strain-limit triples (s, limit, threshold) on both sides of 1.
+strain-limit triples (s, limit, threshold) on both sides of 1, and squared
+slips on both sides of the friction mollifier's switch.
 Run:  python tests/golden/make_golden.py
 """
 import ctypes
@@ -111,6 +113,18 @@ def main():
         L.ref_sl(sv, slim, shat, o.ctypes.data)
         rows.append([1, sv, slim, shat, o[3], o[4], o[5]])
     out["strain_barrier"] = np.array(rows)
+    # friction mollifier (FRICTION_UTILS.h f0_SF, f1_SF_Div_RelDXNorm, f2_SF_Term)
+    # on both sides of the C1 switch |u| = epsv h
+    L.ref_friction.argtypes = [ctypes.c_double, ctypes.c_double, P]
+    rf = np.random.default_rng(20240602)
+    rows = []
+    for _ in range(64):
+        eh = 10.0 ** rf.uniform(-8, -2)
+        x2 = (eh * 10.0 ** rf.uniform(-3, 1)) ** 2
+        o = np.zeros(3)
+        L.ref_friction(x2, eh, o.ctypes.data)
+        rows.append([x2, eh, o[0], o[1], o[2]])
+    out["friction"] = np.array(rows)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_derivs.npz")
     np.savez_compressed(dst, **out)
     print("wrote", dst, os.path.getsize(dst), "bytes")

@@ -47,6 +47,18 @@ def test_strain_barrier_matches_reference(orc):
             assert abs(mine - ref) <= 1e-13 * max(abs(ref), 1e-300), (sv, slim, shat, mine, ref)
 
 
+def test_friction_mollifier_matches_reference(orc):
+    # f0, f1 / |u| and the f2 term of the C1 friction mollifier against the
+    # reference's FRICTION_UTILS.h on both sides of |u| = epsv h
+    z = np.load(GOLD)
+    rows = z["friction"]
+    assert (rows[:, 0] < rows[:, 1] ** 2).any() and (rows[:, 0] >= rows[:, 1] ** 2).any()
+    for x2, eh, f0, f1, f2 in rows:
+        out = orc.friction_scalars(x2, eh)
+        for mine, ref in zip(out, (f0, f1, f2)):
+            assert abs(mine - ref) <= 1e-14 * abs(ref), (x2, eh, mine, ref)
+
+
 def _fd_grad(f, x, eps):
     g = np.zeros_like(x)
     for i in range(x.size):
