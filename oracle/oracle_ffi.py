@@ -357,6 +357,16 @@ def rod_bending(x9, lsum, Kb, project=True):
     return E, g, H
 
 
+def dihedral_derivs(x12):
+    """(gradient[12], Hessian[12x12]) of the signed dihedral angle of a hinge stencil."""
+    lb = lib()
+    lb.orc_dihedral_derivs.argtypes = [_P, _P, _P]
+    g = np.zeros(12)
+    H = np.zeros((12, 12))
+    lb.orc_dihedral_derivs(_p(_c(x12, np.float64)), _p(g), _p(H))
+    return g, H
+
+
 def friction_scalars(x2, eh):
     """(f0, f1 / |u|, f2 term) of the friction mollifier at squared slip x2, eh = epsv h."""
     lb = lib()

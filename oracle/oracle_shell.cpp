@@ -2071,6 +2071,15 @@ double orc_membrane_elem(const double* x9, const double* P, double k, double lam
     return membrane_energy(x9, P, k, lam, mu, nh);
 }
 
+// gradient and Hessian of the dihedral angle itself (the bending element's
+// building block), for the golden-vector checks
+void orc_dihedral_derivs(const double* x12, double* g, double* H)
+{
+    dihedral_grad<double>(x12, g);
+    auto gf = [&](const Du* xx, Du* gg) { dihedral_grad<Du>(xx, gg); };
+    hess_from_grad<12>(x12, gf, H);
+}
+
 double orc_bending_elem(const double* x12, double thetabar, double c, int project, double* g, double* H)
 {
     bending_grad_d(x12, thetabar, c, g);

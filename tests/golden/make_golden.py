@@ -3,7 +3,7 @@
 The reference's symbolic-toolbox derivative routines (g_PT/H_PT, g_EE/H_EE,
 g_PE3D/H_PE3D, g_EECN2/H_EECN2, the rod's g_MS/H_MS and g_RB/H_RB), its contact
 barrier functions, its strain-limiting barrier (INEXT.h) and its friction
-mollifier (FRICTION_UTILS.h) are compiled from the
+mollifier (FRICTION_UTILS.h) and its dihedral-angle derivatives are compiled from the
 Codim-IPC sources by ``oracle/build.py:build_ref`` into
 ``oracle/_ref/libcipc_ref.so``; this script evaluates them on seeded inputs and
 stores inputs and outputs, so that the oracle and the CUDA kernels can be
@@ -12,8 +12,8 @@ checked against the reference on machines without its sources.
 Inputs: 48 random vertex sets per kind (standard normal coordinates) plus the
 fixed vertex set of the reference's derivTest_EECross / derivTest_e
 (EDGE_EDGE_MOLLIFIER.h:384-438), barrier arguments spanning 1e-12..1, and
-strain-limit triples (s, limit, threshold) on both sides of 1, and squared
-slips on both sides of the friction mollifier's switch.
+strain-limit triples (s, limit, threshold) on both sides of 1, squared slips
+on both sides of the friction mollifier's switch, and 48 random hinge stencils.
 Run:  python tests/golden/make_golden.py
 """
 import ctypes
@@ -125,6 +125,22 @@ def main():
         L.ref_friction(x2, eh, o.ctypes.data)
         rows.append([x2, eh, o[0], o[1], o[2]])
     out["friction"] = np.array(rows)
+    # dihedral-angle gradient and Hessian (DIHEDRAL_ANGLE.h g_DA / H_DA, generated
+    # for the unsigned acos angle) on random hinge stencils (x0, x1, x2, x3)
+    L.ref_g_DA.argtypes = [P, P]
+    L.ref_H_DA.argtypes = [P, P]
+    rd = np.random.default_rng(20240603)
+    XD = rd.standard_normal((48, 12))
+    GD = np.zeros((48, 12))
+    HD = np.zeros((48, 12, 12))
+    for i in range(48):
+        xx = np.ascontiguousarray(XD[i])
+        g = np.zeros(12)
+        h = np.zeros(144)
+        L.ref_g_DA(xx.ctypes.data, g.ctypes.data)
+        L.ref_H_DA(xx.ctypes.data, h.ctypes.data)
+        GD[i], HD[i] = g, h.reshape(12, 12)
+    out.update(x_DA=XD, g_DA=GD, H_DA=HD)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_derivs.npz")
     np.savez_compressed(dst, **out)
     print("wrote", dst, os.path.getsize(dst), "bytes")

@@ -59,6 +59,23 @@ def test_friction_mollifier_matches_reference(orc):
             assert abs(mine - ref) <= 1e-14 * abs(ref), (x2, eh, mine, ref)
 
 
+def test_dihedral_angle_derivatives_match_reference(orc):
+    # the reference's generated g_DA / H_DA differentiate the unsigned (acos)
+    # angle; the bending energy uses the signed one, so they agree up to the sign
+    # of the angle, (n2 x n1).(x1 - x2) with n1 = (x1-x0) x (x2-x0), n2 = (x2-x3) x (x1-x3)
+    z = np.load(GOLD)
+    signs = set()
+    for x, g_ref, h_ref in zip(z["x_DA"], z["g_DA"], z["H_DA"]):
+        v0, v1, v2, v3 = x[:3], x[3:6], x[6:9], x[9:]
+        n1, n2 = np.cross(v1 - v0, v2 - v0), np.cross(v2 - v3, v1 - v3)
+        sg = -1.0 if np.cross(n2, n1) @ (v1 - v2) < 0 else 1.0
+        signs.add(sg)
+        g, h = orc.dihedral_derivs(x)
+        assert np.abs(g - sg * g_ref).max() <= 1e-11 * np.abs(g_ref).max()
+        assert np.abs(h - sg * h_ref).max() <= 1e-9 * np.abs(h_ref).max()
+    assert signs == {-1.0, 1.0}
+
+
 def _fd_grad(f, x, eps):
     g = np.zeros_like(x)
     for i in range(x.size):
