@@ -11,8 +11,9 @@ built here, but its symbolic-toolbox derivative routines (``g_PT``, ``H_PT``,
 ``g_EE``, ``H_EE``, ``g_PE3D``, ``H_PE3D``, ``g_EECN2``, ``H_EECN2``, the rod's
 ``g_MS``/``H_MS``/``g_RB``/``H_RB``), its contact barrier functions and its
 strain-limiting barrier (``f/g/h_sl_u``, ``f/g/h_sl_l`` of INEXT.h), friction
-mollifier (``f0_SF``, ``f1_SF_Div_RelDXNorm``, ``f2_SF_Term``) and dihedral-angle
-derivatives (``g_DA``, ``H_DA``) are plain scalar C++.  They are cut out of the headers where
+mollifier (``f0_SF``, ``f1_SF_Div_RelDXNorm``, ``f2_SF_Term``), edge-edge
+mollifier (``EEM``, ``g_EEM``, ``H_EEM``) and dihedral-angle derivatives
+(``g_DA``, ``H_DA``) are plain scalar C++.  They are cut out of the headers where
 they lie and piped straight into g++ (nothing is written to disk but the .so),
 so the oracle's own derivation can be pinned against them.
 """
@@ -66,6 +67,9 @@ _REF_FUNCS = [
     ("Library/FEM/FRICTION_UTILS.h", "f2_SF_Term"),
     ("Library/Math/DIHEDRAL_ANGLE.h", "g_DA"),
     ("Library/Math/DIHEDRAL_ANGLE.h", "H_DA"),
+    ("Library/Math/Distance/EDGE_EDGE_MOLLIFIER.h", "EEM"),
+    ("Library/Math/Distance/EDGE_EDGE_MOLLIFIER.h", "g_EEM"),
+    ("Library/Math/Distance/EDGE_EDGE_MOLLIFIER.h", "H_EEM"),
 ]
 
 
@@ -132,6 +136,9 @@ def build_ref(force=False):
                  "  out[4] = ref::g_sl_l<double>(s, slim, shat); out[5] = ref::h_sl_l<double>(s, slim, shat); }\n"
                  "void ref_g_DA(const double* x, double* g) { ref::g_DA<double>(%s, g); }\n"
                  "void ref_H_DA(const double* x, double* H) { ref::H_DA<double>(%s, H); }\n"
+                 "void ref_eem(double c, double eps, double* out) {\n"
+                 "  ref::EEM<double>(c, eps, out[0]); ref::g_EEM<double>(c, eps, out[1]);\n"
+                 "  ref::H_EEM<double>(c, eps, out[2]); }\n"
                  "void ref_friction(double x2, double eh, double* out) {\n"
                  "  ref::f0_SF<double>(x2, eh, out[0]); ref::f1_SF_Div_RelDXNorm<double>(x2, eh, out[1]);\n"
                  "  ref::f2_SF_Term<double>(x2, eh, out[2]); }\n"

@@ -3,7 +3,8 @@
 The reference's symbolic-toolbox derivative routines (g_PT/H_PT, g_EE/H_EE,
 g_PE3D/H_PE3D, g_EECN2/H_EECN2, the rod's g_MS/H_MS and g_RB/H_RB), its contact
 barrier functions, its strain-limiting barrier (INEXT.h) and its friction
-mollifier (FRICTION_UTILS.h) and its dihedral-angle derivatives are compiled from the
+mollifier (FRICTION_UTILS.h), its edge-edge mollifier scalars and its
+dihedral-angle derivatives are compiled from the
 Codim-IPC sources by ``oracle/build.py:build_ref`` into
 ``oracle/_ref/libcipc_ref.so``; this script evaluates them on seeded inputs and
 stores inputs and outputs, so that the oracle and the CUDA kernels can be
@@ -13,7 +14,8 @@ Inputs: 48 random vertex sets per kind (standard normal coordinates) plus the
 fixed vertex set of the reference's derivTest_EECross / derivTest_e
 (EDGE_EDGE_MOLLIFIER.h:384-438), barrier arguments spanning 1e-12..1, and
 strain-limit triples (s, limit, threshold) on both sides of 1, squared slips
-on both sides of the friction mollifier's switch, and 48 random hinge stencils.
+on both sides of the friction mollifier's switch, 48 random hinge stencils and
+32 edge pairs inside the mollifier's range.
 Run:  python tests/golden/make_golden.py
 """
 import ctypes
@@ -141,6 +143,29 @@ def main():
         L.ref_H_DA(xx.ctypes.data, h.ctypes.data)
         GD[i], HD[i] = g, h.reshape(12, 12)
     out.update(x_DA=XD, g_DA=GD, H_DA=HD)
+    # the edge-edge mollifier e(c) = EEM(c, eps_x) of c = |ea x eb|^2 with its
+    # chain-rule gradient and Hessian (g_EEM / H_EEM with g_EECN2 / H_EECN2)
+    L.ref_eem.argtypes = [ctypes.c_double, ctypes.c_double, P]
+    rm = np.random.default_rng(20240604)
+    XM = rm.standard_normal((32, 12))
+    EPS = np.zeros(32)
+    EM = np.zeros(32)
+    GM = np.zeros((32, 12))
+    HM = np.zeros((32, 12, 12))
+    for i in range(32):
+        xx = np.ascontiguousarray(XM[i])
+        c = float(np.sum(np.cross(xx[3:6] - xx[0:3], xx[9:12] - xx[6:9]) ** 2))
+        EPS[i] = c * rm.uniform(1.05, 20.0)
+        o = np.zeros(3)
+        L.ref_eem(c, EPS[i], o.ctypes.data)
+        g = np.zeros(12)
+        h = np.zeros(144)
+        L.ref_g_EECN2(xx.ctypes.data, g.ctypes.data)
+        L.ref_H_EECN2(xx.ctypes.data, h.ctypes.data)
+        EM[i] = o[0]
+        GM[i] = o[1] * g
+        HM[i] = o[1] * h.reshape(12, 12) + o[2] * np.outer(g, g)
+    out.update(x_EEM=XM, eps_EEM=EPS, e_EEM=EM, g_EEM=GM, H_EEM=HM)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_derivs.npz")
     np.savez_compressed(dst, **out)
     print("wrote", dst, os.path.getsize(dst), "bytes")

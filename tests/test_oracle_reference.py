@@ -76,6 +76,18 @@ def test_dihedral_angle_derivatives_match_reference(orc):
     assert signs == {-1.0, 1.0}
 
 
+def test_ee_mollifier_matches_reference(orc):
+    # e(c) = (2 - c/eps) c/eps of c = |ea x eb|^2 below eps, with gradient and
+    # Hessian by the chain rule, against the reference's EEM / g_EEM / H_EEM
+    # composed with its g_EECN2 / H_EECN2
+    z = np.load(GOLD)
+    for x, eps, e_ref, g_ref, h_ref in zip(z["x_EEM"], z["eps_EEM"], z["e_EEM"], z["g_EEM"], z["H_EEM"]):
+        e, g, h = orc.mollifier(x, eps)
+        assert abs(e - e_ref) <= 1e-14 * abs(e_ref)
+        assert np.abs(g - g_ref).max() <= 1e-10 * np.abs(g_ref).max()
+        assert np.abs(h - h_ref).max() <= 1e-9 * np.abs(h_ref).max()
+
+
 def _fd_grad(f, x, eps):
     g = np.zeros_like(x)
     for i in range(x.size):
