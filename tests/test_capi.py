@@ -32,6 +32,54 @@ def test_library_exports_every_declared_symbol():
     assert set(declared) <= set(cipc_ffi.exported_symbols())
 
 
+def _prototypes():
+    """name -> (return type, [parameter types]) of every cipc_* prototype in include/*.h."""
+    out = {}
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        with open(os.path.join(ROOT, "include", h)) as f:
+            src = re.sub(r"/\*.*?\*/", "", f.read(), flags=re.S)
+        for m in re.finditer(r"([\w\s\*]+?)\b(cipc_\w+)\s*\(([^;{]*?)\)\s*;", src):
+            params = [p.strip() for p in m.group(3).split(",") if p.strip() and p.strip() != "void"]
+            out[m.group(2)] = (m.group(1).split()[-1], params)
+    return out
+
+
+def _kind_c(decl):
+    """Coarse ABI class of a C parameter declaration."""
+    if "*" in decl:
+        return "ptr"
+    t = decl.replace("const", "").split()[0]
+    return {"int64_t": "i64", "uint64_t": "i64", "int": "i32", "int32_t": "i32", "uint32_t": "i32",
+            "double": "f64", "float": "f32"}.get(t, t)
+
+
+def _kind_ctypes(t):
+    if t in (ctypes.c_int64, ctypes.c_longlong, ctypes.c_uint64, ctypes.c_ulonglong):
+        return "i64"
+    if t in (ctypes.c_int, ctypes.c_int32, ctypes.c_uint32):
+        return "i32"
+    if t is ctypes.c_double:
+        return "f64"
+    if t is ctypes.c_float:
+        return "f32"
+    return "ptr"  # c_void_p, c_char_p and POINTER(...)
+
+
+def test_ctypes_signatures_match_header():
+    # a drift between include/cipc.h and the ctypes table would pass arguments in
+    # the wrong registers without any error; compare count and kind of every one
+    import cipc_ffi
+    protos = _prototypes()
+    assert set(_declared()) <= set(protos)
+    for name, (_, params) in protos.items():
+        args = cipc_ffi._SIGS[name][1]
+        assert len(args) == len(params), (name, params, args)
+        for decl, t in zip(params, args):
+            assert _kind_c(decl) == _kind_ctypes(t), (name, decl, t)
+
+
 def test_host_only_entry_points():
     import cipc_ffi
     assert cipc_ffi.lib().cipc_version().startswith(b"cipc-gb300")
