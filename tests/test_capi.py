@@ -80,6 +80,39 @@ def test_ctypes_signatures_match_header():
             assert _kind_c(decl) == _kind_ctypes(t), (name, decl, t)
 
 
+def test_struct_layouts_match_header(tmp_path):
+    # the ctypes mirrors of the ABI structs must have the C compiler's field
+    # offsets and sizes: a C program built against include/cipc.h prints them
+    import shutil
+    import subprocess
+
+    import cipc_ffi
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    structs = {"cipc_step_params": cipc_ffi.StepParams, "cipc_step_stats": cipc_ffi.StepStats,
+               "cipc_codim_desc": cipc_ffi.CodimDesc, "cipc_tet_desc": cipc_ffi.TetDesc}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "cipc.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append('printf("%s sizeof %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines += ["return 0; }"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = str(tmp_path / "layout")
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", exe], check=True)
+    got = {}
+    for line in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.splitlines():
+        cname, field, v = line.split()
+        got[(cname, field)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "sizeof")] == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
 def test_host_only_entry_points():
     import cipc_ffi
     assert cipc_ffi.lib().cipc_version().startswith(b"cipc-gb300")
