@@ -161,3 +161,27 @@ def test_noalloc_argument_validation_without_gpu():
     st, ov = cipc_ffi.ccd_pairs_noalloc(e0, np.zeros((0, 4), np.int32), x, x, np.zeros(0), np.zeros(0, np.uint8),
                                         slot=cipc_ffi.NOALLOC_SLOTS - 1)
     assert st == cipc_ffi.CIPC_OK and ov == 0
+
+
+def test_fails_loudly_without_gpu_or_library():
+    """The product path has no CPU fallback: without a CUDA device a compute call
+    returns CIPC_ERR_NO_DEVICE, and without the built library the binding raises."""
+    import subprocess
+    import sys
+
+    import cipc_ffi
+    if cipc_ffi.lib().cipc_device_count() == 0:
+        t = np.zeros(1, np.uint8)
+        idx = np.array([[0, 1, -1, -1]], np.int32)
+        x = np.zeros((2, 3))
+        try:
+            cipc_ffi.ccd_pairs(t, idx, x, x + 1.0, np.zeros(1), np.zeros(1, np.uint8))
+            raise AssertionError("expected an error without a device")
+        except cipc_ffi.CipcError as e:
+            assert e.status == cipc_ffi.CIPC_ERR_NO_DEVICE
+    code = ("import sys; sys.path.insert(0, %r); import cipc_ffi\n"
+            "cipc_ffi.LIB_PATH = '/nonexistent/libcipc.so'; cipc_ffi._lib = None\n"
+            "try:\n    cipc_ffi.lib()\nexcept ImportError as e:\n    print('raised', e)\n"
+            % os.path.join(ROOT, "codim-ipc_gb300"))
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert out.stdout.startswith("raised"), out.stdout + out.stderr
