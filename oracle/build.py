@@ -126,6 +126,11 @@ def build_ref(force=False):
                  "  ref::Barrier<false>(d, dHat, k, out[0]);\n"
                  "  ref::Barrier_Gradient<false>(d, dHat, k, out[1]);\n"
                  "  ref::Barrier_Hessian<false>(d, dHat, k, out[2]); }\n"
+                 "void ref_barrier_elastic(double d, double dHat, double kappa, double* out) {\n"
+                 "  double k[3] = {kappa, 0, 0};\n"
+                 "  ref::Barrier<true>(d, dHat, k, out[0]);\n"
+                 "  ref::Barrier_Gradient<true>(d, dHat, k, out[1]);\n"
+                 "  ref::Barrier_Hessian<true>(d, dHat, k, out[2]); }\n"
                  "void ref_g_MS(double k, double l, const double* x, double* g) { ref::g_MS<double>(k, l, %s, g); }\n"
                  "void ref_H_MS(double k, double l, const double* x, double* H) { ref::H_MS<double>(k, l, %s, H); }\n"
                  "void ref_g_RB(const double* x, double* g) { ref::g_RB<double>(%s, g); }\n"

@@ -14,8 +14,8 @@ Inputs: 48 random vertex sets per kind (standard normal coordinates) plus the
 fixed vertex set of the reference's derivTest_EECross / derivTest_e
 (EDGE_EDGE_MOLLIFIER.h:384-438), barrier arguments spanning 1e-12..1, and
 strain-limit triples (s, limit, threshold) on both sides of 1, squared slips
-on both sides of the friction mollifier's switch, 48 random hinge stencils and
-32 edge pairs inside the mollifier's range.
+on both sides of the friction mollifier's switch, 48 random hinge stencils,
+32 edge pairs inside the mollifier's range and elastic-IPC barrier arguments.
 Run:  python tests/golden/make_golden.py
 """
 import ctypes
@@ -166,6 +166,17 @@ def main():
         GM[i] = o[1] * g
         HM[i] = o[1] * h.reshape(12, 12) + o[2] * np.outer(g, g)
     out.update(x_EEM=XM, eps_EEM=EPS, e_EEM=EM, g_EEM=GM, H_EEM=HM)
+    # the elastic-IPC branch of the barrier (Barrier<true> and its derivatives)
+    L.ref_barrier_elastic.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, P]
+    rb = np.random.default_rng(20240605)
+    rows = []
+    for d in 10.0 ** rb.uniform(-12, 0, 48):
+        dhat = d * rb.uniform(1.01, 100.0)
+        kappa = 10.0 ** rb.uniform(-2, 11)
+        o = np.zeros(3)
+        L.ref_barrier_elastic(d, dhat, kappa, o.ctypes.data)
+        rows.append([d, dhat, kappa, o[0], o[1], o[2]])
+    out["barrier_elastic"] = np.array(rows)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_derivs.npz")
     np.savez_compressed(dst, **out)
     print("wrote", dst, os.path.getsize(dst), "bytes")

@@ -35,6 +35,17 @@ def test_barrier_matches_reference(orc):
             assert abs(mine - ref) <= 1e-12 * max(abs(ref), 1e-300)
 
 
+def test_elastic_barrier_is_offset_form_with_scaled_kappa(orc):
+    # the reference's elastic-IPC barrier -kappa (s/shat - 1)^2 ln(s/shat) and its
+    # derivatives equal the offset-IPC barrier with kappa / shat^2, the identity
+    # the elastic-IPC path here is built on
+    z = np.load(GOLD)
+    for d, dhat, kappa, b, g, h in z["barrier_elastic"]:
+        out = orc.barrier(d, dhat, kappa / (dhat * dhat))
+        for mine, ref in zip(out, (b, g, h)):
+            assert abs(mine - ref) <= 1e-12 * max(abs(ref), 1e-300), (d, dhat, mine, ref)
+
+
 def test_strain_barrier_matches_reference(orc):
     # the strain-limiting barrier of one singular value against the reference's
     # f/g/h_sl_u (upper limit) and f/g/h_sl_l (lower limit) of INEXT.h, C2 form
