@@ -104,11 +104,67 @@ def _stream_ptr(stream):
     return int(getattr(stream, "cuda_stream", stream))
 
 
+_NP_DTYPES = {"u8": np.uint8, "i32": np.int32, "f32": np.float32, "f64": np.float64}
+
+
+def _dtype_name(a):
+    if isinstance(a, np.ndarray):
+        for k, v in _NP_DTYPES.items():
+            if a.dtype == v:
+                return k
+        return str(a.dtype)
+    s = str(a.dtype)  # torch dtypes
+    return {"torch.uint8": "u8", "torch.int32": "i32", "torch.float32": "f32", "torch.float64": "f64"}.get(s, s)
+
+
+def _where(a):
+    """'host' for numpy arrays and CPU tensors, ('cuda', index) for CUDA tensors."""
+    if isinstance(a, np.ndarray):
+        return "host"
+    if getattr(a, "is_cuda", False):
+        return ("cuda", a.device.index)
+    return "host"
+
+
+def _check_buffers(name, bufs, mem):
+    """Checks dtype, shape and placement of the buffers handed to a pair entry
+    point, so that a wrong buffer is an exception here instead of an
+    out-of-bounds or host-pointer access in a kernel.  bufs: list of
+    (label, array, dtype name, expected shape)."""
+    places = set()
+    for label, a, dt, shape in bufs:
+        if a is None:
+            raise ValueError("%s: %s is missing" % (name, label))
+        if _dtype_name(a) != dt:
+            raise TypeError("%s: %s must be %s, got %s" % (name, label, dt, _dtype_name(a)))
+        if tuple(a.shape) != tuple(shape):
+            raise ValueError("%s: %s must have shape %s, got %s" % (name, label, tuple(shape), tuple(a.shape)))
+        if isinstance(a, np.ndarray):
+            if not a.flags["C_CONTIGUOUS"]:
+                raise ValueError("%s: %s must be C-contiguous" % (name, label))
+        elif not a.is_contiguous():
+            raise ValueError("%s: %s must be contiguous" % (name, label))
+        places.add(_where(a))
+    if mem == MEM_DEVICE:
+        if len(places) != 1 or "host" in places:
+            raise ValueError("%s: device-memory call needs every buffer on one CUDA device, got %s"
+                             % (name, sorted(map(str, places))))
+    elif any(p != "host" for p in places):
+        raise ValueError("%s: host-memory call needs host buffers (numpy or CPU tensors)" % name)
+
+
+def _pair_buffers(type_, idx, x, dx, toc_out, hit):
+    n = int(type_.shape[0])
+    nv = int(x.shape[0])
+    return n, nv, [("type", type_, "u8", (n,)), ("idx", idx, "i32", (n, 4)), ("x", x, "f64", (nv, 3)),
+                   ("dx", dx, "f64", (nv, 3)), ("toc_out", toc_out, "f64", (n,)), ("hit", hit, "u8", (n,))]
+
+
 def ccd_pairs(type_, idx, x, dx, toc_out, hit, eta=0.1, thickness=0.0, toc_in=1.0, precision=FP64,
               mem=MEM_HOST, stream=None, allow=(CIPC_ERR_ITER_CAP,)):
     """Additive CCD over pairs (see cipc_ccd_pairs).  Returns (status, n_overflow)."""
-    n = int(type_.shape[0])
-    nv = int(x.shape[0])
+    n, nv, bufs = _pair_buffers(type_, idx, x, dx, toc_out, hit)
+    _check_buffers("ccd_pairs", bufs, mem)
     ov = _c_i64(0)
     st = lib().cipc_ccd_pairs(n, _ptr(type_), _ptr(idx), nv, _ptr(x), _ptr(dx), eta, thickness, toc_in,
                               precision, mem, _ptr(toc_out), _ptr(hit), ctypes.byref(ov), _stream_ptr(stream))
@@ -119,8 +175,8 @@ def ccd_pairs(type_, idx, x, dx, toc_out, hit, eta=0.1, thickness=0.0, toc_in=1.
 def ccd_pairs_async(type_, idx, x, dx, toc_out, hit, eta=0.1, thickness=0.0, toc_in=1.0, precision=FP64,
                     stream=None):
     """Device-memory CCD that only enqueues (no overflow readback, no wait)."""
-    n = int(type_.shape[0])
-    nv = int(x.shape[0])
+    n, nv, bufs = _pair_buffers(type_, idx, x, dx, toc_out, hit)
+    _check_buffers("ccd_pairs_async", bufs, MEM_DEVICE)
     st = lib().cipc_ccd_pairs(n, _ptr(type_), _ptr(idx), nv, _ptr(x), _ptr(dx), eta, thickness, toc_in,
                               precision, MEM_DEVICE, _ptr(toc_out), _ptr(hit), None, _stream_ptr(stream))
     return _check(st)
@@ -133,8 +189,8 @@ def ccd_pairs_noalloc(type_, idx, x, dx, toc_out, hit, eta=0.1, thickness=0.0, t
                       slot=0, stream=None, counts=True, allow=(CIPC_ERR_ITER_CAP,)):
     """Device-memory CCD that allocates nothing (see cipc_ccd_pairs_noalloc).
     Returns (status, n_overflow); with counts=False it only enqueues."""
-    n = int(type_.shape[0])
-    nv = int(x.shape[0])
+    n, nv, bufs = _pair_buffers(type_, idx, x, dx, toc_out, hit)
+    _check_buffers("ccd_pairs_noalloc", bufs, MEM_DEVICE)
     ov = _c_i64(0)
     st = lib().cipc_ccd_pairs_noalloc(n, _ptr(type_), _ptr(idx), nv, _ptr(x), _ptr(dx), eta, thickness, toc_in,
                                       precision, slot, _ptr(toc_out), _ptr(hit),
@@ -143,11 +199,20 @@ def ccd_pairs_noalloc(type_, idx, x, dx, toc_out, hit, eta=0.1, thickness=0.0, t
     return st, ov.value
 
 
+def _barrier_check(name, type_, idx, x, x_rest, energy, grad, hess, precision, mem):
+    n = int(type_.shape[0])
+    nv = int(x.shape[0])
+    _check_buffers(name, [("type", type_, "u8", (n,)), ("idx", idx, "i32", (n, 4)), ("x", x, "f64", (nv, 3)),
+                          ("x_rest", x_rest, "f64", (nv, 3)), ("energy", energy, "f64", (n,)),
+                          ("grad", grad, "f64", (n, 12)),
+                          ("hess", hess, "f64" if precision == FP64 else "f32", (n, 78))], mem)
+    return n, nv
+
+
 def barrier_pairs(type_, idx, x, x_rest, energy, grad, hess, dhat2, xi, kappa, project_pd=True,
                   precision=FP64, mem=MEM_HOST, stream=None, allow=(CIPC_ERR_NONPOSITIVE_DISTANCE,)):
     """Barrier energy/gradient/PSD Hessian per pair (see cipc_barrier_pairs).  Returns (status, n_bad)."""
-    n = int(type_.shape[0])
-    nv = int(x.shape[0])
+    n, nv = _barrier_check("barrier_pairs", type_, idx, x, x_rest, energy, grad, hess, precision, mem)
     bad = _c_i64(0)
     st = lib().cipc_barrier_pairs(n, _ptr(type_), _ptr(idx), nv, _ptr(x), _ptr(x_rest), dhat2, xi, kappa,
                                   1 if project_pd else 0, precision, mem, _ptr(energy), _ptr(grad), _ptr(hess),
@@ -158,8 +223,7 @@ def barrier_pairs(type_, idx, x, x_rest, energy, grad, hess, dhat2, xi, kappa, p
 
 def barrier_pairs_async(type_, idx, x, x_rest, energy, grad, hess, dhat2, xi, kappa, project_pd=True,
                         precision=FP64, stream=None):
-    n = int(type_.shape[0])
-    nv = int(x.shape[0])
+    n, nv = _barrier_check("barrier_pairs_async", type_, idx, x, x_rest, energy, grad, hess, precision, MEM_DEVICE)
     st = lib().cipc_barrier_pairs(n, _ptr(type_), _ptr(idx), nv, _ptr(x), _ptr(x_rest), dhat2, xi, kappa,
                                   1 if project_pd else 0, precision, MEM_DEVICE, _ptr(energy), _ptr(grad),
                                   _ptr(hess), None, _stream_ptr(stream))

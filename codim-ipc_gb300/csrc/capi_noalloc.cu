@@ -1,8 +1,9 @@
 // cipc_ccd_pairs_noalloc (include/cipc.h): the device-memory CCD over pairs
 // with its kernel counters taken from a scratch array compiled into the library.
 // Nothing on this path allocates: no cudaMalloc / cudaMallocAsync / cudaFree,
-// no allocating library call; the only CUDA calls are cudaGetDevice,
-// cudaGetSymbolAddress (once per device), cudaMemsetAsync, the kernel launch
+// no allocating library call; the only CUDA calls are cudaGetDevice, the
+// context-id lookup, cudaGetSymbolAddress (once per device context),
+// cudaMemsetAsync, the kernel launch
 // and, when counts are asked for, one device-to-host copy of 24 bytes.
 #include <cuda_runtime.h>
 
@@ -30,6 +31,40 @@ static __device__ __align__(256) unsigned long long g_ccd_scratch[kSlots * kSlot
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 unsigned long long* g_addr[kMaxDevices] = {};
+unsigned long long g_ctx[kMaxDevices] = {};  // id of the context the address belongs to
+
+// The address of g_ccd_scratch belongs to the device's current context.  After a
+// cudaDeviceReset (or any new primary context) the old address is unmapped, so
+// the cache is keyed on the driver's unique context id (cuCtxGetId, looked up
+// through the runtime so that the library keeps no link-time libcuda
+// dependency); without that entry point the id stays 0 and the address is
+// looked up once per device.
+typedef int (*PfnCtxGetCurrent)(void**);
+typedef int (*PfnCtxGetId)(void*, unsigned long long*);
+
+unsigned long long current_context_id()
+{
+    static PfnCtxGetCurrent get_cur = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        looked_up = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = reinterpret_cast<PfnCtxGetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<PfnCtxGetId>(f);
+    }
+    if (!get_cur || !get_id) return 0;
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_cur(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
 
 int scratch_slot(int slot, unsigned long long** out)
 {
@@ -39,11 +74,13 @@ int scratch_slot(int slot, unsigned long long** out)
     if (dev < 0 || dev >= kMaxDevices)
         return set_error(CIPC_ERR_INVALID_ARG, "cipc_ccd_pairs_noalloc: device %d beyond %d", dev, kMaxDevices);
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_addr[dev] || g_ctx[dev] != ctx) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_ccd_scratch);
         if (e != cudaSuccess) return set_cuda_error(e, "cipc_ccd_pairs_noalloc: cudaGetSymbolAddress");
         g_addr[dev] = static_cast<unsigned long long*>(p);
+        g_ctx[dev] = ctx;
     }
     *out = g_addr[dev] + (size_t)slot * kSlotWords;
     return CIPC_OK;

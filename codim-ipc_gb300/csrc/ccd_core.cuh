@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(256) k_accd(CcdArgs a)
             t = 0;
             phase = 1;
         } else {
-            if (t != 0 && (f / (dist + th) < gap)) {
+            if (t != 0 && Pol::gap_less(f, dist + th, gap)) {
                 a.toc_out[pid] = t;
                 a.hit[pid] = 1;
                 if (a.toc_min) atomicMin(a.toc_min, (unsigned long long)__double_as_longlong(t));

@@ -355,12 +355,16 @@ int sim_step(Sim* s, StepStats* st)
         // barrier stiffness update (IMPLICIT_EULER.h:566-595; offset IPC only)
         if (s->npcon > 0 && !P.elastic) {
             unsigned long long* flag = s->cnt.p + 32;
-            cudaMemsetAsync(flag, 0, sizeof(unsigned long long), str);
+            cudaError_t ce = cudaMemsetAsync(flag, 0, sizeof(unsigned long long), str);
+            if (ce != cudaSuccess) return set_cuda_error(ce, "kappa update: clearing the flag");
             k_kappa_flag<<<nblk(s->npcon, 256), 256, 0, str>>>(s->npcon, s->pkind.p, s->pverts.p, s->pd2.p, s->x.p,
                                                                P.xi * P.xi, flag);
+            if ((ce = cudaGetLastError()) != cudaSuccess) return set_cuda_error(ce, "kappa update: k_kappa_flag");
             unsigned long long hf = 0;
-            cudaMemcpyAsync(&hf, flag, sizeof(hf), cudaMemcpyDeviceToHost, str);
-            cudaStreamSynchronize(str);
+            if ((ce = cudaMemcpyAsync(&hf, flag, sizeof(hf), cudaMemcpyDeviceToHost, str)) != cudaSuccess)
+                return set_cuda_error(ce, "kappa update: reading the flag");
+            if ((ce = cudaStreamSynchronize(str)) != cudaSuccess)
+                return set_cuda_error(ce, "kappa update: synchronize");
             if (hf && s->kappa < s->kappa_max) {
                 s->kappa *= 2;
                 if ((rc = eval_energy(s, s->x.p, &Eprev, &ok))) return rc;

@@ -36,10 +36,19 @@ extern "C" {
 #define CIPC_ERR_NO_DEVICE 7
 #define CIPC_ERR_INDEX_RANGE 8
 
-#define CIPC_PRECISION_FP64 0  /* all-FP64, decisions bit-exact with the CPU restatement */
-#define CIPC_PRECISION_MIXED 1 /* FP32 classification and Hessians; barrier distances FP64; CCD   \
-                                  distances and times in float-float (FP32 pairs, ~47 bits) from \
-                                  FP64 vertex differences */
+/* CIPC_PRECISION_FP64: every value that reaches a result is FP64; decisions and
+ * results are bit-identical to the CPU restatement.  Distance-type decisions are
+ * taken by a certified FP32 evaluation when it is certain (it returns the FP64
+ * decision or defers to FP64), which does not change any result.
+ * CIPC_PRECISION_MIXED: for the pair CCD, distances and times in float-float (FP32
+ * pairs, ~47 bits) from FP64 vertex differences -- NOT bit-exact and NOT
+ * guaranteed conservative: on seeded benchmark pairs ~1e-5 of the hit/miss
+ * decisions differ from FP64, in both directions, and a shared hit's time can be
+ * later than FP64's.  For the barrier pairs and the time step: FP32 Hessians and
+ * PCG (inside FP64 iterative refinement); distances, constraint sets, CCD step
+ * sizes, energies and gradients stay FP64. */
+#define CIPC_PRECISION_FP64 0
+#define CIPC_PRECISION_MIXED 1
 #define CIPC_BARRIER_OFFSET 0  /* offset IPC (C-IPC): barrier on d^2 - xi^2 */
 #define CIPC_BARRIER_ELASTIC 1 /* elastic IPC: no offset, barrier normalised by dhat */
 
@@ -97,7 +106,8 @@ int cipc_ccd_pairs(int64_t n_pairs, const uint8_t* type, const int32_t* idx, int
  * (the counters must start at zero).  Two calls that overlap in time on the same
  * device and the same slot race on its counters and give wrong results: give
  * each stream that may run concurrently its own slot, or order the calls.
- * The first call on each device looks up the slot's device address
+ * The first call on each device, and the first call after the device's context
+ * was replaced (cudaDeviceReset), looks up the scratch array's device address
  * (cudaGetSymbolAddress, which may load the library's kernels on that device);
  * make that first call outside any stream capture.  With n_overflow == NULL the
  * call only enqueues work on `stream` and reports no kernel-side counts.

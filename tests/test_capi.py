@@ -4,6 +4,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -151,16 +152,51 @@ def test_noalloc_argument_validation_without_gpu():
     x = np.zeros((2, 3))
     toc = np.zeros(1)
     hit = np.zeros(1, np.uint8)
+    L = cipc_ffi.lib()
+
+    def raw(n, eta=0.1, precision=0, slot=0):
+        # straight through the C ABI: the binding itself refuses host buffers for a device call
+        return L.cipc_ccd_pairs_noalloc(n, t.ctypes.data, idx.ctypes.data, 2, x.ctypes.data, x.ctypes.data, eta,
+                                        0.0, 1.0, precision, slot, toc.ctypes.data, hit.ctypes.data, None, None)
+
     for kw in (dict(slot=-1), dict(slot=cipc_ffi.NOALLOC_SLOTS), dict(eta=0.0), dict(precision=7)):
-        try:
-            cipc_ffi.ccd_pairs_noalloc(t, idx, x, x, toc, hit, **kw)
-            raise AssertionError("expected an error for %r" % (kw,))
-        except cipc_ffi.CipcError as e:
-            assert e.status == cipc_ffi.CIPC_ERR_INVALID_ARG, kw
-    e0 = np.zeros(0, np.uint8)
-    st, ov = cipc_ffi.ccd_pairs_noalloc(e0, np.zeros((0, 4), np.int32), x, x, np.zeros(0), np.zeros(0, np.uint8),
-                                        slot=cipc_ffi.NOALLOC_SLOTS - 1)
-    assert st == cipc_ffi.CIPC_OK and ov == 0
+        assert raw(1, **kw) == cipc_ffi.CIPC_ERR_INVALID_ARG, kw
+    assert raw(0, slot=cipc_ffi.NOALLOC_SLOTS - 1) == cipc_ffi.CIPC_OK
+
+
+def test_binding_checks_pair_buffers():
+    """The Python binding rejects buffers of the wrong dtype, shape or placement
+    before they reach a kernel (a float32 vertex array or an (n, 2) index array
+    would otherwise be read past its end on the device)."""
+    import cipc_ffi
+    n, nv = 3, 8
+    t = np.zeros(n, np.uint8)
+    idx = np.zeros((n, 4), np.int32)
+    x = np.zeros((nv, 3))
+    toc = np.zeros(n)
+    hit = np.zeros(n, np.uint8)
+    bad = [dict(x=x.astype(np.float32)), dict(idx=np.zeros((n, 2), np.int32)), dict(dx=np.zeros((nv - 1, 3))),
+           dict(toc_out=np.zeros(n, np.float32)), dict(hit=np.zeros(n + 1, np.uint8)),
+           dict(type_=np.zeros(n, np.int32)), dict(x=np.zeros((nv, 3))[:, :2].copy())]
+    for b in bad:
+        args = dict(type_=t, idx=idx, x=x, dx=x, toc_out=toc, hit=hit)
+        args.update(b)
+        with pytest.raises((TypeError, ValueError)):
+            cipc_ffi.ccd_pairs(**args)
+    # host arrays are refused by the device-memory entry points
+    for fn in (cipc_ffi.ccd_pairs_async, cipc_ffi.ccd_pairs_noalloc):
+        with pytest.raises(ValueError):
+            fn(t, idx, x, x, toc, hit)
+    with pytest.raises(ValueError):
+        cipc_ffi.ccd_pairs(t, idx, x, x, toc, hit, mem=cipc_ffi.MEM_DEVICE)
+    E = np.zeros(n)
+    g = np.zeros((n, 12))
+    with pytest.raises(TypeError):  # FP64 needs a double Hessian
+        cipc_ffi.barrier_pairs(t, idx, x, x, E, g, np.zeros((n, 78), np.float32), 1e-4, 1e-7, 1.0, True,
+                               cipc_ffi.FP64)
+    with pytest.raises(ValueError):
+        cipc_ffi.barrier_pairs(t, idx, x, x, E, np.zeros((n, 9)), np.zeros((n, 78), np.float32), 1e-4, 1e-7, 1.0,
+                               True, cipc_ffi.MIXED)
 
 
 def test_fails_loudly_without_gpu_or_library():

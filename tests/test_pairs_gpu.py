@@ -1,7 +1,8 @@
 """GPU contact-pair kernels against the CPU oracle, through the C ABI.
 
 Bars (stated per test):
-  * CCD, FP64 variant: hit/miss decisions and times of impact bit-identical.
+  * CCD, FP64 variant: hit/miss decisions and times of impact bit-identical,
+    also over the full 10M-pair benchmark workload.
   * CCD, mixed variant: decisions may differ only for pairs within FP32 rounding
     of a region boundary (<= 1e-4 of pairs); times agree to 1e-5 relative at the
     99.9th percentile, the rest within one conservative step, also for a scene
@@ -214,6 +215,40 @@ def test_barrier_nonpositive_reported(cuda, orc):
     H = np.zeros((n, 78))
     st, bad = F.barrier_pairs(w["type"], w["idx"], w["x"], w["x"], E, g, H, 1e-4, 1e-5, 1.0, True, F.FP64)
     assert st == F.CIPC_ERR_NONPOSITIVE_DISTANCE and bad == bad_o
+
+
+def test_ccd_fp64_bit_exact_benchmark_workload(cuda, orc):
+    """The timed path of the contact-kernel benchmark at its full size: 10M seeded
+    pairs (40/40/10/10, separations 1e-6..1e-2), device-memory FP64 kernel (with
+    its certified FP32 type decisions), against the CPU oracle: hit/miss and the
+    bits of every time of impact identical."""
+    import torch
+    w = workloads.contact_pairs(10_000_000, seed=0)
+    toc_o, hit_o, _, ov_o = orc.ccd_pairs(w["type"], w["idx"], w["x"], w["dx"], ETA, TH, 1.0)
+    dev = {k: torch.from_numpy(np.ascontiguousarray(w[k])).to(cuda) for k in ("type", "idx", "x", "dx")}
+    n = w["type"].shape[0]
+    toc = torch.empty(n, dtype=torch.float64, device=cuda)
+    hit = torch.empty(n, dtype=torch.uint8, device=cuda)
+    st, ov = F.ccd_pairs(dev["type"], dev["idx"], dev["x"], dev["dx"], toc, hit, eta=ETA, thickness=TH,
+                         precision=F.FP64, mem=F.MEM_DEVICE)
+    assert st == 0 and ov == 0 and ov_o == 0
+    assert np.array_equal(hit.cpu().numpy(), hit_o)
+    assert np.array_equal(toc.cpu().numpy().view(np.uint64), toc_o.view(np.uint64))
+
+
+def test_ccd_mixed_direction_of_differences(cuda, orc):
+    """The mixed kernel is neither bit-exact nor guaranteed conservative (the
+    header says so); its differences from FP64 are counted by direction on 1M
+    pairs and stay rare: unsafe misses (mixed no-hit where FP64 hits) below 2e-5
+    of the pairs, times later than FP64's by more than 1e-5 relative below 1e-4."""
+    w = workloads.contact_pairs(1_000_000, seed=13)
+    toc_o, hit_o, _, _ = orc.ccd_pairs(w["type"], w["idx"], w["x"], w["dx"], ETA, TH, 1.0)
+    toc_g, hit_g, st, ov = _gpu_ccd(w, F.MIXED)
+    n = hit_o.size
+    unsafe = int(((hit_g == 0) & (hit_o == 1)).sum())
+    both = (hit_g == 1) & (hit_o == 1)
+    late = int((toc_g[both] > toc_o[both] * (1 + 1e-5)).sum())
+    assert unsafe <= 2e-5 * n and late <= 1e-4 * n, (unsafe, late)
 
 
 def test_full_size_properties(cuda):

@@ -90,3 +90,49 @@ def test_noalloc_counters_reset_between_calls(cuda):
     F.ccd_pairs_noalloc(d["type"], d["idx"], d["x"], d["dx"], toc, hit, slot=F.NOALLOC_SLOTS - 1, counts=False)
     torch.cuda.synchronize()
     assert torch.equal(toc, toc_r) and torch.equal(hit, hit_r)
+
+
+def _default_pool_stats(device_index):
+    """(used, reserved, used high-water mark) of the device's default stream-ordered
+    memory pool, read through the driver API (the pool every cudaMallocAsync on
+    that device draws from unless the caller set another)."""
+    import ctypes
+    cu = ctypes.CDLL("libcuda.so.1")
+    dev = ctypes.c_int()
+    assert cu.cuDeviceGet(ctypes.byref(dev), device_index) == 0
+    pool = ctypes.c_void_p()
+    assert cu.cuDeviceGetDefaultMemPool(ctypes.byref(pool), dev) == 0
+    out = []
+    for attr in (7, 5, 8):  # CU_MEMPOOL_ATTR_USED_MEM_CURRENT, _RESERVED_MEM_CURRENT, _USED_MEM_HIGH
+        v = ctypes.c_uint64()
+        assert cu.cuMemPoolGetAttribute(pool, attr, ctypes.byref(v)) == 0
+        out.append(v.value)
+    return out, cu, pool
+
+
+@pytest.mark.gpu
+def test_noalloc_calls_leave_device_memory_untouched(cuda):
+    """At run time, not only in the source: after a first call (which may load
+    the kernels), repeated calls change neither torch's allocated memory nor the
+    default pool's used and reserved bytes, and the pool's high-water mark (reset
+    before the calls) does not rise."""
+    import ctypes
+
+    import torch
+    n = 100_000
+    d = _device_pairs(cuda, n, seed=21)
+    toc, hit = _outputs(cuda, n)
+    F.ccd_pairs_noalloc(d["type"], d["idx"], d["x"], d["dx"], toc, hit, slot=1)
+    torch.cuda.synchronize()
+    (used0, res0, _), cu, pool = _default_pool_stats(cuda.index or 0)
+    zero = ctypes.c_uint64(0)
+    assert cu.cuMemPoolSetAttribute(pool, 8, ctypes.byref(zero)) == 0  # reset the high-water mark
+    alloc0 = torch.cuda.memory_allocated(cuda)
+    for _ in range(3):
+        F.ccd_pairs_noalloc(d["type"], d["idx"], d["x"], d["dx"], toc, hit, slot=1)
+        F.ccd_pairs_noalloc(d["type"], d["idx"], d["x"], d["dx"], toc, hit, slot=2, counts=False)
+    torch.cuda.synchronize()
+    (used1, res1, high1), _, _ = _default_pool_stats(cuda.index or 0)
+    assert torch.cuda.memory_allocated(cuda) == alloc0
+    assert used1 == used0 and res1 == res0
+    assert high1 <= used0
