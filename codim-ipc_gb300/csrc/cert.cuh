@@ -396,6 +396,31 @@ CIPC_HD int gap_less_cert(double f, double den, double gap)
 // differences already formed for the classification (RN(t0 - p) = -RN(p - t0)
 // and RN(eb0 - ea0) = -RN(ea0 - eb0) exactly).
 // ---------------------------------------------------------------------------
+// type with the FP64 classifier as the fallback (inputs as the FP64 code forms them)
+CIPC_HD int pt_type_fast(d3 p, d3 t0, d3 t1, d3 t2, d3 w, d3 e1, d3 e2)
+{
+    const int ty = pt_type_cert(w, e1, e2);
+    return ty >= 0 ? ty : pt_type(p, t0, t1, t2);
+}
+CIPC_HD int ee_type_fast(d3 ea0, d3 ea1, d3 eb0, d3 eb1, d3 u, d3 v, d3 w)
+{
+    const int ty = ee_type_cert(u, v, w);
+    return ty >= 0 ? ty : ee_type(ea0, ea1, eb0, eb1);
+}
+// pt_d2 / ee_d2 of geom.cuh from the differences already formed
+CIPC_HD double pt_d2_w(d3 w, d3 e1, d3 e2)
+{
+    const d3 b = cross(e1, e2);
+    const double aTb = dot(w, b);
+    return G_DIV(G_MUL(aTb, aTb), n2(b));
+}
+CIPC_HD double ee_d2_w(d3 u, d3 v, d3 w)
+{
+    const d3 b = cross(u, v);
+    const double aTb = dot(mk(-w.x, -w.y, -w.z), b);
+    return G_DIV(G_MUL(aTb, aTb), n2(b));
+}
+
 CIPC_HD double pt_d2_cert(d3 p, d3 t0, d3 t1, d3 t2)
 {
     const d3 e1 = t1 - t0, e2 = t2 - t0, w = p - t0;
@@ -411,7 +436,7 @@ CIPC_HD double pt_d2_cert(d3 p, d3 t0, d3 t1, d3 t2)
         default: {
             const d3 b = cross(e1, e2);
             const double aTb = dot(w, b);
-            return aTb * aTb / n2(b);
+            return G_DIV(G_MUL(aTb, aTb), n2(b));
         }
     }
 }
@@ -433,7 +458,7 @@ CIPC_HD double ee_d2_cert(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
         default: {
             const d3 b = cross(u, v);
             const double aTb = dot(mk(-w.x, -w.y, -w.z), b);
-            return aTb * aTb / n2(b);
+            return G_DIV(G_MUL(aTb, aTb), n2(b));
         }
     }
 }

@@ -4,9 +4,10 @@
 // Arithmetic rule (shared with the CPU checker so FP64 decisions agree bit for
 // bit): dot products are fma chains  dot(a,b) = fma(a.z,b.z, fma(a.y,b.y, a.x*b.x)),
 // cross products use one fma per component, position updates x + t*d are a single
-// fma, and everything else is evaluated left to right.  Translation units that
-// include this header for exact FP64 kernels are compiled with -fmad=false so the
-// compiler adds no contractions of its own.
+// fma, and everything else is evaluated left to right.  On the device every other
+// FP64 operation here is an explicit-rounding intrinsic (__dadd_rn, __dmul_rn,
+// __ddiv_rn, ...), which the compiler never contracts, so the rule holds in any
+// translation unit whatever its -fmad setting.
 #pragma once
 #include <cmath>
 #include <cstdint>
@@ -17,20 +18,32 @@
 
 namespace cipc {
 
+#ifdef __CUDA_ARCH__
+#define G_ADD(a, b) __dadd_rn((a), (b))
+#define G_SUB(a, b) __dsub_rn((a), (b))
+#define G_MUL(a, b) __dmul_rn((a), (b))
+#define G_DIV(a, b) __ddiv_rn((a), (b))
+#else
+#define G_ADD(a, b) ((a) + (b))
+#define G_SUB(a, b) ((a) - (b))
+#define G_MUL(a, b) ((a) * (b))
+#define G_DIV(a, b) ((a) / (b))
+#endif
+
 struct d3 {
     double x, y, z;
 };
 
 CIPC_HD d3 mk(double a, double b, double c) { return d3{a, b, c}; }
-CIPC_HD d3 operator-(d3 a, d3 b) { return d3{a.x - b.x, a.y - b.y, a.z - b.z}; }
-CIPC_HD d3 operator+(d3 a, d3 b) { return d3{a.x + b.x, a.y + b.y, a.z + b.z}; }
-CIPC_HD d3 scl(d3 a, double s) { return d3{a.x * s, a.y * s, a.z * s}; }
-CIPC_HD d3 dvs(d3 a, double s) { return d3{a.x / s, a.y / s, a.z / s}; }
-CIPC_HD double dot(d3 a, d3 b) { return fma(a.z, b.z, fma(a.y, b.y, a.x * b.x)); }
+CIPC_HD d3 operator-(d3 a, d3 b) { return d3{G_SUB(a.x, b.x), G_SUB(a.y, b.y), G_SUB(a.z, b.z)}; }
+CIPC_HD d3 operator+(d3 a, d3 b) { return d3{G_ADD(a.x, b.x), G_ADD(a.y, b.y), G_ADD(a.z, b.z)}; }
+CIPC_HD d3 scl(d3 a, double s) { return d3{G_MUL(a.x, s), G_MUL(a.y, s), G_MUL(a.z, s)}; }
+CIPC_HD d3 dvs(d3 a, double s) { return d3{G_DIV(a.x, s), G_DIV(a.y, s), G_DIV(a.z, s)}; }
+CIPC_HD double dot(d3 a, d3 b) { return fma(a.z, b.z, fma(a.y, b.y, G_MUL(a.x, b.x))); }
 CIPC_HD double n2(d3 a) { return dot(a, a); }
 CIPC_HD d3 cross(d3 a, d3 b)
 {
-    return d3{fma(a.y, b.z, -(a.z * b.y)), fma(a.z, b.x, -(a.x * b.z)), fma(a.x, b.y, -(a.y * b.x))};
+    return d3{fma(a.y, b.z, -G_MUL(a.z, b.y)), fma(a.z, b.x, -G_MUL(a.x, b.z)), fma(a.x, b.y, -G_MUL(a.y, b.x))};
 }
 CIPC_HD d3 axpy(double t, d3 d, d3 x)
 {
@@ -64,12 +77,12 @@ CIPC_HD void ldlt2(double a00, double a10, double a11, double b0, double b1,
         y1 = 0.0;
         return;
     }
-    const double l10 = a10 / d0;
-    const double d1 = fma(-l10, d0 * l10, m11);
+    const double l10 = G_DIV(a10, d0);
+    const double d1 = fma(-l10, G_MUL(d0, l10), m11);
     double z0 = b0;
     double z1 = fma(-l10, z0, b1);
-    z0 = (fabs(d0) > 2.2250738585072014e-308) ? z0 / d0 : 0.0;
-    z1 = (fabs(d1) > 2.2250738585072014e-308) ? z1 / d1 : 0.0;
+    z0 = (fabs(d0) > 2.2250738585072014e-308) ? G_DIV(z0, d0) : 0.0;
+    z1 = (fabs(d1) > 2.2250738585072014e-308) ? G_DIV(z1, d1) : 0.0;
     z0 = fma(-l10, z1, z0);
     if (sw) {
         y0 = z1;
@@ -109,29 +122,29 @@ CIPC_HD int ee_type(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
 {
     const d3 u = ea1 - ea0, v = eb1 - eb0, w = ea0 - eb0;
     const double a = dot(u, u), b = dot(u, v), c = dot(v, v), d = dot(u, w), e = dot(v, w);
-    const double D = fma(a, c, -(b * b));
+    const double D = fma(a, c, -G_MUL(b, b));
     double tD = D, tN;
     int dc = 8;
-    const double sN = fma(b, e, -(c * d));
+    const double sN = fma(b, e, -G_MUL(c, d));
     if (sN <= 0.0) {
         tN = e;
         tD = c;
         dc = 2;
     } else if (sN >= D) {
-        tN = e + b;
+        tN = G_ADD(e, b);
         tD = c;
         dc = 5;
     } else {
-        tN = fma(a, e, -(b * d));
+        tN = fma(a, e, -G_MUL(b, d));
         if (tN > 0.0 && tN < tD) {
             const d3 uxv = cross(u, v);
-            if (dot(uxv, w) == 0.0 || n2(uxv) < 1.0e-20 * a * c) {
-                if (sN < D / 2) {
+            if (dot(uxv, w) == 0.0 || n2(uxv) < G_MUL(G_MUL(1.0e-20, a), c)) {
+                if (sN < G_DIV(D, 2.0)) {
                     tN = e;
                     tD = c;
                     dc = 2;
                 } else {
-                    tN = e + b;
+                    tN = G_ADD(e, b);
                     tD = c;
                     dc = 5;
                 }
@@ -143,34 +156,34 @@ CIPC_HD int ee_type(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
         if (-d >= a) return 3;
         return 6;
     } else if (tN >= tD) {
-        if ((-d + b) <= 0.0) return 1;
-        if ((-d + b) >= a) return 4;
+        if (G_ADD(-d, b) <= 0.0) return 1;
+        if (G_ADD(-d, b) >= a) return 4;
         return 7;
     }
     return dc;
 }
 
 CIPC_HD double pp_d2(d3 a, d3 b) { return n2(a - b); }
-CIPC_HD double pe_d2(d3 p, d3 e0, d3 e1) { return n2(cross(e0 - p, e1 - p)) / n2(e1 - e0); }
+CIPC_HD double pe_d2(d3 p, d3 e0, d3 e1) { return G_DIV(n2(cross(e0 - p, e1 - p)), n2(e1 - e0)); }
 
 // DISTANCE_TYPE.h:11-27, point-edge: 0 point-e0, 1 point-e1, 2 interior
 CIPC_HD int pe_type(d3 p, d3 e0, d3 e1)
 {
     const d3 e = e1 - e0;
-    const double ratio = dot(e, p - e0) / n2(e);
+    const double ratio = G_DIV(dot(e, p - e0), n2(e));
     return ratio < 0 ? 0 : (ratio > 1 ? 1 : 2);
 }
 CIPC_HD double pt_d2(d3 p, d3 t0, d3 t1, d3 t2)
 {
     const d3 b = cross(t1 - t0, t2 - t0);
     const double aTb = dot(p - t0, b);
-    return aTb * aTb / n2(b);
+    return G_DIV(G_MUL(aTb, aTb), n2(b));
 }
 CIPC_HD double ee_d2(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
 {
     const d3 b = cross(ea1 - ea0, eb1 - eb0);
     const double aTb = dot(eb0 - ea0, b);
-    return aTb * aTb / n2(b);
+    return G_DIV(G_MUL(aTb, aTb), n2(b));
 }
 CIPC_HD double ee_cross_n2(d3 ea0, d3 ea1, d3 eb0, d3 eb1)
 {
@@ -213,7 +226,7 @@ CIPC_HD double pe_d2_any(d3 p, d3 e0, d3 e1)
     if (c1 <= 0.0) return pp_d2(p, e0);
     const double c2 = dot(v, v);
     if (c2 <= c1) return pp_d2(p, e1);
-    return pp_d2(p, axpy(c1 / c2, v, e0));
+    return pp_d2(p, axpy(G_DIV(c1, c2), v, e0));
 }
 
 // Pair types used throughout: PP=0, PE=1, PT=2, EE=3 (vertex counts 2,3,4,4).

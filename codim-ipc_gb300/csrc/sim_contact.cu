@@ -22,6 +22,7 @@
 
 #include "../../include/cipc.h"
 #include "ccd_core.cuh"
+#include "cert.cuh"
 #include "cipc_internal.h"
 #include "cipc_util.h"
 #include "constraint_eval.cuh"
@@ -427,14 +428,15 @@ __global__ void k_cs_pt(CsArgs a)
         const d3 t0 = ld(a.x, t0i), t1 = ld(a.x, t1i), t2 = ld(a.x, t2i);
         const d3 mx = vmax3(vmax3(t0, t1), t2), mn = vmin3(vmin3(t0, t1), t2);
         if (any_gt3(p - mx, a.dHat) || any_gt3(mn - p, a.dHat)) return;
-        switch (pt_type(p, t0, t1, t2)) {
-            case 0: if (pp_d2(p, t0) < a.dh2) emit_merge(a.S, kc_PP, vI, t0i, -1); break;
+        const d3 e1 = t1 - t0, e2 = t2 - t0, w = p - t0;
+        switch (pt_type_fast(p, t0, t1, t2, w, e1, e2)) {
+            case 0: if (n2(w) < a.dh2) emit_merge(a.S, kc_PP, vI, t0i, -1); break;
             case 1: if (pp_d2(p, t1) < a.dh2) emit_merge(a.S, kc_PP, vI, t1i, -1); break;
             case 2: if (pp_d2(p, t2) < a.dh2) emit_merge(a.S, kc_PP, vI, t2i, -1); break;
             case 3: if (pe_d2(p, t0, t1) < a.dh2) emit_merge(a.S, kc_PE, vI, t0i, t1i); break;
             case 4: if (pe_d2(p, t1, t2) < a.dh2) emit_merge(a.S, kc_PE, vI, t1i, t2i); break;
             case 5: if (pe_d2(p, t2, t0) < a.dh2) emit_merge(a.S, kc_PE, vI, t2i, t0i); break;
-            default: if (pt_d2(p, t0, t1, t2) < a.dh2) emit(a.S, kc_PT, vI, t0i, t1i, t2i); break;
+            default: if (pt_d2_w(w, e1, e2) < a.dh2) emit(a.S, kc_PT, vI, t0i, t1i, t2i); break;
         }
     });
 }
@@ -465,11 +467,12 @@ __global__ void k_cs_ee(CsArgs a)
         const d3 eb0 = ld(a.x, b0), eb1 = ld(a.x, b1);
         const d3 mnb = vmin3(eb0, eb1), mxb = vmax3(eb0, eb1);
         if (any_gt3(mna - mxb, a.dHat) || any_gt3(mnb - mxa, a.dHat)) return;
-        const double eps_x = 1.0e-3 * n2(ld(a.X0, a0) - ld(a.X0, a1)) * n2(ld(a.X0, b0) - ld(a.X0, b1));
-        const bool moll = ee_cross_n2(ea0, ea1, eb0, eb1) < eps_x;
-        switch (ee_type(ea0, ea1, eb0, eb1)) {
+        const double eps_x = G_MUL(G_MUL(1.0e-3, n2(ld(a.X0, a0) - ld(a.X0, a1))), n2(ld(a.X0, b0) - ld(a.X0, b1)));
+        const d3 u = ea1 - ea0, v = eb1 - eb0, w = ea0 - eb0;
+        const bool moll = n2(cross(u, v)) < eps_x;
+        switch (ee_type_fast(ea0, ea1, eb0, eb1, u, v, w)) {
             case 0:
-                if (pp_d2(ea0, eb0) < a.dh2) {
+                if (n2(w) < a.dh2) {
                     if (moll) emit(a.S, kc_PPM, a0, a1, b0, b1);
                     else emit_merge(a.S, kc_PP, a0, b0, -1);
                 }
@@ -517,7 +520,7 @@ __global__ void k_cs_ee(CsArgs a)
                 }
                 break;
             default:
-                if (ee_d2(ea0, ea1, eb0, eb1) < a.dh2) emit(a.S, moll ? kc_EEM : kc_EE, a0, a1, b0, b1);
+                if (ee_d2_w(u, v, w) < a.dh2) emit(a.S, moll ? kc_EEM : kc_EE, a0, a1, b0, b1);
                 break;
         }
     });
