@@ -9,8 +9,9 @@ Bars:
   * constraint sets at identical states: equal as sets (kind, vertices, multiplicity);
   * incremental potential and gradient at identical states: 1e-10 relative;
   * intersection-free step size along a direction: 1e-12 relative;
-  * positions after time steps solved to a tight Newton tolerance (1e-7) and a
-    tight PCG tolerance (1e-12): within 1e-8 of the bounding-box diagonal of the
+  * positions after time steps solved to a tight Newton tolerance (2e-8 on the
+    cloth-on-box steps, 1e-7 elsewhere) and a tight PCG tolerance (1e-12): within
+    1e-8 of the bounding-box diagonal of the
     oracle's direct-solve Newton (1e-7 on the augmented-Lagrangian Dirichlet path);
   * every step ends intersection free (minimum d^2 - xi^2 > 0).
 """
@@ -116,13 +117,16 @@ def test_steps_match_direct_solve(cuda, orc, nh):
     assert np.allclose(k2o, k2g, rtol=1e-12) and dhat2 == dhat2g
     xo = X.copy()
     vo = np.zeros_like(X)
-    prm = F.make_params(DT, dhat2, XI, newton_tol=1e-7, pcg_tol=1e-12, max_newton_iters=400)
+    # at a Newton tolerance of 1e-7 the oracle's own endpoint is determined only to
+    # ~1.6e-8 of the diagonal (its distance to the endpoint of a run to 5e-9);
+    # at 2e-8 it is within 1.4e-9, which leaves the 1e-8 bar to the GPU path
+    prm = F.make_params(DT, dhat2, XI, newton_tol=2e-8, pcg_tol=1e-12, max_newton_iters=400)
     diag = np.linalg.norm(X.max(0) - X.min(0))
     for step in range(4):
         # each step starts from the oracle's state
         s.set_state(xo, vo)
         s.set_kappa(k2o[0], k2o[1])
-        rc, sto = sh.step(xo, vo, k2o, dbc, X[dbc], DT, dhat2, XI, tol=1e-7, max_iter=400)
+        rc, sto = sh.step(xo, vo, k2o, dbc, X[dbc], DT, dhat2, XI, tol=2e-8, max_iter=400)
         assert rc == 0
         stg = s.step(prm)
         xg, vg = s.state()
