@@ -27,6 +27,27 @@ cudaError_t stage_in(T** dptr, const T* h, size_t count, cudaStream_t s)
     return cudaSuccess;
 }
 
+// Host memory the current device can address directly (page-locked by
+// cudaHostAlloc / cudaHostRegister, as torch's pin_memory does): returns its device
+// address, or null for pageable memory.  The whole range must be one mapping.
+const void* mapped_host(const void* p, size_t bytes)
+{
+    if (!p || bytes == 0) return nullptr;
+    cudaPointerAttributes a0, a1;
+    if (cudaPointerGetAttributes(&a0, p) != cudaSuccess || a0.type != cudaMemoryTypeHost || !a0.devicePointer) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    const char* last = static_cast<const char*>(p) + bytes - 1;
+    if (cudaPointerGetAttributes(&a1, last) != cudaSuccess || a1.type != cudaMemoryTypeHost || !a1.devicePointer ||
+        static_cast<const char*>(a1.devicePointer) - static_cast<const char*>(a0.devicePointer) !=
+            (ptrdiff_t)(bytes - 1)) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a0.devicePointer;
+}
+
 }  // namespace
 
 extern "C" int cipc_ccd_pairs(int64_t n, const uint8_t* type, const int32_t* idx, int64_t nv, const double* x,
@@ -54,6 +75,56 @@ extern "C" int cipc_ccd_pairs(int64_t n, const uint8_t* type, const int32_t* idx
     // most 64) on a copy stream while the kernel runs on the chunks already
     // there, and each chunk's results go back on a third stream as soon as its
     // kernel ends.  Device buffers, or one chunk: everything on the caller's stream.
+    // Host buffers that are page-locked: the kernel reads the pairs and vertices
+    // and writes the results in place, over the CPU-GPU link (NVLink-C2C on
+    // Grace-Blackwell), with no staging copies; the call returns when they are
+    // written.  Pageable host buffers take the staged path below.
+    if (host) {
+        const void *m_type = mapped_host(type, (size_t)n), *m_idx = mapped_host(idx, (size_t)n * 16),
+                   *m_x = mapped_host(x, (size_t)nv * 24), *m_dx = mapped_host(dx, (size_t)nv * 24),
+                   *m_toc = mapped_host(toc_out, (size_t)n * 8), *m_hit = mapped_host(hit, (size_t)n);
+        if (m_type && m_idx && m_x && m_dx && m_toc && m_hit) {
+            unsigned long long* cnt_d = nullptr;
+            unsigned long long cnt[3] = {0, 0, 0};
+            cudaError_t e2 = cudaMallocAsync((void**)&cnt_d, sizeof(cnt), s);
+            if (e2 == cudaSuccess) e2 = cudaMemsetAsync(cnt_d, 0, sizeof(cnt), s);
+            if (e2 == cudaSuccess) {
+                CcdArgs a;
+                a.n = n;
+                a.type = static_cast<const uint8_t*>(m_type);
+                a.idx = static_cast<const int4*>(m_idx);
+                a.x = static_cast<const double*>(m_x);
+                a.dx = static_cast<const double*>(m_dx);
+                a.eta = eta;
+                a.th = thickness;
+                a.toc_in = toc_in;
+                a.max_iter = 1 << 20;
+                a.nv = nv;
+                a.toc_out = static_cast<double*>(const_cast<void*>(m_toc));
+                a.hit = static_cast<uint8_t*>(const_cast<void*>(m_hit));
+                a.iters = nullptr;
+                a.counter = cnt_d;
+                const int bps = exact ? accd_exact_blocks_per_sm() : accd_mixed_blocks_per_sm();
+                int grid = num_sms() * bps;
+                const int64_t need = (n + 255) / 256;
+                if (need < grid) grid = (int)need;
+                e2 = exact ? launch_accd_exact(a, grid, s) : launch_accd_mixed(a, grid, s);
+            }
+            if (e2 == cudaSuccess) e2 = cudaMemcpyAsync(cnt, cnt_d, sizeof(cnt), cudaMemcpyDeviceToHost, s);
+            if (cnt_d) cudaFreeAsync(cnt_d, s);
+            const cudaError_t e3 = cudaStreamSynchronize(s);
+            if (e2 == cudaSuccess) e2 = e3;
+            if (e2 != cudaSuccess) return set_cuda_error(e2, "cipc_ccd_pairs (page-locked host buffers)");
+            if (n_overflow) *n_overflow = (int64_t)cnt[1];
+            if (cnt[2])
+                return set_error(CIPC_ERR_INDEX_RANGE, "cipc_ccd_pairs: %llu pairs with a bad type or vertex index",
+                                 cnt[2]);
+            if (cnt[1])
+                return set_error(CIPC_ERR_ITER_CAP, "cipc_ccd_pairs: %llu pairs reached the iteration cap", cnt[1]);
+            return CIPC_OK;
+        }
+    }
+
     const int64_t chunk = std::max<int64_t>(2500000, (n + 63) / 64);
     const int nchunk = host ? (int)((n + chunk - 1) / chunk) : 1;
     const bool pipelined = nchunk > 1;

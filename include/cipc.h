@@ -80,9 +80,12 @@ int cipc_device_count(void);
  * iteration cap (2^20 steps) — they are reported as no hit; with any overflow the
  * call returns CIPC_ERR_ITER_CAP.  Pairs with an index outside [0, n_verts) or a
  * type above 3 are not evaluated and make the call return CIPC_ERR_INDEX_RANGE.
- * With CIPC_MEM_HOST the inputs are staged in stream-ordered allocations and
- * the call returns after the results are back; n_pairs above 2.5M are streamed
- * in chunks (records in, results out) around the kernel on internal streams.
+ * With CIPC_MEM_HOST the call returns after the results are back.  Page-locked
+ * host buffers (cudaHostAlloc / cudaHostRegister, e.g. pinned tensors) are read
+ * and written in place by the kernel over the CPU-GPU link (NVLink-C2C on
+ * Grace-Blackwell), with no staging copies.  Pageable host buffers are staged
+ * in stream-ordered allocations; n_pairs above 2.5M are then streamed in chunks
+ * (records in, results out) around the kernel on internal streams.
  */
 int cipc_ccd_pairs(int64_t n_pairs, const uint8_t* type, const int32_t* idx, int64_t n_verts,
                    const double* x, const double* dx, double eta, double thickness, double toc_in,

@@ -104,6 +104,29 @@ def test_ccd_scale_invariant(cuda, precision):
         assert np.array_equal(toc.view(np.uint64), toc0.view(np.uint64)), k
 
 
+@pytest.mark.parametrize("precision", [F.FP64, F.MIXED])
+def test_ccd_page_locked_host_buffers(cuda, precision):
+    """Host buffers in page-locked memory are read and written in place by the
+    kernel (no staging); results are bit-identical to the staged pageable call."""
+    import torch
+    w = workloads.contact_pairs(300_000, seed=14)
+    n = w["type"].shape[0]
+    pin = {k: torch.from_numpy(np.ascontiguousarray(w[k])).pin_memory().numpy() for k in ("type", "idx", "x", "dx")}
+    toc_p = torch.full((n,), -1.0, dtype=torch.float64).pin_memory().numpy()
+    hit_p = torch.full((n,), 7, dtype=torch.uint8).pin_memory().numpy()
+    st, ov = F.ccd_pairs(pin["type"], pin["idx"], pin["x"], pin["dx"], toc_p, hit_p, eta=ETA, thickness=TH,
+                         precision=precision)
+    toc_h, hit_h, st_h, ov_h = _gpu_ccd(w, precision)
+    assert st == st_h == 0 and ov == ov_h == 0
+    assert np.array_equal(hit_p, hit_h) and 0 < hit_p.sum() < n
+    assert np.array_equal(toc_p.view(np.uint64), toc_h.view(np.uint64))
+    # a bad index is still caught and reported
+    pin["idx"][5, 1] = w["x"].shape[0] + 2
+    with pytest.raises(F.CipcError) as ei:
+        F.ccd_pairs(pin["type"], pin["idx"], pin["x"], pin["dx"], toc_p, hit_p, eta=ETA, thickness=TH)
+    assert ei.value.status == F.CIPC_ERR_INDEX_RANGE
+
+
 def test_ccd_device_memory_matches_host(cuda):
     import torch
     w = workloads.contact_pairs(50_000, seed=4)
