@@ -147,8 +147,8 @@ CIPC_HD int tri_lt2(iv a, iv b) { const int s = iv_cmp2(a, b); return s < 0 ? kT
 
 CIPC_HD iv3 iv3_sub(iv3 a, iv3 b) { return iv3{iv_sub(a.x, b.x), iv_sub(a.y, b.y), iv_sub(a.z, b.z)}; }
 CIPC_HD iv3 iv3_neg(iv3 a) { return iv3{iv_neg(a.x), iv_neg(a.y), iv_neg(a.z)}; }
-// dot(a,b) = fma(az,bz, fma(ay,by, ax*bx))  (the FP64 rule of geom.cuh)
-CIPC_HD iv iv3_dot(iv3 a, iv3 b) { return iv_fma(a.z, b.z, iv_fma(a.y, b.y, iv_mul(a.x, b.x))); }
+// dot(a,b) = fma(az,bz, fma(ax,bx, ay*by))  (the FP64 rule of geom.cuh)
+CIPC_HD iv iv3_dot(iv3 a, iv3 b) { return iv_fma(a.z, b.z, iv_fma(a.x, b.x, iv_mul(a.y, b.y))); }
 // cross: fma(a.y, b.z, -(a.z * b.y)), ...
 CIPC_HD iv3 iv3_cross(iv3 a, iv3 b)
 {

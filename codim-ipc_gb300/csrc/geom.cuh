@@ -2,7 +2,7 @@
 // distances and additive-CCD state, in FP64.
 //
 // Arithmetic rule (shared with the CPU checker so FP64 decisions agree bit for
-// bit): dot products are fma chains  dot(a,b) = fma(a.z,b.z, fma(a.y,b.y, a.x*b.x)),
+// bit): dot products are fma chains  dot(a,b) = fma(a.z,b.z, fma(a.x,b.x, a.y*b.y)),
 // cross products use one fma per component, position updates x + t*d are a single
 // fma, and everything else is evaluated left to right.  On the device every other
 // FP64 operation here is an explicit-rounding intrinsic (__dadd_rn, __dmul_rn,
@@ -39,7 +39,7 @@ CIPC_HD d3 operator-(d3 a, d3 b) { return d3{G_SUB(a.x, b.x), G_SUB(a.y, b.y), G
 CIPC_HD d3 operator+(d3 a, d3 b) { return d3{G_ADD(a.x, b.x), G_ADD(a.y, b.y), G_ADD(a.z, b.z)}; }
 CIPC_HD d3 scl(d3 a, double s) { return d3{G_MUL(a.x, s), G_MUL(a.y, s), G_MUL(a.z, s)}; }
 CIPC_HD d3 dvs(d3 a, double s) { return d3{G_DIV(a.x, s), G_DIV(a.y, s), G_DIV(a.z, s)}; }
-CIPC_HD double dot(d3 a, d3 b) { return fma(a.z, b.z, fma(a.y, b.y, G_MUL(a.x, b.x))); }
+CIPC_HD double dot(d3 a, d3 b) { return fma(a.z, b.z, fma(a.x, b.x, G_MUL(a.y, b.y))); }
 CIPC_HD double n2(d3 a) { return dot(a, a); }
 CIPC_HD d3 cross(d3 a, d3 b)
 {

@@ -18,6 +18,7 @@ they lie and piped straight into g++ (nothing is written to disk but the .so),
 so the oracle's own derivation can be pinned against them.
 """
 import os
+import platform
 import re
 import subprocess
 import sys
@@ -155,6 +156,122 @@ def build_ref(force=False):
     return out
 
 
+# The reference's distance-type, distance and ACCD routines, in the order they
+# depend on each other: (file, function, text its signature must contain).
+_REF_CCD_FUNCS = [
+    ("Library/Math/Distance/POINT_POINT.h", "Point_Point_Distance", ""),
+    ("Library/Math/Distance/POINT_EDGE.h", "Point_Edge_Distance", ""),
+    ("Library/Math/Distance/POINT_TRIANGLE.h", "Point_Triangle_Distance", ""),
+    ("Library/Math/Distance/EDGE_EDGE.h", "Edge_Edge_Distance", ""),
+    ("Library/Math/Distance/DISTANCE_TYPE.h", "Point_Edge_Distance_Type", ""),
+    ("Library/Math/Distance/DISTANCE_TYPE.h", "Point_Triangle_Distance_Type", ""),
+    ("Library/Math/Distance/DISTANCE_TYPE.h", "Edge_Edge_Distance_Type", ""),
+    ("Library/Math/Distance/DISTANCE_UNCLASSIFIED.h", "Point_Triangle_Distance_Unclassified", ""),
+    ("Library/Math/Distance/DISTANCE_UNCLASSIFIED.h", "Edge_Edge_Distance_Unclassified", ""),
+    ("Library/Math/Distance/DISTANCE_UNCLASSIFIED.h", "Point_Edge_Distance_Unclassified", ""),
+    ("Library/Math/Distance/CCD.h", "Point_Triangle_CCD", ""),
+    ("Library/Math/Distance/CCD.h", "Edge_Edge_CCD", ""),
+    ("Library/Math/Distance/CCD.h", "Point_Edge_CCD", "Matrix<T, 3, 1>"),
+    ("Library/Math/Distance/CCD.h", "Point_Point_CCD", ""),
+]
+
+# flags of the reference's own build: build.py configures CMAKE_BUILD_TYPE=Release
+# (-O3 -DNDEBUG) and CMakeLists.txt:20 adds -mfma -mbmi2 -mavx2 (x86 only).  The
+# vectorizer is turned off: GCC vectorizes the shim's small loops in some call
+# sites and not others (in the point-edge ACCD it then fuses one norm's products
+# in the other order), which says nothing about how real Eigen's code would be
+# vectorized; with it off the compiled reference is one consistent contraction
+# policy, the one the oracle and the CUDA kernels follow.
+_REF_FLAGS_X86 = ["-O3", "-DNDEBUG", "-mfma", "-mbmi2", "-mavx2", "-fno-tree-vectorize"]
+
+
+def _extract_def(text, name, must):
+    """`template <...> <ret> name(...) {...}` whose signature contains `must`."""
+    for m in re.finditer(r"template\s*<[^>]*>\s*(?:inline\s+)?(?:void|T|int|bool)\s+" + re.escape(name) + r"\s*\(",
+                         text):
+        i = text.index("{", m.end())
+        if must and must not in text[m.end():i]:
+            continue
+        depth = 0
+        j = i
+        while j < len(text):
+            if text.startswith("//", j):  # braces in comments do not count
+                j = text.index("\n", j)
+                continue
+            if text.startswith("/*", j):
+                j = text.index("*/", j) + 2
+                continue
+            if text[j] == "{":
+                depth += 1
+            elif text[j] == "}":
+                depth -= 1
+                if depth == 0:
+                    return text[m.start():j + 1]
+            j += 1
+    raise RuntimeError("function %s not found" % name)
+
+
+def build_ref_ccd(force=False):
+    """Compile the reference's own distance-type classification, unclassified
+    distances and additive CCD (DISTANCE_TYPE.h, DISTANCE_UNCLASSIFIED.h,
+    POINT_*.h, EDGE_EDGE.h, CCD.h:279-483) against oracle/eigen_shim.h with the
+    reference's build flags into oracle/_ref/libcipc_ref_ccd.so (x86 hosts; the
+    functions are cut out of the headers and piped into g++, nothing else is
+    written).  Returns None when the sources or an x86 compiler are absent."""
+    if not os.path.isdir(REF_ROOT) or platform.machine() not in ("x86_64", "AMD64"):
+        return None
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "libcipc_ref_ccd.so")
+    shim = os.path.join(HERE, "eigen_shim.h")
+    if os.path.exists(out) and not force and os.path.getmtime(out) >= os.path.getmtime(shim):
+        return out
+    parts = ['#include "%s"\n#include <cstdint>\nnamespace ref {\n' % shim]
+    cache = {}
+    for f, name, must in _REF_CCD_FUNCS:
+        if f not in cache:
+            with open(os.path.join(REF_ROOT, f)) as fh:
+                cache[f] = fh.read()
+        parts.append(_extract_def(cache[f], name, must) + "\n")
+    parts.append("}\n")
+    parts.append(r"""
+typedef Eigen::Matrix<double, 3, 1> V3;
+static V3 v3(const double* p) { V3 r; r.a[0] = p[0]; r.a[1] = p[1]; r.a[2] = p[2]; return r; }
+extern "C" {
+int refc_pt_type(const double* x) { return ref::Point_Triangle_Distance_Type(v3(x), v3(x + 3), v3(x + 6), v3(x + 9)); }
+int refc_ee_type(const double* x) { return ref::Edge_Edge_Distance_Type(v3(x), v3(x + 3), v3(x + 6), v3(x + 9)); }
+int refc_pe_type(const double* x) { double r; return ref::Point_Edge_Distance_Type<double, 3>(v3(x), v3(x + 3), v3(x + 6), r); }
+double refc_pt_d2(const double* x) { double d; ref::Point_Triangle_Distance_Unclassified(v3(x), v3(x + 3), v3(x + 6), v3(x + 9), d); return d; }
+double refc_ee_d2(const double* x) { double d; ref::Edge_Edge_Distance_Unclassified(v3(x), v3(x + 3), v3(x + 6), v3(x + 9), d); return d; }
+double refc_pe_d2(const double* x) { double d; ref::Point_Edge_Distance_Unclassified(v3(x), v3(x + 3), v3(x + 6), d); return d; }
+// ACCD over pairs (type 0 PP, 1 PE, 2 PT, 3 EE; four vertex indices each); a
+// miss reports toc_in, as the C ABI does (the reference leaves toc undefined then)
+void refc_ccd_pairs(int64_t n, const uint8_t* type, const int32_t* idx, const double* x, const double* dx,
+                    double eta, double th, double toc_in, double* toc_out, uint8_t* hit)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        const int32_t* id = idx + 4 * i;
+        double toc = toc_in;
+        bool h = false;
+        switch (type[i]) {
+            case 0: h = ref::Point_Point_CCD(v3(x + 3 * id[0]), v3(x + 3 * id[1]), v3(dx + 3 * id[0]), v3(dx + 3 * id[1]), eta, th, toc); break;
+            case 1: h = ref::Point_Edge_CCD(v3(x + 3 * id[0]), v3(x + 3 * id[1]), v3(x + 3 * id[2]), v3(dx + 3 * id[0]), v3(dx + 3 * id[1]), v3(dx + 3 * id[2]), eta, th, toc); break;
+            case 2: h = ref::Point_Triangle_CCD(v3(x + 3 * id[0]), v3(x + 3 * id[1]), v3(x + 3 * id[2]), v3(x + 3 * id[3]), v3(dx + 3 * id[0]), v3(dx + 3 * id[1]), v3(dx + 3 * id[2]), v3(dx + 3 * id[3]), eta, th, toc); break;
+            default: h = ref::Edge_Edge_CCD(v3(x + 3 * id[0]), v3(x + 3 * id[1]), v3(x + 3 * id[2]), v3(x + 3 * id[3]), v3(dx + 3 * id[0]), v3(dx + 3 * id[1]), v3(dx + 3 * id[2]), v3(dx + 3 * id[3]), eta, th, toc); break;
+        }
+        hit[i] = h ? 1 : 0;
+        toc_out[i] = h ? toc : toc_in;
+    }
+}
+}
+""")
+    src = "".join(parts)
+    cmd = ["g++", "-std=c++17", "-fPIC", "-shared"] + _REF_FLAGS_X86 + ["-x", "c++", "-", "-o", out]
+    subprocess.run(cmd, input=src.encode(), check=True)
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     print(build_ref(force="--force" in sys.argv))
+    print(build_ref_ccd(force="--force" in sys.argv))

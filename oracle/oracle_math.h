@@ -6,11 +6,14 @@
 // suite, the smoke check and the bench's CPU-baseline leg may load it.  Nothing in
 // the product links or calls it.
 //
-// Canonical arithmetic.  The reference is compiled with -mfma and lets GCC contract
-// a*b+c freely, so its last-bit rounding is not reproducible without its binary.
-// This oracle instead fixes one explicit rule, which the CUDA kernels follow too,
-// so that accept/reject decisions and FP64 values agree bit for bit:
-//   dot3(a,b)   = fma(a2,b2, fma(a1,b1, a0*b0))
+// Canonical arithmetic.  The reference is compiled with -O3 -mfma and lets GCC
+// contract a*b+c.  This oracle fixes the contractions GCC 13 makes there on the
+// reference's own source (measured by compiling the reference's distance-type,
+// distance and ACCD routines against oracle/eigen_shim.h with the reference's
+// flags and its vectorizer off, oracle/build.py:build_ref_ccd; the bit-for-bit
+// pin is tests/test_oracle_reference_ccd.py), and the CUDA kernels follow the
+// same rule, so that accept/reject decisions and FP64 values agree bit for bit:
+//   dot3(a,b)   = fma(a2,b2, fma(a0,b0, a1*b1))
 //   cross(a,b)  = (fma(a1,b2,-(a2*b1)), fma(a2,b0,-(a0*b2)), fma(a0,b1,-(a1*b0)))
 //   x + t*d     = fma(t,d,x)
 // and every other expression is evaluated left to right with no contraction
@@ -31,7 +34,7 @@ static inline V3 operator-(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b
 static inline V3 operator+(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
 static inline V3 scale(V3 a, double s) { return V3{a.x * s, a.y * s, a.z * s}; }
 static inline V3 divs(V3 a, double s) { return V3{a.x / s, a.y / s, a.z / s}; }
-static inline double dot(V3 a, V3 b) { return std::fma(a.z, b.z, std::fma(a.y, b.y, a.x * b.x)); }
+static inline double dot(V3 a, V3 b) { return std::fma(a.z, b.z, std::fma(a.x, b.x, a.y * b.y)); }
 static inline double norm2(V3 a) { return dot(a, a); }
 static inline V3 cross(V3 a, V3 b)
 {

@@ -9,9 +9,9 @@ Bars:
   * constraint sets at identical states: equal as sets (kind, vertices, multiplicity);
   * incremental potential and gradient at identical states: 1e-10 relative;
   * intersection-free step size along a direction: 1e-12 relative;
-  * positions after time steps solved to a tight Newton tolerance (3e-8 on the
-    cloth-on-box steps, 1e-7 elsewhere) and a tight PCG tolerance (1e-12): within
-    1e-8 of the bounding-box diagonal of the
+  * positions after time steps solved to a tight Newton tolerance (1e-7; on the
+    cloth-on-box steps the GPU runs the oracle's iteration count) and a tight PCG
+    tolerance (1e-12): within 1e-8 of the bounding-box diagonal of the
     oracle's direct-solve Newton (1e-7 on the augmented-Lagrangian Dirichlet path);
   * every step ends intersection free (minimum d^2 - xi^2 > 0).
 """
@@ -109,6 +109,15 @@ def test_ccd_step_size_matches(cuda, trajectory):
 
 @pytest.mark.parametrize("nh", [True, False])
 def test_steps_match_direct_solve(cuda, orc, nh):
+    """Single steps from the oracle's states: GPU positions within 1e-8 of the
+    bounding-box diagonal of the oracle's direct-solve Newton after the same
+    number of Newton iterations.  The oracle stops at a Newton tolerance of 1e-7;
+    the GPU runs exactly as many iterations (its tolerance set below reach, the
+    iteration cap at the oracle's count).  A tolerance-based stop on both sides
+    would compare endpoints that are not determined to 1e-8: on these contact
+    steps the max-of-last-3 test can pass one iteration apart, and continuing
+    past 1e-7 moves the oracle's own endpoint by up to 0.6% of the diagonal on a
+    plateau step."""
     X, T, dbc = scene(n=8, y=-0.095)
     sh = orc.Shell(X, T, **MAT, nh=nh)
     k2o, dhat2 = sh.init_oipc(DHAT)
@@ -117,22 +126,16 @@ def test_steps_match_direct_solve(cuda, orc, nh):
     assert np.allclose(k2o, k2g, rtol=1e-12) and dhat2 == dhat2g
     xo = X.copy()
     vo = np.zeros_like(X)
-    # at a Newton tolerance of 1e-7 the oracle's own endpoint is determined only to
-    # ~1.4e-8 of the diagonal (its distance to the endpoint of a run to 2e-8); at
-    # 3e-8 it is within 8e-10, which leaves the 1e-8 bar to the GPU path.  Near
-    # that tolerance a line search may no longer decrease the FP64 energy (its
-    # rounding floor); a GPU step that stops there at the iteration cap is still
-    # held to the same bar
-    prm = F.make_params(DT, dhat2, XI, newton_tol=3e-8, pcg_tol=1e-12, max_newton_iters=150)
     diag = np.linalg.norm(X.max(0) - X.min(0))
     for step in range(4):
         # each step starts from the oracle's state
         s.set_state(xo, vo)
         s.set_kappa(k2o[0], k2o[1])
-        rc, sto = sh.step(xo, vo, k2o, dbc, X[dbc], DT, dhat2, XI, tol=3e-8, max_iter=400)
+        rc, sto = sh.step(xo, vo, k2o, dbc, X[dbc], DT, dhat2, XI, tol=1e-7, max_iter=400)
         assert rc == 0
+        prm = F.make_params(DT, dhat2, XI, newton_tol=1e-30, pcg_tol=1e-12, max_newton_iters=sto["newton_iters"])
         stg = s.step(prm, allow=(F.CIPC_ERR_NOT_CONVERGED,))
-        assert stg.status in (0, -1, -3), stg.as_dict()
+        assert stg.newton_iters == sto["newton_iters"], (stg.as_dict(), sto)
         xg, vg = s.state()
         assert stg.min_dist2 > 0 or stg.n_constraints == 0
         err = np.abs(xg - xo).max()
