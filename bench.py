@@ -110,14 +110,18 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _traffic(name):
-    """DRAM bytes per launch from a committed ncu summary (profiles/<name>.txt), else None."""
+def _traffic(name, pairs=None):
+    """DRAM bytes per launch from a committed ncu summary (profiles/<name>.txt):
+    its `dram_bytes_per_launch:` line, or its `dram_bytes_per_pair:` line times
+    `pairs` (a capture of a smaller case scaled to the launch); else None."""
     p = os.path.join(ROOT, "profiles", name + ".txt")
     if not os.path.exists(p):
         return None
     for line in open(p):
         if line.startswith("dram_bytes_per_launch:"):
             return float(line.split(":")[1])
+        if line.startswith("dram_bytes_per_pair:") and pairs:
+            return round(float(line.split(":")[1]) * pairs)
     return None
 
 
@@ -516,7 +520,7 @@ def run_ours(args):
     launch_s = float(np.mean(per)) / 1e3
     peak, peak_kind = _peaks()
     achieved = ccd_bytes / launch_s / 1e9
-    traffic = _traffic("accd_%s_10M_pairs" % args.precision)
+    traffic = _traffic("accd_mixed_10M_pairs") if prec == F.MIXED else _traffic("accd_fp64_2M_pairs", n)
 
     line = None
     if rank == 0:

@@ -21,6 +21,7 @@ CIPC_ERR_NOT_CONVERGED = 5
 CIPC_ERR_NAN = 6
 CIPC_ERR_NO_DEVICE = 7
 CIPC_ERR_INDEX_RANGE = 8
+CIPC_ERR_TIMEOUT = 9
 
 FP64 = 0
 MIXED = 1
@@ -246,7 +247,8 @@ class StepParams(ctypes.Structure):
                 ("epsv2", ctypes.c_double), ("fric_iters", ctypes.c_int), ("newton_tol", ctypes.c_double),
                 ("with_collision", ctypes.c_int), ("max_newton_iters", ctypes.c_int), ("precision", ctypes.c_int),
                 ("pcg_tol", ctypes.c_double), ("pcg_max_iters", ctypes.c_int), ("preconditioner", ctypes.c_int),
-                ("forcing", ctypes.c_int), ("barrier_model", ctypes.c_int)]
+                ("forcing", ctypes.c_int), ("barrier_model", ctypes.c_int), ("accd_max_iters", ctypes.c_int),
+                ("pcg_wait_polls", ctypes.c_int)]
 
 
 class StepStats(ctypes.Structure):
@@ -290,9 +292,10 @@ _SIGS.update({
 
 def make_params(h, dhat2, xi, mu=0.0, epsv2=1e-6, fric_iters=1, newton_tol=1e-2, with_collision=True,
                 max_newton_iters=200, precision=FP64, pcg_tol=1e-6, pcg_max_iters=10000, preconditioner=0,
-                forcing=0, elastic_ipc=False):
+                forcing=0, elastic_ipc=False, accd_max_iters=0, pcg_wait_polls=0):
     return StepParams(h, dhat2, xi, mu, epsv2, fric_iters, newton_tol, int(bool(with_collision)), max_newton_iters,
-                      precision, pcg_tol, pcg_max_iters, preconditioner, forcing, 1 if elastic_ipc else 0)
+                      precision, pcg_tol, pcg_max_iters, preconditioner, forcing, 1 if elastic_ipc else 0,
+                      accd_max_iters, pcg_wait_polls)
 
 
 class CodimDesc(ctypes.Structure):
@@ -583,3 +586,36 @@ def sim_capture_systems(sim, precond, max_systems):
 
 def sim_set_precond(sim, precond):
     _check(lib().cipc_sim_set_precond(sim.h, precond.h if precond is not None else None))
+
+
+_SIGS.update({
+    "cipc_sim_set_output": (_c_int, [_vp, ctypes.c_char_p]),
+    "cipc_sim_save_state": (_c_int, [_vp, ctypes.c_char_p]),
+    "cipc_sim_load_state": (_c_int, [_vp, ctypes.c_char_p]),
+    "cipc_sim_load_obj_frames": (_c_int, [_vp, ctypes.c_char_p, ctypes.c_char_p, _c_dbl]),
+})
+if _lib is not None:
+    for _name in ("cipc_sim_set_output", "cipc_sim_save_state", "cipc_sim_load_state", "cipc_sim_load_obj_frames"):
+        _f = getattr(_lib, _name)
+        _f.restype, _f.argtypes = _SIGS[_name]
+
+
+def _enc(p):
+    return None if p is None else str(p).encode()
+
+
+def sim_set_output(sim, folder):
+    """Run logs (residual.txt, counter.txt, Hessian_info.txt, steps.jsonl) into folder; None stops."""
+    _check(lib().cipc_sim_set_output(sim.h, _enc(folder)))
+
+
+def sim_save_state(sim, path):
+    _check(lib().cipc_sim_save_state(sim.h, _enc(path)))
+
+
+def sim_load_state(sim, path):
+    _check(lib().cipc_sim_load_state(sim.h, _enc(path)))
+
+
+def sim_load_obj_frames(sim, obj_prev, obj_last, dt):
+    _check(lib().cipc_sim_load_obj_frames(sim.h, _enc(obj_prev), _enc(obj_last), float(dt)))

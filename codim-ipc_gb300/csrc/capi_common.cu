@@ -84,6 +84,7 @@ extern "C" const char* cipc_status_string(int status)
         case CIPC_ERR_NAN: return "NaN encountered";
         case CIPC_ERR_NO_DEVICE: return "no CUDA device";
         case CIPC_ERR_INDEX_RANGE: return "index out of range";
+        case CIPC_ERR_TIMEOUT: return "device-side wait timed out";
     }
     return "unknown status";
 }

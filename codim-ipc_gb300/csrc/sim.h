@@ -1,6 +1,7 @@
 // Device-resident state of one shell simulation (one CUDA stream per handle) and
 // the internal entry points of the time-step kernels.
 #pragma once
+#include <string>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -77,6 +78,8 @@ struct SimParams {
     int precond = 0;          // 0 block-Jacobi, 1 learned correction (when a model is loaded)
     int forcing = 0;          // 1: inexact Newton (Eisenstat-Walker forcing term)
     int elastic = 0;          // 1: elastic IPC (no offset, barrier scaled by 1/dhat^4, kappa fixed)
+    long long accd_max_iter = 1 << 20;  // ACCD steps per pair before the step reports CIPC_ERR_ITER_CAP
+    int pcg_wait_polls = 0;   // PCG grid-wait poll limit (0: the solver's default, over a second)
 };
 
 struct StepStats {
@@ -105,6 +108,8 @@ struct Sim {
     DBuf<double> sl_prev;     // per-triangle largest stretch after the previous Newton iteration
     bool sl_have_prev = false;
     int trace = 0;    // CIPC_TRACE set: one stderr line per Newton iteration and refinement pass
+    std::string out_dir;  // run logs (residual.txt, counter.txt, Hessian_info.txt, steps.jsonl) when set
+    int step_count = 0;   // steps taken (successful or not) since creation or the last restore
     // static device data
     DBuf<int> tri, hinge, bnode, bedge, btri;
     DBuf<double> P, vol, hinfo, mass, b, X0;

@@ -1453,7 +1453,7 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         a.eta = 0.1;
         a.th = s->prm.xi;
         a.toc_in = alpha;
-        a.max_iter = 1 << 20;
+        a.max_iter = s->prm.accd_max_iter;
         a.nv = s->nv;
         a.toc_out = toc;
         a.hit = hit;
@@ -1469,10 +1469,16 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         e = launch_accd_exact(a, grid, st);
         if (e != cudaSuccess) return set_cuda_error(e, "ccd");
         double res;
+        unsigned long long over = 0;
         cudaMemcpyAsync(&res, amin, sizeof(double), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(&over, ctr + 3, sizeof(over), cudaMemcpyDeviceToHost, st);
         e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return set_cuda_error(e, "ccd");
         *alpha_out = res;
+        // the reference's ACCD loops without bound there; here the step stops and says so
+        if (over)
+            return set_error(CIPC_ERR_ITER_CAP, "step size: %llu CCD pairs reached the cap of %lld ACCD steps", over,
+                             s->prm.accd_max_iter);
         return CIPC_OK;
     }
     return set_error(CIPC_ERR_CUDA, "ccd candidates did not fit after resizing");

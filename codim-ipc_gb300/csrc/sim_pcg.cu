@@ -50,10 +50,8 @@ struct PcgScalars {
     int done;       // 1 converged, 2 NaN, 3 (p, Hp) <= 0, 4 iteration cap, 5 barrier wait gave up
     int err;
     int pad;
-    // arrivals (monotone: gridDim.x per reduction) and the accumulators, on their
-    // own 128-byte lines; reduction e adds into acc[e % 3]
+    // arrivals (monotone: gridDim.x per reduction), on its own 128-byte line
     alignas(128) unsigned int arrive;
-    alignas(128) double acc[3][4];
     // with tracing on: block 0's time (ns) in apply, reduction 1, -, update,
     // reduction 2, -, summed over iterations
     unsigned long long tphase[6];
@@ -106,15 +104,17 @@ struct PcgArgs {
     int maxit;
     int ncon, nfric;
     int trace;
+    unsigned int wait_polls;  // polls of the arrival counter before a grid wait gives up
+    double* part;             // 2 x gridDim.x x 4 block partial sums (reduction e uses half e % 2)
 };
 
 // 256-thread blocks: a grid-wide reduction costs ~2.5 us with 152 blocks, ~3.7
 // with 304 and ~6 with 608 (arrivals on one counter), against ~3.5 / ~5 with
 // 512-thread blocks (the block-level sum grows)
 constexpr int kPcgThreads = 256;
-// polls of the arrival counter before a wait gives up: each poll is an L2 round
-// trip (>= ~0.3 us), and past kBarrierBackoff polls a 64 ns sleep is added, so the
-// limit is over a second
+// default polls of the arrival counter before a wait gives up: each poll is an L2
+// round trip (>= ~0.3 us), and past kBarrierBackoff polls a 64 ns sleep is added,
+// so the limit is over a second (cipc_step_params.pcg_wait_polls overrides it)
 constexpr unsigned int kBarrierSpinLimit = 1u << 22;
 constexpr unsigned int kBarrierBackoff = 4096;
 
@@ -142,16 +142,21 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p)
 // Grid-wide sum of v (N <= 4 values per thread, summed over all threads of all
 // blocks), returned in v to every thread; also a grid barrier.  epoch counts the
 // reductions this thread has taken part in (the same in every thread).  Thread 0
-// of each block adds the block's sums into acc[epoch % 3], arrives with release
-// semantics and polls the counter until every block of reduction `epoch` has
-// arrived.  acc[(epoch + 2) % 3] held the totals of reduction epoch - 1, which
-// every block has read before arriving here, so block 0 clears it for reduction
-// epoch + 2.  Returns false if the wait gave up (err set; the kernel returns).
-// Warp-level sums run in the solver's precision AT (FP32 shuffles and adds in the
-// FP32 solver: this part's FP64 work otherwise competes for GB300's narrow FP64
-// pipe); block and grid sums are FP64.  The totals land in out.
+// of each block stores the block's sums into its slot of part[epoch % 2], arrives
+// on a monotone counter with release semantics and polls it (acquire) until every
+// block of reduction `epoch` has arrived; then warp 0 of every block adds all
+// blocks' partials in one fixed order (lane l takes blocks l, l + 32, ...; then a
+// fixed shuffle tree), so the totals are identical in every block and in every
+// run: the solver is deterministic.  part[epoch % 2] is rewritten only by
+// reduction epoch + 2, which no block can reach before every block has passed
+// reduction epoch + 1, i.e. finished reading it.  Returns false if the wait gave
+// up (err set; the kernel returns).  Warp-level sums of the thread values run in
+// the solver's precision AT (FP32 shuffles and adds in the FP32 solver: this
+// part's FP64 work otherwise competes for GB300's narrow FP64 pipe); block and
+// grid sums are FP64.  The totals land in out.
 template <int N, typename AT>
-__device__ __forceinline__ bool grid_allreduce(const AT (&v)[N], double (&out)[N], PcgScalars* d, unsigned int& epoch)
+__device__ __forceinline__ bool grid_allreduce(const AT (&v)[N], double (&out)[N], PcgScalars* d, unsigned int& epoch,
+                                               unsigned int limit, double* part)
 {
     static_assert(N >= 1 && N <= 4, "reduction width");
     __shared__ double sh[N][kPcgThreads / 32];
@@ -166,14 +171,14 @@ __device__ __forceinline__ bool grid_allreduce(const AT (&v)[N], double (&out)[N
         if (lane == 0) sh[k][wid] = (double)a;
     }
     __syncthreads();
+    double* half = part + (size_t)(epoch & 1u) * gridDim.x * 4;
     if (threadIdx.x == 0) {
-        double* acc = d->acc[epoch % 3];
 #pragma unroll
         for (int k = 0; k < N; ++k) {
             double a = 0;
 #pragma unroll
             for (int w = 0; w < kPcgThreads / 32; ++w) a += sh[k][w];
-            red_add_f64(acc + k, a);
+            __stcg(half + 4 * (size_t)blockIdx.x + k, a);
         }
         red_release_add_u32(&d->arrive, 1u);
         const unsigned int target = (epoch + 1) * gridDim.x;
@@ -181,25 +186,29 @@ __device__ __forceinline__ bool grid_allreduce(const AT (&v)[N], double (&out)[N
         unsigned int spins = 0;
         while ((int)(ld_acquire_u32(&d->arrive) - target) < 0) {
             ++spins;
-            if (spins > kBarrierSpinLimit || ((spins & 255) == 0 && *(volatile int*)&d->err)) {
+            if (spins > limit || ((spins & 255) == 0 && *(volatile int*)&d->err)) {
                 atomicExch(&d->err, 1);
                 good = 0;
                 break;
             }
             if (spins > kBarrierBackoff) __nanosleep(64);
         }
-#pragma unroll
-        for (int k = 0; k < N; ++k) res[k] = __ldcg(acc + k);
-        if (blockIdx.x == 0) {
-            double* z = d->acc[(epoch + 2) % 3];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) z[k] = 0;
-        }
         ok = good;
     }
     __syncthreads();
     ++epoch;
     if (!ok) return false;
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            double a = 0;
+            for (int b = lane; b < (int)gridDim.x; b += 32) a += __ldcg(half + 4 * (size_t)b + k);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+            if (lane == 0) res[k] = a;
+        }
+    }
+    __syncthreads();
 #pragma unroll
     for (int k = 0; k < N; ++k) out[k] = res[k];
     return true;
@@ -368,7 +377,7 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
                 v[1] += (double)r[c] * (double)r[c];
             }
         }
-        if (!grid_allreduce<2>(v, v, d, epoch)) return;
+        if (!grid_allreduce<2>(v, v, d, epoch, a.wait_polls, a.part)) return;
         tot[0] = v[0];
         tot[1] = v[1];
     }
@@ -398,7 +407,7 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
         const XT va[1] = {apply_phase<VT, XT, PT>(a, beta, zp, zp_next)};
         double vd[1];
         lap(0);
-        if (!grid_allreduce<1>(va, vd, d, epoch)) return;
+        if (!grid_allreduce<1>(va, vd, d, epoch, a.wait_polls, a.part)) return;
         lap(1);
         pq = vd[0];
         if (!(pq > 0 && pq < INFINITY)) {
@@ -428,7 +437,7 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
         const XT vb_t[2] = {rz_t, rr_t};
         double vb[2];
         lap(3);
-        if (!grid_allreduce<2>(vb_t, vb, d, epoch)) return;
+        if (!grid_allreduce<2>(vb_t, vb, d, epoch, a.wait_polls, a.part)) return;
         lap(4);
         tot[0] = vb[0];
         tot[1] = vb[1];
@@ -459,6 +468,7 @@ constexpr int kVecs = 9;  // r, (z, p) pairs x 2 (two vectors each), q_e, q_c, a
 struct PcgState {
     DBuf<char> vec;              // kVecs vectors of 3 nv entries
     DBuf<PcgScalars> dsc;        // device scalars
+    DBuf<double> part;           // block partial sums of the grid reductions
     PcgScalars* host = nullptr;  // pinned copy of the results
     int grid[2] = {0, 0};        // co-resident grid per precision (0 FP64, 1 FP32)
     ~PcgState()
@@ -466,6 +476,7 @@ struct PcgState {
         if (host) cudaFreeHost(host);
         vec.release();
         dsc.release();
+        part.release();
     }
 };
 
@@ -562,6 +573,10 @@ int solve(Sim* s, const XT* b, XT* x, double tol, int maxit, int* iters, double*
     a.ncon = s->prm.withCollision ? s->ncon : 0;
     a.nfric = (s->prm.withCollision && s->prm.mu > 0) ? s->nfric : 0;
     a.trace = s->trace;
+    a.wait_polls = s->prm.pcg_wait_polls > 0 ? (unsigned int)s->prm.pcg_wait_polls : kBarrierSpinLimit;
+    if ((int)st->part.n < 8 * g && st->part.alloc(8 * (size_t)g) != cudaSuccess)
+        return set_error(CIPC_ERR_CUDA, "PCG partial sums");
+    a.part = st->part.p;
     // barrier state starts clear (a previous solve may have given up mid-way)
     cudaError_t e = cudaMemsetAsync(st->dsc.p, 0, sizeof(PcgScalars), str);
     void* args[] = {&a};
@@ -582,7 +597,7 @@ int solve(Sim* s, const XT* b, XT* x, double tol, int maxit, int* iters, double*
                      *rel, h->it, h->done, g, h->tphase[0] * 1e-3 / it, h->tphase[1] * 1e-3 / it,
                      h->tphase[3] * 1e-3 / it, h->tphase[4] * 1e-3 / it);
     }
-    if (h->err) return set_error(CIPC_ERR_CUDA, "PCG: grid barrier wait gave up");
+    if (h->err) return set_error(CIPC_ERR_TIMEOUT, "PCG: a grid-wide wait gave up after %u polls", a.wait_polls);
     if (h->done == 2) return set_error(CIPC_ERR_NAN, "PCG produced NaN");
     if (h->done == 3) return set_error(CIPC_ERR_NOT_CONVERGED, "PCG: non-positive curvature (p, Hp) = %g", h->pq);
     if (h->done == 4) return set_error(CIPC_ERR_NOT_CONVERGED, "PCG stopped at relative residual %g", *rel);

@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <deque>
@@ -172,6 +173,108 @@ static int min_d2(Sim* s, const double* x, double* out)
     return e == cudaSuccess ? CIPC_OK : set_cuda_error(e, "min distance");
 }
 
+// Run logs in the reference's formats, appended in the simulation's output
+// folder when one is set (cipc_sim_set_output): residual.txt one line per Newton
+// iteration, "PNIter avgResMag maxRes Eprev L2Norm" (IMPLICIT_EULER.h:647-670);
+// counter.txt one line per step, "PNIter[ #constraints]" (:868-875);
+// Hessian_info.txt when a Newton system could not be solved (:531-534, there a
+// non-SPD factorisation); and steps.jsonl, one JSON object of step statistics
+// per step (no reference counterpart).
+static void log_line(Sim* s, const char* file, const char* fmt, ...)
+{
+    FILE* f = std::fopen((s->out_dir + "/" + file).c_str(), "a+");
+    if (!f) return;
+    va_list ap;
+    va_start(ap, fmt);
+    std::vfprintf(f, fmt, ap);
+    va_end(ap);
+    std::fclose(f);
+}
+
+// per-vertex magnitudes of the Newton step: sum of |p_i| and max |p_ij|
+__global__ void k_resmag(int nv, const double* p, double* part)
+{
+    __shared__ double ss[256], sm[256];
+    double sum = 0, mx = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) {
+        const double a = p[3 * i], b = p[3 * i + 1], c = p[3 * i + 2];
+        sum += sqrt(a * a + b * b + c * c);
+        mx = fmax(mx, fmax(fabs(a), fmax(fabs(b), fabs(c))));
+    }
+    ss[threadIdx.x] = sum;
+    sm[threadIdx.x] = mx;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            ss[threadIdx.x] += ss[threadIdx.x + w];
+            sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + w]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = ss[0];
+        part[2 * blockIdx.x + 1] = sm[0];
+    }
+}
+
+static void log_residual(Sim* s, int pn_iter, int n_free, double Eprev, double L2)
+{
+    double* part = s->red.p;
+    k_resmag<<<64, 256, 0, s->stream>>>(s->nv, s->dir.p, part);
+    double h[128];
+    cudaMemcpyAsync(h, part, sizeof(h), cudaMemcpyDeviceToHost, s->stream);
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess) return;
+    double avg = 0, mx = 0;
+    for (int b = 0; b < 64; ++b) {
+        avg += h[2 * b];
+        mx = std::max(mx, h[2 * b + 1]);
+    }
+    avg /= n_free;
+    const double hh = s->prm.h;
+    log_line(s, "residual.txt", "%d %le %le %le %le\n", pn_iter, avg / hh, mx / hh, Eprev, L2);
+}
+
+static void log_step(Sim* s, const StepStats& S, bool with_collision)
+{
+    if (with_collision)
+        log_line(s, "counter.txt", "%d %lu\n", S.newton_iters, (unsigned long)S.n_constraints);
+    else
+        log_line(s, "counter.txt", "%d\n", S.newton_iters);
+    log_line(s, "steps.jsonl",
+             "{\"step\": %d, \"newton_iters\": %d, \"pcg_iters\": %d, \"line_search_trials\": %d, "
+             "\"n_constraints\": %d, \"status\": %d, \"min_dist2\": %.17g, \"kappa\": %.17g, \"ms\": %.3f, "
+             "\"precond_fallbacks\": %d, \"learned_solves\": %d}\n",
+             s->step_count, S.newton_iters, S.pcg_iters, S.line_search_trials, S.n_constraints, S.status, S.min_dist2,
+             S.kappa, S.ms, S.precond_fallbacks, S.learned_solves);
+}
+
+// 1 in *flag when some entry is NaN or infinite
+__global__ void k_nonfinite(int n, const double* a, unsigned long long* flag)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (!isfinite(a[i])) {
+            *flag = 1;
+            return;
+        }
+}
+
+static int check_finite_state(Sim* s)
+{
+    unsigned long long* flag = s->cnt.p + 33;
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(unsigned long long), s->stream);
+    const int n3 = 3 * s->nv;
+    if (e == cudaSuccess) {
+        k_nonfinite<<<nblk(n3, 256) < 304 ? nblk(n3, 256) : 304, 256, 0, s->stream>>>(n3, s->x.p, flag);
+        k_nonfinite<<<nblk(n3, 256) < 304 ? nblk(n3, 256) : 304, 256, 0, s->stream>>>(n3, s->v.p, flag);
+        e = cudaGetLastError();
+    }
+    unsigned long long hf = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hf, flag, sizeof(hf), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return set_cuda_error(e, "state check");
+    return hf ? set_error(CIPC_ERR_NAN, "the state holds a NaN or infinite position or velocity") : CIPC_OK;
+}
+
 static void save_prev(Sim* s, const double* x)
 {
     s->npcon = s->ncon;
@@ -210,6 +313,13 @@ int sim_step(Sim* s, StepStats* st)
         ph[k] += std::chrono::duration<double, std::milli>(now - tmark).count();
         tmark = now;
     };
+    // a non-finite position or velocity would propagate silently through every
+    // kernel; the step refuses it up front
+    if ((rc = check_finite_state(s))) {
+        S.status = -5;
+        *st = S;
+        return rc;
+    }
     cudaMemcpyAsync(s->xn.p, s->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
     launch_xtilde(s);
     // Dirichlet step (IMPLICIT_EULER.h:304-401): move the Dirichlet vertices to
@@ -250,6 +360,18 @@ int sim_step(Sim* s, StepStats* st)
     double Eprev;
     bool ok;
     if ((rc = eval_energy(s, s->x.p, &Eprev, &ok))) return rc;
+    // the reference exits where a constraint's d^2 - xi^2 is not positive
+    // (IPC.h:773-776); a start state inside the offset cannot be stepped from
+    if (!ok) {
+        S.status = -4;
+        *st = S;
+        return set_error(CIPC_ERR_NONPOSITIVE_DISTANCE, "the step's start state has a contact at or inside the offset");
+    }
+    if (!std::isfinite(Eprev)) {
+        S.status = -5;
+        *st = S;
+        return set_error(CIPC_ERR_NAN, "the incremental potential at the step's start is not finite");
+    }
     mark(3);
     std::deque<double> res;
     int fricIterI = 0, it = 0;
@@ -294,6 +416,7 @@ int sim_step(Sim* s, StepStats* st)
             const int lr = linear_solve(s, s->rhs.p, s->dir.p, &pit);
             s->solve_tol = 0;
             S.pcg_iters += pit;
+            if (lr == CIPC_ERR_NAN && !s->out_dir.empty()) log_line(s, "Hessian_info.txt", "Hessian not SPD in PNIter%d\n", it);
             if (lr == CIPC_ERR_NAN) {
                 useGD = true;
                 cudaMemcpyAsync(s->dir.p, s->rhs.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
@@ -383,6 +506,7 @@ int sim_step(Sim* s, StepStats* st)
         // convergence (IMPLICIT_EULER.h:647-710)
         L2 = std::sqrt(sum_sq(s, s->dir.p, n3) / (nv - nd)) / P.h;
         ++it;
+        if (!s->out_dir.empty()) log_residual(s, it, nv - nd, Eprev, L2);
         res.push_back(L2);
         if (res.size() > 3) res.pop_front();
         const double cur = L2;
@@ -446,6 +570,7 @@ int sim_step(Sim* s, StepStats* st)
                      "cipc step: %.2f ms  setup %.2f  sets %.2f  fbasis %.2f  energy %.2f  gradhess %.2f  solve %.2f  "
                      "ccd %.2f  other %.2f  (newton %d pcg %d)\n",
                      S.ms, ph[0], ph[1], ph[2], ph[3], ph[4], ph[5], ph[6], ph[7], it, S.pcg_iters);
+    if (!s->out_dir.empty()) log_step(s, S, P.withCollision != 0);
     *st = S;
     return rc;
 }
@@ -469,6 +594,10 @@ int sim_step_split(Sim* s, StepStats* st)
     const int nv = s->nv, n3 = 3 * nv, nd = (int)s->dbc_idx_h.size();
     cudaStream_t str = s->stream;
     int rc = CIPC_OK;
+    if ((rc = check_finite_state(s))) {
+        st->status = -5;
+        return rc;
+    }
     if (s->xsplit.alloc(n3) != cudaSuccess) return set_error(CIPC_ERR_CUDA, "split stepper buffer");
     cudaMemcpyAsync(s->xsplit.p, s->x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, str);
     // elastodynamic substep: no contact, no strain limiting
@@ -599,6 +728,7 @@ int sim_step_split(Sim* s, StepStats* st)
         Eprev = E;
         L2 = std::sqrt(sum_sq(s, s->dir.p, n3) / (nv - nd)) / P.h;
         ++it;
+        if (!s->out_dir.empty()) log_residual(s, it, nv - nd, Eprev, L2);
         res.push_back(L2);
         if (res.size() > 3) res.pop_front();
         L2 = *std::max_element(res.begin(), res.end());
@@ -633,6 +763,7 @@ int sim_step_split(Sim* s, StepStats* st)
     S.ms = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
     S.precond_fallbacks = s->solve_fallbacks;
     S.learned_solves = s->solve_learned;
+    if (!s->out_dir.empty()) log_step(s, S, P.withCollision != 0);
     *st = S;
     return rc;
 }
@@ -893,6 +1024,8 @@ static void to_params(const cipc_step_params* p, SimParams& q)
     // elastic IPC (Advance_One_Step_IE_Hinge_EIPC): no offset anywhere
     // (IPC.h:49-51, 752-754, FRICTION.h:28-30)
     q.elastic = p->barrier_model == CIPC_BARRIER_ELASTIC;
+    q.accd_max_iter = p->accd_max_iters > 0 ? p->accd_max_iters : (1 << 20);
+    q.pcg_wait_polls = p->pcg_wait_polls > 0 ? p->pcg_wait_polls : 0;
     if (q.elastic) q.xi = 0;
 }
 
@@ -907,6 +1040,7 @@ static int step_entry(cipc_sim* h, const cipc_step_params* p, cipc_step_stats* s
     to_params(p, s->prm);
     if (old_prec != s->prm.precision) s->hval.alloc(9 * sizeof(double) * (size_t)s->nnzb);
     StepStats S;
+    ++s->step_count;
     const int rc = split ? sim_step_split(s, &S) : sim_step(s, &S);
     if (stats) {
         stats->newton_iters = S.newton_iters;

@@ -35,6 +35,7 @@ extern "C" {
 #define CIPC_ERR_NAN 6
 #define CIPC_ERR_NO_DEVICE 7
 #define CIPC_ERR_INDEX_RANGE 8
+#define CIPC_ERR_TIMEOUT 9 /* a bounded device-side wait gave up (the kernel returned, the context is usable) */
 
 /* CIPC_PRECISION_FP64: every value that reaches a result is FP64; decisions and
  * results are bit-identical to the CPU restatement.  Distance-type decisions are
@@ -182,6 +183,12 @@ typedef struct cipc_step_params {
     int barrier_model;     /* CIPC_BARRIER_OFFSET (0, Advance_One_Step_IE_Hinge) or
                               CIPC_BARRIER_ELASTIC (1, Advance_One_Step_IE_Hinge_EIPC:
                               no offset, normalised barrier, kappa not adapted) */
+    int accd_max_iters;    /* ACCD steps per candidate pair in the step-size search (0 = 2^20);
+                              a pair that reaches it ends the step with CIPC_ERR_ITER_CAP
+                              (the reference's CCD loop has no bound, CCD.h:279-483) */
+    int pcg_wait_polls;    /* polls of a grid-wide wait inside the PCG kernel before it gives
+                              up (0 = 2^22, over a second); giving up ends the linear solve,
+                              and the step, with CIPC_ERR_TIMEOUT */
 } cipc_step_params;
 
 typedef struct cipc_step_stats {
@@ -284,6 +291,26 @@ int cipc_sim_get_dbc(cipc_sim* sim, int cap, int* idx, double* targets, int* cou
 /* Writes the current positions and the shell triangles as an OBJ file in the
  * reference's format (Write_TriMesh_Obj, Library/Utils/MESHIO.h:182-213). */
 int cipc_sim_write_obj(cipc_sim* sim, const char* path);
+/* Run logs in the reference's formats, appended in `folder` during steps
+ * (Advance_One_Step_IE_Hinge's outputFolder argument): residual.txt, one line
+ * "PNIter avgResMag maxRes Eprev L2Norm" per Newton iteration
+ * (IMPLICIT_EULER.h:647-670); counter.txt, "PNIter #constraints" per step
+ * (:868-875); Hessian_info.txt when a Newton system could not be solved
+ * (:531-534); steps.jsonl, one JSON object of cipc_step_stats per step.
+ * NULL or "" turns logging off (the default). */
+int cipc_sim_set_output(cipc_sim* sim, const char* folder);
+/* Checkpoint of a run: positions and velocities (bit for bit), the barrier
+ * stiffness and its maximum (kappaVec, kept across steps by the reference only
+ * in memory, IMPLICIT_EULER.h:578-580), the strain-limit stiffness and the step
+ * count.  load checks the vertex count; the mesh, materials and Dirichlet setup
+ * come from the simulation it is loaded into. */
+int cipc_sim_save_state(cipc_sim* sim, const char* path);
+int cipc_sim_load_state(cipc_sim* sim, const char* path);
+/* The reference drivers' restart (load_frame + load_velocity,
+ * Python/Drivers/FEMDiscreteShellBase.py:244-253; Load_Velocity,
+ * Library/Utils/MESHIO.h:967-984): positions from the vertex lines of obj_last,
+ * velocities (obj_last - obj_prev) / dt, or zero when obj_prev is NULL. */
+int cipc_sim_load_obj_frames(cipc_sim* sim, const char* obj_prev, const char* obj_last, double dt);
 /* One time step; replaces Advance_One_Step_IE_Hinge (IMPLICIT_EULER.h:151-902).
  * Returns CIPC_OK, or CIPC_ERR_NOT_CONVERGED when the Newton cap is reached or
  * the Dirichlet motion is blocked by contact (stats->status -1 / -2). */

@@ -1,0 +1,124 @@
+"""Parity on the benchmark's own scene configurations, through the C ABI.
+
+Config "cloth on cube": a 40x40 StVK cloth (1 m, E 1e5, nu 0.3, rho 200,
+t 1 mm) falling from 0.1 m onto a fixed 0.3 m cube shell, xi = dhat = 1 mm,
+dt 0.04, Newton tolerance 1e-2, all 50 steps on the GPU (FP64).  At every one
+of the 51 states:
+  * the constraint set equals the oracle's as a set (kind, vertices, multiplicity);
+  * the intersection-free step size along the step actually taken (x_{k+1} - x_k,
+    and three times it) is bit-identical to the oracle's;
+and from three of the states, one time step by the oracle's direct-solve Newton
+(tolerance 1e-2) and by the GPU for the same number of Newton iterations agree
+within 1e-8 of the bounding-box diagonal.
+
+Config "cloth on rotating sphere": a 200x200 cloth (2 m) draped over a sphere
+(r 0.5 m) turning at 2 rad/s, xi 0.5 mm, dhat 1 mm, mu 0.4, dt 0.02, 12 steps on
+the GPU (mixed precision, as the benchmark runs it); the constraint sets at 4 of
+the draped states equal the oracle's as sets.
+"""
+import numpy as np
+import pytest
+
+import cipc_ffi as F
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _rows(c):
+    return sorted(map(tuple, c.tolist()))
+
+
+@pytest.fixture(scope="module")
+def cube_run(cuda):
+    X, T, dbc = W.cloth_on_box(n=40)
+    s = F.Sim(X, T, 200.0, 1e5, 0.3, 1e-3, nh=False)
+    k2, dhat2 = s.init_oipc(1e-3)
+    prm = F.make_params(0.04, dhat2, 1e-3, newton_tol=1e-2, precision=F.FP64, pcg_tol=1e-6)
+    states, vels, kappas = [X.copy()], [np.zeros_like(X)], [s.kappa().copy()]
+    for _ in range(50):
+        s.set_dbc(dbc, X[dbc])
+        st = s.step(prm, allow=(F.CIPC_ERR_NOT_CONVERGED,))
+        assert st.min_dist2 > 0 or st.n_constraints == 0
+        x, v = s.state()
+        states.append(x)
+        vels.append(v)
+        kappas.append(s.kappa().copy())
+    return dict(X=X, T=T, dbc=dbc, sim=s, prm=prm, dhat2=dhat2, states=states, vels=vels, kappas=kappas)
+
+
+def test_cube_constraint_sets_every_state(cube_run, orc):
+    r = cube_run
+    sh = orc.Shell(r["X"], r["T"], 200.0, 1e5, 0.3, 1e-3, nh=False)
+    sh.dbc = r["dbc"]
+    total = 0
+    for k, x in enumerate(r["states"]):
+        go = _rows(sh.constraints(x, r["dhat2"], 1e-3))
+        gg = _rows(r["sim"].constraints(r["prm"], x))
+        assert gg == go, k
+        total += len(go)
+    assert total > 1000  # the cloth lands on the cube and drapes over its edges
+
+
+def test_cube_step_sizes_bit_identical(cube_run, orc):
+    r = cube_run
+    sh = orc.Shell(r["X"], r["T"], 200.0, 1e5, 0.3, 1e-3, nh=False)
+    sh.dbc = r["dbc"]
+    limited = 0
+    for k in range(len(r["states"]) - 1):
+        x = r["states"][k]
+        for scale in (1.0, 3.0):
+            d = scale * (r["states"][k + 1] - x)
+            d[r["dbc"]] = 0
+            ag = r["sim"].ccd(r["prm"], x, d, 1.0)
+            ao = sh.ccd(x, d, 1.0, 1e-3)
+            assert np.float64(ag).view(np.uint64) == np.float64(ao).view(np.uint64), (k, scale, ag, ao)
+            limited += ao < 1.0
+    assert limited > 0  # some steps are cut by CCD
+
+
+@pytest.mark.parametrize("k", [3, 20, 45])
+def test_cube_single_step_positions(cube_run, orc, k):
+    r = cube_run
+    X, dbc = r["X"], r["dbc"]
+    sh = orc.Shell(X, r["T"], 200.0, 1e5, 0.3, 1e-3, nh=False)
+    x, v, k2 = r["states"][k].copy(), r["vels"][k].copy(), r["kappas"][k].copy()
+    rc, sto = sh.step(x, v, k2, dbc, X[dbc], 0.04, r["dhat2"], 1e-3, tol=1e-2, max_iter=400)
+    assert rc == 0
+    s = r["sim"]
+    s.set_state(r["states"][k], r["vels"][k])
+    s.set_kappa(r["kappas"][k][0], r["kappas"][k][1])
+    s.set_dbc(dbc, X[dbc])
+    prm = F.make_params(0.04, r["dhat2"], 1e-3, newton_tol=1e-30, precision=F.FP64, pcg_tol=1e-12,
+                        max_newton_iters=sto["newton_iters"])
+    st = s.step(prm, allow=(F.CIPC_ERR_NOT_CONVERGED,))
+    assert st.newton_iters == sto["newton_iters"]
+    xg, _ = s.state()
+    diag = np.linalg.norm(X.max(0) - X.min(0))
+    err = np.abs(xg - x).max()
+    assert err <= 1e-8 * diag, (k, err / diag, sto, st.as_dict())
+
+
+def test_sphere_constraint_sets_draped_states(cuda, orc):
+    X, T, dbc, c = W.cloth_on_sphere(n=200)
+    s = F.Sim(X, T, 200.0, 1e5, 0.3, 1e-3)
+    _, dhat2 = s.init_oipc(1e-3)
+    prm = F.make_params(0.02, dhat2, 5e-4, mu=0.4, epsv2=1e-6, fric_iters=1, newton_tol=1e-3, precision=F.MIXED,
+                        pcg_tol=1e-4)
+    sh = orc.Shell(X, T, 200.0, 1e5, 0.3, 1e-3)
+    sh.dbc = dbc
+    compared = 0
+    for k in range(12):
+        tg = W.rotate_y(X[dbc], c, 2.0 * 0.02 * (k + 1))
+        s.set_dbc(dbc, tg)
+        st = s.step(prm, allow=(F.CIPC_ERR_NOT_CONVERGED,))
+        assert st.min_dist2 > 0 or st.n_constraints == 0
+        if k in (5, 8, 10, 11):
+            x, _ = s.state()
+            go = _rows(sh.constraints(x, dhat2, 5e-4))
+            gg = _rows(s.constraints(prm, x))
+            assert len(go) > 1000
+            assert gg == go, k
+            compared += 1
+    s.close()
+    assert compared == 4
