@@ -313,6 +313,9 @@ static void shell_init(Shell& S, int nv, const double* X, int nt, const int* tri
     S.bnode.clear();
     for (int i = 0; i < nv; ++i)
         if (isb[i]) S.bnode.push_back(i);
+    // no rod nodes or particles until codim_init adds them after the shell nodes
+    // (the codimensional contact loops start at these indices)
+    S.codim0 = S.codim1 = (int)S.bnode.size();
     // rest first fundamental form, stored inverted (P)
     S.P.resize(3 * nt);
     S.vol.resize(nt);

@@ -78,9 +78,14 @@ def test_start_inside_offset_reported(cuda):
 
 
 def test_accd_iteration_cap_reported(cuda):
-    X, T, dbc = _scene(-0.0985)  # 1.5 mm above the box top: CCD candidates at once
+    # 3 mm above the box top, falling at 0.5 m/s: the first Newton step heads into
+    # the box, so the step-size search meets candidate pairs that need several
+    # ACCD steps
+    X, T, dbc = _scene(-0.097)
     s, dhat2 = _sim(X, T, dbc)
-    s.set_state(X, np.zeros_like(X))
+    v = np.zeros_like(X)
+    v[:64, 1] = -0.5
+    s.set_state(X, v)
     with pytest.raises(F.CipcError) as ei:
         s.step(F.make_params(DT, dhat2, XI, accd_max_iters=1))
     assert ei.value.status == F.CIPC_ERR_ITER_CAP
