@@ -619,3 +619,25 @@ def sim_load_state(sim, path):
 
 def sim_load_obj_frames(sim, obj_prev, obj_last, dt):
     _check(lib().cipc_sim_load_obj_frames(sim.h, _enc(obj_prev), _enc(obj_last), float(dt)))
+
+
+_SIGS["cipc_scene_oipc_kappa"] = (_c_int, [_c_int, _vp, _c_int, _vp, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _vp, _c_dbl,
+                                           _c_int, _vp, _vp, _c_dbl, _c_dbl, _vp, _vp])
+if _lib is not None:
+    _lib.cipc_scene_oipc_kappa.restype, _lib.cipc_scene_oipc_kappa.argtypes = _SIGS["cipc_scene_oipc_kappa"]
+
+
+def scene_oipc_kappa(X, T, rho, E, nu, thickness, gravity, codim_desc, dhat, stiff_mult=1.0, bend_stiff_mult=1.0,
+                     nh=True):
+    """Offset-IPC stiffness (kappa, kappa_max) and dhat^2 of a scene description,
+    computed on the host without a device (cipc_scene_oipc_kappa)."""
+    X = np.ascontiguousarray(X, np.float64).reshape(-1, 3)
+    T = np.ascontiguousarray(T, np.int32).reshape(-1, 3)
+    g = np.ascontiguousarray(gravity, np.float64).reshape(3)
+    k2 = np.zeros(2)
+    d2 = ctypes.c_double()
+    _check(lib().cipc_scene_oipc_kappa(X.shape[0], X.ctypes.data, T.shape[0], T.ctypes.data if T.size else None, rho, E,
+                                       nu, thickness, g.ctypes.data, bend_stiff_mult, 1 if nh else 0,
+                                       ctypes.byref(codim_desc) if codim_desc is not None else None, None, dhat,
+                                       stiff_mult, k2.ctypes.data, ctypes.byref(d2)))
+    return k2, d2.value

@@ -902,6 +902,42 @@ extern "C" int cipc_sim_init_oipc(cipc_sim* h, double dhat, double stiff_mult, d
     return CIPC_OK;
 }
 
+extern "C" int cipc_scene_oipc_kappa(int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
+                                     double thickness, const double* gravity, double bend_stiff_mult,
+                                     int membrane_model, const cipc_codim_desc* codim, const cipc_tet_desc* tets,
+                                     double dhat, double stiff_mult, double* kappa2, double* dhat2)
+{
+    if (!gravity || !kappa2) return set_error(CIPC_ERR_INVALID_ARG, "cipc_scene_oipc_kappa: null argument");
+    CodimDesc cd;
+    if (codim) {
+        cd.nseg = codim->n_segments;
+        cd.seg = codim->segments;
+        cd.rod_E = codim->rod_E;
+        cd.rod_rho = codim->rod_rho;
+        cd.rod_thickness = codim->rod_thickness;
+        cd.rod_bend_mult = codim->rod_bend_mult;
+        cd.npart = codim->n_particles;
+        cd.part = codim->particles;
+        cd.part_rho = codim->particle_rho;
+        cd.part_thickness = codim->particle_thickness;
+    }
+    TetDesc td;
+    if (tets) {
+        td.ntet = tets->n_tets;
+        td.tet = tets->tets;
+        td.E = tets->E;
+        td.nu = tets->nu;
+        td.rho = tets->rho;
+    }
+    HostScene S;  // host only: no device is touched
+    int rc = build_host_scene(S, nv, X, nt, tri, rho, E, nu, thickness, gravity, bend_stiff_mult, membrane_model,
+                              codim ? &cd : nullptr, tets ? &td : nullptr);
+    if (rc) return rc;
+    const double d2 = oipc_kappa(S.mass, dhat, stiff_mult, kappa2);
+    if (dhat2) *dhat2 = d2;
+    return CIPC_OK;
+}
+
 extern "C" int cipc_sim_init_eipc(cipc_sim* h, double E, double nu, double thickness, double dt, double* kappa3,
                                   double* dhat2)
 {

@@ -251,6 +251,14 @@ int cipc_sim_destroy(cipc_sim* sim);
 /* Offset-IPC barrier stiffness; replaces FEM.DiscreteShell.Initialize_OIPC
  * (DISCRETE_SHELL.h:555-577, export :1103).  Writes (kappa, kappa_max) and dhat^2. */
 int cipc_sim_init_oipc(cipc_sim* sim, double dhat, double stiff_mult, double* kappa2, double* dhat2);
+/* The same stiffness from a scene description alone (the arguments of
+ * cipc_sim_create_full), computed on the host with no device: what
+ * FEM.DiscreteShell.Initialize_OIPC returns at set-up time, before a simulation
+ * exists on the GPU. */
+int cipc_scene_oipc_kappa(int nv, const double* X, int nt, const int* tri, double rho, double E, double nu,
+                          double thickness, const double* gravity, double bend_stiff_mult, int membrane_model,
+                          const cipc_codim_desc* codim, const cipc_tet_desc* tets, double dhat, double stiff_mult,
+                          double* kappa2, double* dhat2);
 /* Elastic-IPC stiffness; replaces FEM.DiscreteShell.Initialize_EIPC
  * (DISCRETE_SHELL.h:555-577, export :1102): kappa3 = (h^2 mu, h^2 lambda, nu) of the
  * plane-stress material, dhat^2 = thickness^2; sets the simulation's kappa. */
