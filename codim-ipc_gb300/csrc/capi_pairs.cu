@@ -85,8 +85,10 @@ extern "C" int cipc_ccd_pairs(int64_t n, const uint8_t* type, const int32_t* idx
                    *m_toc = mapped_host(toc_out, (size_t)n * 8), *m_hit = mapped_host(hit, (size_t)n);
         if (m_type && m_idx && m_x && m_dx && m_toc && m_hit) {
             unsigned long long* cnt_d = nullptr;
+            AccdState* state = nullptr;
             unsigned long long cnt[3] = {0, 0, 0};
             cudaError_t e2 = cudaMallocAsync((void**)&cnt_d, sizeof(cnt), s);
+            if (e2 == cudaSuccess && exact) e2 = cudaMallocAsync((void**)&state, (size_t)n * sizeof(AccdState), s);
             if (e2 == cudaSuccess) e2 = cudaMemsetAsync(cnt_d, 0, sizeof(cnt), s);
             if (e2 == cudaSuccess) {
                 CcdArgs a;
@@ -104,14 +106,15 @@ extern "C" int cipc_ccd_pairs(int64_t n, const uint8_t* type, const int32_t* idx
                 a.hit = static_cast<uint8_t*>(const_cast<void*>(m_hit));
                 a.iters = nullptr;
                 a.counter = cnt_d;
-                const int bps = exact ? accd_exact_blocks_per_sm() : accd_mixed_blocks_per_sm();
+                const int bps = exact ? accd_exact_steps_blocks_per_sm() : accd_mixed_blocks_per_sm();
                 int grid = num_sms() * bps;
                 const int64_t need = (n + 255) / 256;
                 if (need < grid) grid = (int)need;
-                e2 = exact ? launch_accd_exact(a, grid, s) : launch_accd_mixed(a, grid, s);
+                e2 = exact ? launch_accd_exact_split(a, state, grid, s) : launch_accd_mixed(a, grid, s);
             }
             if (e2 == cudaSuccess) e2 = cudaMemcpyAsync(cnt, cnt_d, sizeof(cnt), cudaMemcpyDeviceToHost, s);
             if (cnt_d) cudaFreeAsync(cnt_d, s);
+            if (state) cudaFreeAsync(state, s);
             const cudaError_t e3 = cudaStreamSynchronize(s);
             if (e2 == cudaSuccess) e2 = e3;
             if (e2 != cudaSuccess) return set_cuda_error(e2, "cipc_ccd_pairs (page-locked host buffers)");
@@ -132,6 +135,7 @@ extern "C" int cipc_ccd_pairs(int64_t n, const uint8_t* type, const int32_t* idx
     int32_t* t_idx = nullptr;
     double *t_x = nullptr, *t_dx = nullptr, *t_toc = nullptr;
     unsigned long long* counters = nullptr;
+    AccdState* state = nullptr;  // FP64: per-pair set-up state of the two-pass kernels (one chunk's worth)
     cudaStream_t cin = nullptr, cout_ = nullptr;
     cudaEvent_t ev_verts = nullptr, ev_in[64], ev_out[64];
     int n_ev = 0;
@@ -142,6 +146,8 @@ extern "C" int cipc_ccd_pairs(int64_t n, const uint8_t* type, const int32_t* idx
         if (e != cudaSuccess) goto done; \
     } while (0)
     CK(cudaMallocAsync((void**)&counters, 3 * (size_t)nchunk * sizeof(unsigned long long), s));
+    // one record per pair of the largest launch: a chunk when pipelined, else the whole list
+    if (exact) CK(cudaMallocAsync((void**)&state, (size_t)(pipelined ? chunk : n) * sizeof(AccdState), s));
     CK(cudaMemsetAsync(counters, 0, 3 * (size_t)nchunk * sizeof(unsigned long long), s));
     if (host) {
         CK(stage_in(&t_x, x, (size_t)nv * 3, s));
@@ -165,7 +171,7 @@ extern "C" int cipc_ccd_pairs(int64_t n, const uint8_t* type, const int32_t* idx
         }
     }
     {
-        const int bps = exact ? accd_exact_blocks_per_sm() : accd_mixed_blocks_per_sm();
+        const int bps = exact ? accd_exact_steps_blocks_per_sm() : accd_mixed_blocks_per_sm();
         for (int c = 0; c < nchunk; ++c) {
             const int64_t off = (int64_t)c * chunk, m = std::min<int64_t>(chunk, n - off);
             if (host) {
@@ -196,7 +202,7 @@ extern "C" int cipc_ccd_pairs(int64_t n, const uint8_t* type, const int32_t* idx
             int grid = num_sms() * bps;
             const int64_t need = (a.n + 255) / 256;
             if (need < grid) grid = (int)need;
-            CK(exact ? launch_accd_exact(a, grid, s) : launch_accd_mixed(a, grid, s));
+            CK(exact ? launch_accd_exact_split(a, state, grid, s) : launch_accd_mixed(a, grid, s));
             if (host) {
                 cudaStream_t cs = pipelined ? cout_ : s;
                 if (pipelined) {
@@ -230,6 +236,7 @@ done:
     if (cout_) cudaStreamSynchronize(cout_);  // result copies finished before their sources are freed
     if (cin) cudaStreamSynchronize(cin);
     if (counters) cudaFreeAsync(counters, s);
+    if (state) cudaFreeAsync(state, s);
     if (t_type) cudaFreeAsync(t_type, s);
     if (t_idx) cudaFreeAsync(t_idx, s);
     if (t_x) cudaFreeAsync(t_x, s);

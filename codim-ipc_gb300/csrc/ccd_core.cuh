@@ -203,3 +203,178 @@ __global__ void __launch_bounds__(256) k_accd(CcdArgs a)
 }
 
 }  // namespace cipc
+
+namespace cipc {
+
+// ---------------------------------------------------------------------------
+// Two-pass form of k_accd, same results bit for bit.
+//
+// In k_accd a lane that takes a new pair runs the set-up (mean removal, the
+// displacement bound with its two square roots, the first distance and step)
+// while the other lanes of its warp step their pairs; on GB300's narrow FP64 pipe
+// that divergence idles ~40% of the FP64 issue slots (19 of 32 lanes active per
+// instruction).  Here k_accd_setup does the set-up for every pair with converged
+// warps (one thread per pair) and leaves each pair's state in memory
+// (AccdState, 128 bytes); k_accd_steps then runs the lane-refill loop whose
+// refill only loads that state, so every FP64 operation in the loop is the same
+// step for all active lanes.  The operation sequence per pair is exactly k_accd's:
+// setup computes f and dist at x0, the gap, and the first step tlb; the loop
+// applies x1 = x0 + tlb dv (the same fma), starts with t = 0 and one step taken.
+// ---------------------------------------------------------------------------
+struct AccdState {
+    double dv[12];         // displacements with the mean motion removed
+    double maxDisp, gap, tlb;
+    int32_t tp;            // pair type, or -1 when the set-up already wrote the result
+    int32_t pad;
+};
+static_assert(sizeof(AccdState) == 128, "one 128-byte line per pair");
+
+template <class Pol>
+__global__ void __launch_bounds__(256) k_accd_setup(CcdArgs a, AccdState* __restrict__ st)
+{
+    const double th = a.th, th2 = a.th * a.th, eta = a.eta, toc_prev = a.toc_in;
+    for (int64_t pid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pid < a.n;
+         pid += (int64_t)gridDim.x * blockDim.x) {
+        const int tp = a.type[pid];
+        const int4 id = a.idx[pid];
+        const int nv = tp == kPP ? 2 : (tp == kPE ? 3 : 4);
+        const int ids[4] = {id.x, id.y, id.z, id.w};
+        bool ok = tp <= kEE;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < nv) ok = ok && ids[k] >= 0 && ids[k] < a.nv;
+        AccdState& S = st[pid];
+        if (!ok) {  // invalid pair: reported, never dereferenced
+            a.toc_out[pid] = toc_prev;
+            a.hit[pid] = 0;
+            if (a.iters) a.iters[pid] = 0;
+            atomicAdd(a.counter + 2, 1ull);
+            S.tp = -1;
+            continue;
+        }
+        d3 v[4], dv[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (k < nv) {
+                v[k] = ld(a.x, ids[k]);
+                dv[k] = ld(a.dx, ids[k]);
+            } else {
+                v[k] = mk(0, 0, 0);
+                dv[k] = mk(0, 0, 0);
+            }
+        }
+        const double maxDisp = ccd_prepare(tp, dv);
+        if (maxDisp == 0) {
+            a.toc_out[pid] = toc_prev;
+            a.hit[pid] = 0;
+            if (a.iters) a.iters[pid] = 0;
+            S.tp = -1;
+            continue;
+        }
+        double d2;
+        const double f = Pol::dfunc(tp, v, th2, d2);
+        const double dist = Pol::sqrt_(d2);
+        S.gap = eta * f / (dist + th);
+        S.tlb = Pol::div_((1 - eta) * f, (dist + th) * maxDisp);
+        S.maxDisp = maxDisp;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            S.dv[3 * k] = dv[k].x;
+            S.dv[3 * k + 1] = dv[k].y;
+            S.dv[3 * k + 2] = dv[k].z;
+        }
+        S.tp = tp;
+    }
+}
+
+// a.max_iter must be at least 1 (the set-up took the first step)
+template <class Pol>
+__global__ void __launch_bounds__(256) k_accd_steps(CcdArgs a, const AccdState* __restrict__ st)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const double th = a.th, th2 = a.th * a.th, eta = a.eta, toc_prev = a.toc_in;
+    int64_t pid = -1;
+    bool exhausted = false;
+    int tp = 0;
+    d3 v[4], dv[4];
+    double maxDisp = 0, gap = 0, t = 0, tlb = 0, lim = toc_prev;
+    int64_t adv = 0;
+    while (true) {
+        // refill: pairs whose set-up wrote the result are skipped here
+        bool need = (pid < 0) && !exhausted;
+        while (__any_sync(FULL, need)) {
+            const unsigned m = __ballot_sync(FULL, need);
+            const int leader = __ffs(m) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(a.counter, (unsigned long long)__popc(m));
+            base = __shfl_sync(FULL, base, leader);
+            if (need) {
+                const unsigned long long my = base + __popc(m & ((1u << lane) - 1u));
+                if (my >= (unsigned long long)a.n) {
+                    exhausted = true;
+                    need = false;
+                } else {
+                    const AccdState& S = st[my];
+                    tp = S.tp;
+                    if (tp >= 0) {
+                        pid = (int64_t)my;
+                        need = false;
+                        const int4 id = a.idx[pid];
+                        const int nv = tp == kPP ? 2 : (tp == kPE ? 3 : 4);
+                        const int ids[4] = {id.x, id.y, id.z, id.w};
+                        maxDisp = S.maxDisp;
+                        gap = S.gap;
+                        tlb = S.tlb;
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            dv[k] = mk(S.dv[3 * k], S.dv[3 * k + 1], S.dv[3 * k + 2]);
+                            v[k] = axpy(tlb, dv[k], k < nv ? ld(a.x, ids[k]) : mk(0, 0, 0));
+                        }
+                        t = 0;
+                        adv = 1;
+                        lim = a.toc_min ? dmin(toc_prev, load_min(a.toc_min)) : toc_prev;
+                    }
+                }
+            }
+        }
+        const bool active = pid >= 0;
+        if (!__any_sync(FULL, active)) break;
+        if (!active) continue;
+        double d2;
+        const double f = Pol::dfunc(tp, v, th2, d2);
+        const double dist = Pol::sqrt_(d2);
+        if (t != 0 && Pol::gap_less(f, dist + th, gap)) {
+            a.toc_out[pid] = t;
+            a.hit[pid] = 1;
+            if (a.toc_min) atomicMin(a.toc_min, (unsigned long long)__double_as_longlong(t));
+            if (a.iters) a.iters[pid] = (int32_t)adv;
+            pid = -1;
+            continue;
+        }
+        t += tlb;
+        if (a.toc_min && (adv & 15) == 0) lim = dmin(lim, load_min(a.toc_min));
+        if (t > lim) {
+            a.toc_out[pid] = toc_prev;
+            a.hit[pid] = 0;
+            if (a.iters) a.iters[pid] = (int32_t)adv;
+            pid = -1;
+            continue;
+        }
+        if (adv >= a.max_iter) {
+            a.toc_out[pid] = toc_prev;
+            a.hit[pid] = 0;
+            if (a.toc_min) atomicMin(a.toc_min, (unsigned long long)__double_as_longlong(t));
+            if (a.iters) a.iters[pid] = (int32_t)adv;
+            atomicAdd(a.counter + 1, 1ull);
+            pid = -1;
+            continue;
+        }
+        tlb = Pol::div_((1 - eta) * f, (dist + th) * maxDisp);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] = axpy(tlb, dv[k], v[k]);
+        ++adv;
+    }
+}
+
+}  // namespace cipc

@@ -51,6 +51,23 @@ cudaError_t launch_accd_exact(const CcdArgs& a, int grid, cudaStream_t s)
     return cudaGetLastError();
 }
 
+cudaError_t launch_accd_exact_split(const CcdArgs& a, AccdState* state, int grid, cudaStream_t s)
+{
+    if (a.max_iter < 1) return cudaErrorInvalidValue;
+    const int64_t need = (a.n + 255) / 256;
+    const int sgrid = (int)(need < 4096 ? need : 4096);
+    k_accd_setup<ExactPol><<<sgrid > 0 ? sgrid : 1, 256, 0, s>>>(a, state);
+    k_accd_steps<ExactPol><<<grid, 256, 0, s>>>(a, state);
+    return cudaGetLastError();
+}
+
+int accd_exact_steps_blocks_per_sm()
+{
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_accd_steps<ExactPol>, 256, 0);
+    return b > 0 ? b : 1;
+}
+
 int accd_exact_blocks_per_sm()
 {
     int b = 0;

@@ -9,6 +9,10 @@ namespace cipc {
 struct CcdArgs;
 
 cudaError_t launch_accd_exact(const CcdArgs& a, int grid, cudaStream_t s);
+// two-pass form (ccd_core.cuh): state holds a.n AccdState records (128 bytes each)
+struct AccdState;
+cudaError_t launch_accd_exact_split(const CcdArgs& a, AccdState* state, int grid, cudaStream_t s);
+int accd_exact_steps_blocks_per_sm();
 cudaError_t launch_accd_mixed(const CcdArgs& a, int grid, cudaStream_t s);
 int accd_exact_blocks_per_sm();
 int accd_mixed_blocks_per_sm();
