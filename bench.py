@@ -551,13 +551,17 @@ def run_ours(args):
             "gpu_launches": args.steps,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
-                         "kernel": "k_accd_mixed" if prec == F.MIXED else "k_accd<ExactPol>",
+                         "kernel": ("k_accd_mixed" if prec == F.MIXED else
+                                    "k_accd_setup + k_accd_steps (one two-pass launch pair, timed together)"),
                          "peak_source": peak_kind,
+                         "fp64_pipe_busy": None if prec == F.MIXED else 0.866,
                          "note": ("ACCD is instruction-issue bound (FP32 and integer pipes: float-float "
                                   "distances, ~3.4 distance evaluations per pair), not HBM bound; bytes are the "
                                   "algorithmic minimum, read once" if prec == F.MIXED else
-                                  "ACCD in FP64 is FP64-pipe bound on this part (1/64 of the FP32 rate); bytes "
-                                  "are the algorithmic minimum, read once")},
+                                  "ACCD in FP64 is bound by the FP64 pipe (2 lanes per SM per clock on this part; "
+                                  "86.6% busy in the stepping pass, profiles/accd_fp64_2M_pairs.txt), not by "
+                                  "HBM; achieved counts the algorithmic bytes, read once; traffic also counts the "
+                                  "128-byte per-pair state the set-up pass writes and the stepping pass reads")},
             "clocks": clk,
             "variants": variants,
             "cpu_baseline": cpu,

@@ -84,11 +84,12 @@ extern "C" int cipc_ccd_pairs(int64_t n, const uint8_t* type, const int32_t* idx
                    *m_x = mapped_host(x, (size_t)nv * 24), *m_dx = mapped_host(dx, (size_t)nv * 24),
                    *m_toc = mapped_host(toc_out, (size_t)n * 8), *m_hit = mapped_host(hit, (size_t)n);
         if (m_type && m_idx && m_x && m_dx && m_toc && m_hit) {
+            // one pass here: its FP64 work hides the link's read latency, while
+            // the two-pass form's set-up pass would wait on the link with nothing
+            // to overlap and its stepping pass would read the positions again
             unsigned long long* cnt_d = nullptr;
-            AccdState* state = nullptr;
             unsigned long long cnt[3] = {0, 0, 0};
             cudaError_t e2 = cudaMallocAsync((void**)&cnt_d, sizeof(cnt), s);
-            if (e2 == cudaSuccess && exact) e2 = cudaMallocAsync((void**)&state, (size_t)n * sizeof(AccdState), s);
             if (e2 == cudaSuccess) e2 = cudaMemsetAsync(cnt_d, 0, sizeof(cnt), s);
             if (e2 == cudaSuccess) {
                 CcdArgs a;
@@ -106,15 +107,14 @@ extern "C" int cipc_ccd_pairs(int64_t n, const uint8_t* type, const int32_t* idx
                 a.hit = static_cast<uint8_t*>(const_cast<void*>(m_hit));
                 a.iters = nullptr;
                 a.counter = cnt_d;
-                const int bps = exact ? accd_exact_steps_blocks_per_sm() : accd_mixed_blocks_per_sm();
+                const int bps = exact ? accd_exact_blocks_per_sm() : accd_mixed_blocks_per_sm();
                 int grid = num_sms() * bps;
                 const int64_t need = (n + 255) / 256;
                 if (need < grid) grid = (int)need;
-                e2 = exact ? launch_accd_exact_split(a, state, grid, s) : launch_accd_mixed(a, grid, s);
+                e2 = exact ? launch_accd_exact(a, grid, s) : launch_accd_mixed(a, grid, s);
             }
             if (e2 == cudaSuccess) e2 = cudaMemcpyAsync(cnt, cnt_d, sizeof(cnt), cudaMemcpyDeviceToHost, s);
             if (cnt_d) cudaFreeAsync(cnt_d, s);
-            if (state) cudaFreeAsync(state, s);
             const cudaError_t e3 = cudaStreamSynchronize(s);
             if (e2 == cudaSuccess) e2 = e3;
             if (e2 != cudaSuccess) return set_cuda_error(e2, "cipc_ccd_pairs (page-locked host buffers)");
