@@ -78,7 +78,8 @@ struct SimParams {
     int precond = 0;          // 0 block-Jacobi, 1 learned correction (when a model is loaded)
     int forcing = 0;          // 1: inexact Newton (Eisenstat-Walker forcing term)
     int elastic = 0;          // 1: elastic IPC (no offset, barrier scaled by 1/dhat^4, kappa fixed)
-    long long accd_max_iter = 1 << 20;  // ACCD steps per pair before the step reports CIPC_ERR_ITER_CAP
+    long long accd_max_iter = 1 << 20;  // ACCD steps per pair in the step-size search
+    int accd_cap_strict = 0;  // 1: a pair reaching accd_max_iter ends the step with CIPC_ERR_ITER_CAP
     int pcg_wait_polls = 0;   // PCG grid-wait poll limit (0: the solver's default, over a second)
 };
 

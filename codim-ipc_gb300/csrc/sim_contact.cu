@@ -1475,8 +1475,11 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return set_cuda_error(e, "ccd");
         *alpha_out = res;
-        // the reference's ACCD loops without bound there; here the step stops and says so
-        if (over)
+        // A pair at the cap has lowered the minimum to the time it safely advanced
+        // to, so the bound stays conservative; with a cap the caller set
+        // explicitly (cipc_step_params.accd_max_iters > 0) reaching it ends the
+        // step instead (the reference's ACCD loops without bound there)
+        if (over && s->prm.accd_cap_strict)
             return set_error(CIPC_ERR_ITER_CAP, "step size: %llu CCD pairs reached the cap of %lld ACCD steps", over,
                              s->prm.accd_max_iter);
         return CIPC_OK;

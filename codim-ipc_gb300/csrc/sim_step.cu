@@ -1062,6 +1062,7 @@ static void to_params(const cipc_step_params* p, SimParams& q)
     // (IPC.h:49-51, 752-754, FRICTION.h:28-30)
     q.elastic = p->barrier_model == CIPC_BARRIER_ELASTIC;
     q.accd_max_iter = p->accd_max_iters > 0 ? p->accd_max_iters : (1 << 20);
+    q.accd_cap_strict = p->accd_max_iters > 0;
     q.pcg_wait_polls = p->pcg_wait_polls > 0 ? p->pcg_wait_polls : 0;
     if (q.elastic) q.xi = 0;
 }

@@ -183,9 +183,12 @@ typedef struct cipc_step_params {
     int barrier_model;     /* CIPC_BARRIER_OFFSET (0, Advance_One_Step_IE_Hinge) or
                               CIPC_BARRIER_ELASTIC (1, Advance_One_Step_IE_Hinge_EIPC:
                               no offset, normalised barrier, kappa not adapted) */
-    int accd_max_iters;    /* ACCD steps per candidate pair in the step-size search (0 = 2^20);
-                              a pair that reaches it ends the step with CIPC_ERR_ITER_CAP
-                              (the reference's CCD loop has no bound, CCD.h:279-483) */
+    int accd_max_iters;    /* ACCD steps per candidate pair in the step-size search (the
+                              reference's CCD loop has no bound, CCD.h:279-483).  0: 2^20, and
+                              a pair that reaches it lowers the step to the time it has safely
+                              advanced to (a conservative bound; grazing, sliding contact can
+                              take that long).  > 0: that cap, and a pair that reaches it ends
+                              the step with CIPC_ERR_ITER_CAP */
     int pcg_wait_polls;    /* polls of a grid-wide wait inside the PCG kernel before it gives
                               up (0 = 2^22, over a second); giving up ends the linear solve,
                               and the step, with CIPC_ERR_TIMEOUT */
