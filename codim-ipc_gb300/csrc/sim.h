@@ -111,7 +111,6 @@ struct Sim {
     int trace = 0;    // CIPC_TRACE set: one stderr line per Newton iteration and refinement pass
     std::string out_dir;  // run logs (residual.txt, counter.txt, Hessian_info.txt, steps.jsonl) when set
     int step_count = 0;   // steps taken (successful or not) since creation or the last restore
-    bool have_dir = false;  // dir holds a finite Newton direction (the mixed solve warm-starts from it)
     // static device data
     DBuf<int> tri, hinge, bnode, bedge, btri;
     DBuf<double> P, vol, hinfo, mass, b, X0;

@@ -129,7 +129,6 @@ extern "C" int cipc_sim_load_state(cipc_sim* h, const char* path)
     s->sl.k0 = hd.sl_k0;
     s->sl.k1 = hd.sl_k1;
     s->step_count = (int)hd.step_count;
-    s->have_dir = false;
     return CIPC_OK;
 }
 
@@ -156,6 +155,5 @@ extern "C" int cipc_sim_load_obj_frames(cipc_sim* h, const char* obj_prev, const
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(s->v.p, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    s->have_dir = false;
     return e == cudaSuccess ? CIPC_OK : set_cuda_error(e, "cipc_sim_load_obj_frames");
 }

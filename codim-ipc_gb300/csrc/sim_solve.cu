@@ -205,15 +205,6 @@ __global__ void k_convert_scaled(int n, const double* a, double scale, float* b)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) b[i] = (float)(a[i] * scale);
 }
-// warm start: x = beta x, r = b - beta y (y = H x before scaling)
-__global__ void k_scale_residual(int n, double beta, const double* b, const double* y, double* x, double* r)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) {
-        x[i] *= beta;
-        r[i] = b[i] - beta * y[i];
-    }
-}
 // x += scale * d
 __global__ void k_axpy_scaled(int n, const float* d, double scale, double* x)
 {
@@ -297,44 +288,19 @@ static int solve_with_precond(Sim* s, const double* rhs, double* sol, int* iters
         double* y64 = (double*)take((size_t)n3 * 8);
         float *b32 = nullptr, *d32 = nullptr;
         if ((rc = pcg_fp32_io(s, &b32, &d32))) return rc;
+        cudaMemsetAsync(sol, 0, sizeof(double) * n3, s->stream);
+        cudaMemcpyAsync(r64, rhs, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s->stream);
         double* sc = C.sc;
         dot<double>(C, rhs, rhs, sc + 10);
-        double bb = 0, rr0 = -1;
-        if (s->have_dir) {
-            // warm start from the previous Newton direction (still in sol), scaled by
-            // beta = p.b / p.Hp, the factor that minimises the H-norm error along p:
-            // never worse than starting from zero in that norm.  Consecutive Newton
-            // systems of a step are close, most of all when CCD or the line search
-            // cut the last step short.
-            apply_H<float, double>(C, sol, y64);
-            dot<double>(C, sol, rhs, sc + 12);
-            dot<double>(C, sol, y64, sc + 13);
-            double h3[2];
-            cudaMemcpyAsync(h3, sc + 12, sizeof(h3), cudaMemcpyDeviceToHost, s->stream);
-            cudaMemcpyAsync(&bb, sc + 10, sizeof(double), cudaMemcpyDeviceToHost, s->stream);
-            cudaStreamSynchronize(s->stream);
-            const double beta = (h3[1] > 0 && std::isfinite(h3[0] / h3[1])) ? h3[0] / h3[1] : 0.0;
-            if (beta > 0) {
-                k_scale_residual<<<nblk(n3, 256), 256, 0, s->stream>>>(n3, beta, rhs, y64, sol, r64);
-                dot<double>(C, r64, r64, sc + 11);
-                cudaMemcpyAsync(&rr0, sc + 11, sizeof(double), cudaMemcpyDeviceToHost, s->stream);
-                cudaStreamSynchronize(s->stream);
-                if (!(rr0 < bb)) rr0 = -1;  // no gain: start from zero
-            }
-        }
-        if (rr0 < 0) {
-            cudaMemsetAsync(sol, 0, sizeof(double) * n3, s->stream);
-            cudaMemcpyAsync(r64, rhs, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s->stream);
-            cudaMemcpyAsync(&bb, sc + 10, sizeof(double), cudaMemcpyDeviceToHost, s->stream);
-            cudaStreamSynchronize(s->stream);
-        }
-        double rr = rr0 >= 0 ? rr0 : bb;
-        if (rr0 >= 0 && rr0 <= tol * tol * bb) rel = std::sqrt(rr0 / bb);  // the warm start already meets the tolerance
+        double bb = 0;
+        cudaMemcpyAsync(&bb, sc + 10, sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+        cudaStreamSynchronize(s->stream);
         // each pass asks the FP32 solver for what is still missing (with a margin
         // for the gap between its recurrence and the true residual), down to the
         // 1e-5 an FP32 Krylov recurrence reliably reaches; a pass restarts the
         // Krylov space, so fewer, deeper passes take fewer iterations in total
-        for (int outer = 0; outer < 20 && bb > 0 && !(rr0 >= 0 && rr0 <= tol * tol * bb); ++outer) {
+        double rr = bb;
+        for (int outer = 0; outer < 20 && bb > 0; ++outer) {
             const double rn = std::sqrt(rr);
             const double inner_tol = std::min(0.5, std::max(0.5 * tol * std::sqrt(bb / rr), 1e-5));
             k_convert_scaled<<<nblk(n3, 256), 256, 0, s->stream>>>(n3, r64, 1.0 / rn, b32);
@@ -360,7 +326,6 @@ static int solve_with_precond(Sim* s, const double* rhs, double* sol, int* iters
     if (iters) *iters = total;
     cudaError_t e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) return set_cuda_error(e, "linear solve");
-    s->have_dir = rel == rel;
     if (!(rel == rel)) return set_error(CIPC_ERR_NAN, "linear solve produced NaN");
     return rc;
 }

@@ -1003,7 +1003,6 @@ extern "C" int cipc_sim_set_state(cipc_sim* h, const double* x, const double* v)
     const size_t b = sizeof(double) * 3 * s->nv;
     if (x) cudaMemcpyAsync(s->x.p, x, b, cudaMemcpyHostToDevice, s->stream);
     if (v) cudaMemcpyAsync(s->v.p, v, b, cudaMemcpyHostToDevice, s->stream);
-    if (x) s->have_dir = false;  // no warm start across a replaced state
     cudaError_t e = cudaStreamSynchronize(s->stream);
     return e == cudaSuccess ? CIPC_OK : set_cuda_error(e, "cipc_sim_set_state");
 }
