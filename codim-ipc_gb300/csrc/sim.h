@@ -162,6 +162,13 @@ struct Sim {
     // block-Jacobi diagonal (9 per vertex, double) and its inverse (float/double)
     DBuf<double> pdiag;
     DBuf<char> pinv;
+    // Newton operator of the linear solve: the block rows with every contact and
+    // friction constraint folded in whose free-vertex pairs all have a block there
+    // (hval_op, float/double per precision), and the constraints left to apply
+    // matrix-free (crest, frest; their counts on the device in fold_cnt[0..1])
+    bool folded = false;
+    DBuf<char> hval_op;
+    DBuf<int> crest, frest, fold_cnt;
     // scratch
     DBuf<double> red;               // reduction partials
     DBuf<unsigned long long> cnt;   // counters

@@ -63,4 +63,9 @@ void kappa_check(Sim* s, const double* x, int* update_flag_dev);  // uses the pr
 // sim_solve.cu
 int linear_solve(Sim* s, const double* rhs, double* sol, int* iters);
 
+// sim_fold.cu: builds the solver's operator (s->hval_op and the matrix-free rest
+// lists; s->folded) from the assembled rows and constraint Hessians
+int fold_constraints(Sim* s);
+bool fold_enabled();
+
 }  // namespace cipc

@@ -6,6 +6,8 @@
 // Operator H = (elastic + mass, 3x3 block CSR) + sum over contact constraints of
 // their stored PSD blocks (packed upper triangle, 78 per constraint) + sum over
 // friction constraints of w_a w_b T M T^T (applied from the 2x2 inner matrix).
+// Constraints whose blocks were folded into the rows (sim_fold.cu) are left out of
+// the two constraint sums, which then run over the listed rest.
 // The preconditioner is a 3x3 block per vertex (block Jacobi, or any other
 // block-diagonal M^-1 written into the same array).
 //
@@ -103,6 +105,11 @@ struct PcgArgs {
     double tol;
     int maxit;
     int ncon, nfric;
+    // matrix-free constraints: clist[j] / flist[j] (j < nlist[0] / nlist[1]) when
+    // the operator's rows hold the folded constraints, else all ncon / nfric
+    const int* clist;
+    const int* flist;
+    const int* nlist;
     int trace;
     unsigned int wait_polls;  // polls of the arrival counter before a grid wait gives up
     double* part;             // 2 x gridDim.x x 4 block partial sums (reduction e uses half e % 2)
@@ -270,7 +277,7 @@ __device__ __forceinline__ XT con_apply_lane(const VT* __restrict__ H, size_t hs
 template <typename VT, typename XT, typename PT>
 __device__ __forceinline__ XT apply_phase(const PcgArgs<VT, XT, PT>& a, XT beta,
                                               const typename PcgArgs<VT, XT, PT>::XT2* zp,
-                                              typename PcgArgs<VT, XT, PT>::XT2* zp_next)
+                                              typename PcgArgs<VT, XT, PT>::XT2* zp_next, int ncon, int nfric)
 {
     // p_k = z_k + beta p_{k-1} (beta = 0 in the first iteration, where p_{-1} is
     // never written: the pair's second half is ignored then)
@@ -281,7 +288,7 @@ __device__ __forceinline__ XT apply_phase(const PcgArgs<VT, XT, PT>& a, XT beta,
     // work items: elastic scalar rows, then 4 lanes per contact constraint
     // (starting 4-aligned, so a constraint's lanes are 4 aligned lanes of one warp:
     // the grid stride is a multiple of 32), then friction constraints
-    const int nrow = 3 * a.nv, ncon = a.ncon, nfric = a.nfric;
+    const int nrow = 3 * a.nv;
     const int cbeg = (nrow + 3) & ~3, cend = cbeg + 4 * ncon;
     const int total = cend + nfric;
     XT v = 0;  // this thread's share, in the solver's precision; block sums are FP64
@@ -307,7 +314,8 @@ __device__ __forceinline__ XT apply_phase(const PcgArgs<VT, XT, PT>& a, XT beta,
             continue;
         } else if (w < cend) {
             // contact constraint c, lane k of its group of 4
-            const int c = (w - cbeg) >> 2, k = (w - cbeg) & 3;
+            const int j = (w - cbeg) >> 2, k = (w - cbeg) & 3;
+            const int c = a.clist ? __ldg(a.clist + j) : j;
             const int lane = threadIdx.x & 31, gbase = lane & ~3;
             const unsigned gmask = 0xFu << gbase;
             const int cnv = con_nv(__ldg(a.ckind + c));
@@ -318,7 +326,7 @@ __device__ __forceinline__ XT apply_phase(const PcgArgs<VT, XT, PT>& a, XT beta,
             else v += con_apply_lane<4>(H, a.hs, iv, k, gmask, gbase, pget, a.qc);
         } else {
             // friction constraint: w_a T M T^T sum_b w_b p_b over non-projected vertices
-            const int c = w - cend;
+            const int c = a.flist ? __ldg(a.flist + (w - cend)) : w - cend;
             if (a.fkind[c] >= kc_EEM) continue;
             const int cnv = con_nv(a.fkind[c]);
             const int4 iv = a.fverts[c];
@@ -355,6 +363,8 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
 {
     PcgScalars* d = a.d;
     unsigned int epoch = 0;
+    const int ncon = a.nlist ? min(__ldg(a.nlist), a.ncon) : a.ncon;
+    const int nfric = a.nlist ? min(__ldg(a.nlist + 1), a.nfric) : a.nfric;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     // r = b, x = 0, q_c = 0, z = M^-1 r
     double tot[2];
@@ -404,7 +414,7 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
         const XT beta = first ? XT(0) : (XT)(rz / rz_prev);
         const auto* zp = a.zp[k & 1];
         auto* zp_next = a.zp[(k + 1) & 1];
-        const XT va[1] = {apply_phase<VT, XT, PT>(a, beta, zp, zp_next)};
+        const XT va[1] = {apply_phase<VT, XT, PT>(a, beta, zp, zp_next, ncon, nfric)};
         double vd[1];
         lap(0);
         if (!grid_allreduce<1>(va, vd, d, epoch, a.wait_polls, a.part)) return;
@@ -548,7 +558,7 @@ int solve(Sim* s, const XT* b, XT* x, double tol, int maxit, int* iters, double*
     a.nv = s->nv;
     a.ell_k = s->ell_k;
     a.col = s->col.p;
-    a.val = reinterpret_cast<const VT*>(s->hval.p);
+    a.val = reinterpret_cast<const VT*>(s->folded ? s->hval_op.p : s->hval.p);
     a.ckind = s->ckind.p;
     a.cverts = s->cverts.p;
     a.chess = reinterpret_cast<const VT*>(s->chess.p);
@@ -572,6 +582,11 @@ int solve(Sim* s, const XT* b, XT* x, double tol, int maxit, int* iters, double*
     a.maxit = maxit;
     a.ncon = s->prm.withCollision ? s->ncon : 0;
     a.nfric = (s->prm.withCollision && s->prm.mu > 0) ? s->nfric : 0;
+    if (s->folded) {
+        a.clist = s->crest.p;
+        a.flist = s->frest.p;
+        a.nlist = s->fold_cnt.p;
+    }
     a.trace = s->trace;
     a.wait_polls = s->prm.pcg_wait_polls > 0 ? (unsigned int)s->prm.pcg_wait_polls : kBarrierSpinLimit;
     if ((int)st->part.n < 8 * g && st->part.alloc(8 * (size_t)g) != cudaSuccess)

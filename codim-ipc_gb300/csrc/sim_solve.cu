@@ -4,7 +4,8 @@
 //
 // Operator: y = H x with H = (elastic + mass, 3x3 block CSR) + sum over contact
 // constraints of their stored PSD blocks + sum over friction constraints of
-// w_a w_b T M T^T (applied matrix-free from the 2x2 inner matrix).  Dirichlet
+// w_a w_b T M T^T (applied matrix-free from the 2x2 inner matrix); constraints
+// folded into a copy of the block rows (sim_fold.cu) are applied through it.  Dirichlet
 // rows/columns were removed at assembly (identity diagonal), so Dirichlet
 // entries of every PCG vector stay zero.
 //
@@ -56,12 +57,14 @@ __global__ void __launch_bounds__(256) k_bsr_spmv(int nv, int ell_k, const int* 
 // contact blocks: packed upper triangle (row by row) of the (3nv x 3nv) constraint
 // Hessian, entry h of constraint c at hess[h * hs + c]
 template <typename VT, typename XT>
-__global__ void __launch_bounds__(128) k_con_spmv(int n, const int* __restrict__ kind, const int4* __restrict__ verts,
+__global__ void __launch_bounds__(128) k_con_spmv(int n, const int* __restrict__ list, const int* __restrict__ nlist,
+                                                  const int* __restrict__ kind, const int4* __restrict__ verts,
                                                   const VT* __restrict__ hess, size_t hs, const XT* __restrict__ x,
                                                   XT* __restrict__ y)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n || (list && c >= *nlist)) return;
+    if (list) c = list[c];
     const int nv = con_nv(kind[c]);
     const int m = 3 * nv;
     const int4 iv = verts[c];
@@ -90,12 +93,15 @@ __global__ void __launch_bounds__(128) k_con_spmv(int n, const int* __restrict__
 
 // friction: y_a += w_a T M T^T sum_b w_b x_b
 template <typename XT>
-__global__ void k_fric_spmv(int n, const int* __restrict__ kind, const int4* __restrict__ verts,
+__global__ void k_fric_spmv(int n, const int* __restrict__ list, const int* __restrict__ nlist,
+                            const int* __restrict__ kind, const int4* __restrict__ verts,
                             const double* __restrict__ fw, const double* __restrict__ fT, const double* __restrict__ M,
                             const uint8_t* __restrict__ dbc, const XT* __restrict__ x, XT* __restrict__ y)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n || kind[c] >= kc_EEM) return;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n || (list && c >= *nlist)) return;
+    if (list) c = list[c];
+    if (kind[c] >= kc_EEM) return;
     const int nv = con_nv(kind[c]);
     const int4 iv = verts[c];
     const int id[4] = {iv.x, iv.y, iv.z, iv.w};
@@ -232,13 +238,19 @@ template <typename VT, typename XT>
 static void apply_H(SolveCtx& C, const XT* x, XT* y)
 {
     Sim* s = C.s;
-    k_bsr_spmv<VT, XT><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, s->ell_k, s->col.p, (const VT*)s->hval.p, x, y);
-    if (s->ncon > 0)
-        k_con_spmv<VT, XT><<<nblk(s->ncon, 128), 128, 0, C.st>>>(s->ncon, s->ckind.p, s->cverts.p,
-                                                                  (const VT*)s->chess.p, (size_t)s->cap_con, x, y);
-    if (s->nfric > 0 && s->prm.mu > 0)
-        k_fric_spmv<XT><<<nblk(s->nfric, 128), 128, 0, C.st>>>(s->nfric, s->fkind.p, s->fverts.p, s->fw.p, s->fT.p,
-                                                                (const double*)s->fhess.p, s->proj.p, x, y);
+    const bool fo = s->folded;
+    k_bsr_spmv<VT, XT><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, s->ell_k, s->col.p,
+                                                            (const VT*)(fo ? s->hval_op.p : s->hval.p), x, y);
+    const int ncon = s->prm.withCollision ? s->ncon : 0;
+    const int nfric = (s->prm.withCollision && s->prm.mu > 0) ? s->nfric : 0;
+    if (ncon > 0)
+        k_con_spmv<VT, XT><<<nblk(ncon, 128), 128, 0, C.st>>>(ncon, fo ? s->crest.p : nullptr, s->fold_cnt.p,
+                                                               s->ckind.p, s->cverts.p, (const VT*)s->chess.p,
+                                                               (size_t)s->cap_con, x, y);
+    if (nfric > 0)
+        k_fric_spmv<XT><<<nblk(nfric, 128), 128, 0, C.st>>>(nfric, fo ? s->frest.p : nullptr, s->fold_cnt.p + 1,
+                                                             s->fkind.p, s->fverts.p, s->fw.p, s->fT.p,
+                                                             (const double*)s->fhess.p, s->proj.p, x, y);
 }
 
 // Finalizes the block-Jacobi preconditioner from the assembled matrix
@@ -344,6 +356,10 @@ int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
     if (s->prm.precond == 1 && s->learned && s->bj_last_iters > 0 && s->solve_fallbacks < 2)
         learned = lp_precond(s, static_cast<LpModel*>(s->learned)) == CIPC_OK;
     if (!learned) build_precond(s);
+    {
+        const int frc = fold_constraints(s);
+        if (frc) return frc;
+    }
     int total = 0, it = 0;
     const int maxit = s->prm.pcg_maxit;
     if (learned) s->prm.pcg_maxit = std::min(maxit, std::max(100, 3 * s->bj_last_iters));
