@@ -5,17 +5,23 @@ Workload (one "step"): one additive-CCD pass over 10,000,000 candidate pairs
 uniform in the unit cube, separations log-uniform in [1e-6, 1e-2], Gaussian
 displacements with sigma = 0.5 x separation, eta = 0.1, offset xi = 1e-7,
 step fraction 1.  Inputs are ~2 GB, larger than L2, so no flush is needed
-between steps.  The headline `value` runs the mixed-precision kernel on
-device-resident inputs; `e2e` runs the same pass through the C ABI with pinned
-host buffers (copies in the timed region).  The FP64 kernel and the barrier
-(energy/gradient/PSD Hessian) pass are reported under "variants".
+between steps.  The headline `value` runs the FP64 kernel (bit-exact against
+the reference's algorithm) on device-resident inputs; `e2e` runs the same pass
+through the C ABI with pinned host buffers (copies in the timed region).  The
+mixed-precision kernel and the barrier (energy/gradient/PSD Hessian) pass are
+reported under "variants" (--precision mixed times the mixed kernel instead).
 
-Also reported (single GPU): "timestep", ms/timestep of the 200x200 cloth on the
-rotating sphere for plain FP64 block-Jacobi PCG, FP32 Hessians with FP64
-refinement, the learned block-Jacobi correction, and each with inexact-Newton
-forcing; "scenes", absolute steps/s of the cloth-on-cube (with the CPU oracle
-on the same steps), mixed codimensional (rods + particles + cloth) and stacked
-shell scenes.
+Also reported (single GPU):
+  "timestep"  ms/timestep of the 200x200 cloth on the rotating sphere over
+              --ts-steps steps: plain FP64 block-Jacobi PCG, FP32 Hessians with
+              FP64 refinement (block Jacobi, the learned correction, aggregate
+              block Jacobi), and inexact-Newton forcing; --ts-cpu-steps adds the
+              CPU oracle on the same draped state;
+  "scenes"    the cloth-on-cube (with the CPU oracle on its first steps), the
+              mixed codimensional scene and the stacked shells at full size with
+              the learned correction trained on a smaller member of each family
+              (--codim-systems / --stack-systems triples), and the CPU oracle
+              against the GPU on smaller members of the three scene families.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl ours|reference]
 
@@ -226,120 +232,245 @@ def _time_calls(fn, steps, stream):
     return start.elapsed_time(stop), per
 
 
-def timestep_variants(args):
-    """ms/timestep of the cloth-on-rotating-sphere scene (200x200 cloth, 2 m, sphere
-    r 0.5 m at 2 rad/s, mu 0.4, xi 0.5 mm, dhat 1 mm, dt 0.02, Newton tol 1e-3):
-    plain FP64 block-Jacobi PCG vs FP32 Hessians + FP64 refinement, with block
-    Jacobi and with the learned correction trained on systems the plain mixed
-    solver captured while draping.  Every variant starts from the same draped
-    state and advances ts_steps steps."""
-    import cipc_ffi as F
-    import workloads
-
-    X, T, dbc, c = workloads.cloth_on_sphere(n=args.ts_n)
-    dt, omega = 0.02, 2.0
-
-    def target(k):
-        return workloads.rotate_y(X[dbc], c, omega * dt * (k + 1))
-
-    def make(prec, pre, forcing=0):
-        s = F.Sim(X, T, 200.0, 1e5, 0.3, 1e-3)
-        _, dhat2 = s.init_oipc(1e-3)
-        prm = F.make_params(dt, dhat2, 5e-4, mu=0.4, epsv2=1e-6, fric_iters=1, newton_tol=1e-3, precision=prec,
-                            pcg_tol=1e-4, preconditioner=pre, forcing=forcing)
-        return s, prm
-
-    ok = (F.CIPC_ERR_NOT_CONVERGED,)
-    s, prm = make(F.MIXED, 0)
-    pc = F.Precond(hidden=16, layers=2, seed=0)
-    cap_from = max(0, args.ts_warm - 6)
-    for k in range(args.ts_warm):
-        if k == cap_from:
-            F.sim_capture_systems(s, pc, 512)
-        s.set_dbc(dbc, target(k))
-        s.step(prm, allow=ok)
-    F.sim_capture_systems(s, None, 0)
-    x0, v0 = s.state()
-    k0 = s.kappa()
-    s.close()
-    t0 = time.perf_counter()
-    loss_before, loss_after = pc.train(epochs=args.ts_epochs, batch=8, lr=1e-3, seed=0)
-    train_s = time.perf_counter() - t0
-    out = {"workload": "cloth on rotating sphere, %dx%d cloth (%d vertices incl. sphere), %d steps from step %d"
-                       % (args.ts_n, args.ts_n, X.shape[0], args.ts_steps, args.ts_warm),
-           "unit": "ms/timestep", "newton_tol": 1e-3, "pcg_tol": 1e-4,
-           "learned": {"systems": pc.num_systems(), "epochs": args.ts_epochs, "train_s": round(train_s, 2),
-                       "loss_before": round(loss_before, 4), "loss_after": round(loss_after, 4)}}
-    variants = (("fp64_block_jacobi", F.FP64, 0, 0), ("mixed_block_jacobi", F.MIXED, 0, 0),
-                ("mixed_learned", F.MIXED, 1, 0), ("fp64_block_jacobi_inexact", F.FP64, 0, 1),
-                ("mixed_block_jacobi_inexact", F.MIXED, 0, 1))
-    for name, prec, pre, forcing in variants:
-        sv, pv = make(prec, pre, forcing)
-        if pre:
-            F.sim_set_precond(sv, pc)
-        sv.set_state(x0, v0)
-        sv.set_kappa(k0[0], k0[1])
-        rows = []
-        for k in range(args.ts_warm, args.ts_warm + args.ts_steps):
-            sv.set_dbc(dbc, target(k))
-            st = sv.step(pv, allow=ok)
-            rows.append(st.as_dict())
-        sv.close()
-        out[name] = {"ms_per_step": round(float(np.mean([r["ms"] for r in rows])), 2),
-                     "newton_per_step": round(float(np.mean([r["newton_iters"] for r in rows])), 2),
-                     "pcg_per_step": round(float(np.mean([r["pcg_iters"] for r in rows])), 1),
-                     "fallbacks": int(sum(r["precond_fallbacks"] for r in rows)),
-                     "min_dist2_min": float(min(r["min_dist2"] for r in rows)),
-                     "intersection_free": bool(all(r["min_dist2"] > 0 or r["n_constraints"] == 0 for r in rows)),
-                     "status": sorted(set(int(r["status"]) for r in rows))}
-    out["speedup_mixed_learned_vs_fp64"] = round(out["fp64_block_jacobi"]["ms_per_step"]
-                                                 / out["mixed_learned"]["ms_per_step"], 3)
-    out["speedup_mixed_vs_fp64"] = round(out["fp64_block_jacobi"]["ms_per_step"]
-                                         / out["mixed_block_jacobi"]["ms_per_step"], 3)
-    out["speedup_mixed_inexact_vs_fp64"] = round(out["fp64_block_jacobi"]["ms_per_step"]
-                                                 / out["mixed_block_jacobi_inexact"]["ms_per_step"], 3)
-    out["note"] = ("*_inexact: Eisenstat-Walker forcing term for the Newton systems (cipc_step_params.forcing = 1); "
-                   "the Newton tolerance is the same for every variant; the forcing term is not combined with the "
-                   "learned correction")
-    pc.close()
-    return out
+_T0 = time.perf_counter()
 
 
-def _scene_stats(rows):
+def _log(msg):
+    """Progress line on stderr (stdout carries only the JSON line)."""
+    sys.stderr.write("[bench %7.1fs] %s\n" % (time.perf_counter() - _T0, msg))
+    sys.stderr.flush()
+
+
+def _stats(rows):
+    """Per-variant summary of step statistics (one dict per step)."""
     ms = [r["ms"] for r in rows]
     con = [r for r in rows if r["n_constraints"] > 0]
     return {"steps": len(rows), "ms_per_step": round(float(np.mean(ms)), 2),
             "steps_per_s": round(1000.0 / float(np.mean(ms)), 3),
             "newton_per_step": round(float(np.mean([r["newton_iters"] for r in rows])), 2),
             "pcg_per_step": round(float(np.mean([r["pcg_iters"] for r in rows])), 1),
+            "fallbacks": int(sum(r["precond_fallbacks"] for r in rows)),
             "constraints_max": int(max(r["n_constraints"] for r in rows)),
             "min_dist2_min": float(min(r["min_dist2"] for r in con)) if con else None,
             "intersection_free": bool(all(r["min_dist2"] > 0 for r in con)),
             "status": sorted(set(int(r["status"]) for r in rows))}
 
 
-def scene_runs(args):
-    """Absolute steps/s of the other named scenes, each from its initial state:
-    the 40x40 cloth falling on a fixed 0.3 m cube (StVK, 50 steps, dt 0.04, Newton
-    tol 1e-2; FP64 and mixed, and the CPU oracle on its first steps), the mixed
-    codimensional scene (1000 rods x 100 segments, 20000 particles, 120x120 cloth
-    pinned at its corners; dt 0.01, mu 0.2) and the 8-layer stacked shells
-    (8 x 180x180 cloths between a fixed and a descending plate at 0.05 m/s;
-    dt 0.01, mu 0.3, xi = dhat = 0.5 mm)."""
+class Scene:
+    """One named scene: construction of a GPU handle, step parameters and the
+    Dirichlet targets of step k (every variant of a scene runs the same steps)."""
+
+    def __init__(self, name, X, T, dbc, target, dt, xi, dhat, mu, newton_tol, codim=None, desc=""):
+        self.name, self.X, self.T, self.dbc, self.target = name, X, T, dbc, target
+        self.dt, self.xi, self.dhat, self.mu, self.newton_tol, self.codim, self.desc = (dt, xi, dhat, mu, newton_tol,
+                                                                                       codim, desc)
+
+    def sim(self, precision, precond=0, forcing=0, pcg_tol=1e-4):
+        import cipc_ffi as F
+        s = F.Sim(self.X, self.T, 200.0, 1e5, 0.3, 1e-3, codim=self.codim)
+        _, dhat2 = s.init_oipc(self.dhat)
+        prm = F.make_params(self.dt, dhat2, self.xi, mu=self.mu, epsv2=1e-6, fric_iters=1, newton_tol=self.newton_tol,
+                            precision=precision, pcg_tol=pcg_tol, preconditioner=precond, forcing=forcing)
+        return s, prm
+
+    def run(self, s, prm, k0, steps):
+        import cipc_ffi as F
+        rows = []
+        for k in range(k0, k0 + steps):
+            s.set_dbc(self.dbc, self.target(k))
+            rows.append(s.step(prm, allow=(F.CIPC_ERR_NOT_CONVERGED,)).as_dict())
+            if (k - k0) % 10 == 9:
+                r = rows[-1]
+                _log("  %s step %d: %.1f ms, %d Newton, %d PCG, %d constraints" % (
+                    self.name, k, r["ms"], r["newton_iters"], r["pcg_iters"], r["n_constraints"]))
+        return rows
+
+    def oracle(self):
+        from oracle import oracle_ffi as orc
+        sh = orc.Shell(self.X, self.T, 200.0, 1e5, 0.3, 1e-3, codim=self.codim)
+        k2, dhat2 = sh.init_oipc(self.dhat)
+        return sh, k2, dhat2
+
+
+def sphere_scene(n=200, size=2.0, radius=0.5, gap=0.01, subdiv=4):
+    import workloads as W
+    X, T, dbc, c = W.cloth_on_sphere(n=n, size=size, radius=radius, gap=gap, subdiv=subdiv)
+    return Scene("cloth_on_sphere", X, T, dbc, lambda k: W.rotate_y(X[dbc], c, 2.0 * 0.02 * (k + 1)), 0.02, 5e-4,
+                 1e-3, 0.4, 1e-3, desc="%dx%d cloth (%.1f m) on a r = %.2f m sphere at 2 rad/s, mu 0.4, xi 0.5 mm, "
+                                       "dhat 1 mm, dt 0.02, Newton tol 1e-3; %d vertices" % (n, n, size, radius,
+                                                                                             X.shape[0]))
+
+
+def codim_scene(full=True, seed=0):
+    import workloads as W
+    if full:
+        X, T, S, P, corners = W.rods_particles_on_cloth_full(seed=seed)
+        d = "1000 rods x 100 segments (0.5 m), 20000 particles, 120x120 cloth pinned at its corners"
+    else:
+        X, T, S, P, corners = W.rods_particles_on_cloth(
+            n_rods=100, seg_per_rod=50, rod_len=0.25, n_particles=2000, cloth_n=40, cloth_size=0.5,
+            layer_gap=2.5e-3, particle_gap=5e-3, lift=1.5e-3, rods_per_layer=20, rod_spacing=5e-3,
+            particles_per_row=32, seed=seed)
+        d = "100 rods x 50 segments (0.25 m), 2000 particles, 40x40 cloth (0.5 m) pinned at its corners"
+    codim = dict(segments=S, rod_E=1e7, rod_rho=1000.0, rod_thickness=1e-3, particles=P, particle_rho=1000.0,
+                 particle_thickness=4e-3)
+    return Scene("rods_particles_on_cloth", X, T, corners, lambda k: X[corners], 0.01, 1e-3, 1e-3, 0.2, 1e-2,
+                 codim=codim, desc="%s; E_rod 1e7, xi = dhat = 1 mm, mu 0.2, dt 0.01, Newton tol 1e-2; %d vertices"
+                                   % (d, X.shape[0]))
+
+
+def stacked_scene(full=True, seed=0):
+    import workloads as W
+    if full:
+        X, T, dbc, top = W.stacked_shells(seed=seed)
+        d = "8 layers of 180x180 cloth (1 m, 5 mm apart, 1 mm jitter)"
+    else:
+        X, T, dbc, top = W.stacked_shells(n=30, layers=8, size=1.0 / 6, plate_n=6, seed=seed)
+        d = "8 layers of 30x30 cloth (0.17 m, 5 mm apart, 1 mm jitter)"
+    istop = np.isin(dbc, top)
+
+    def plate(k):
+        Y = X[dbc].copy()
+        Y[istop, 1] -= 0.05 * 0.01 * (k + 1)
+        return Y
+
+    return Scene("stacked_shells", X, T, dbc, plate, 0.01, 5e-4, 5e-4, 0.3, 1e-2,
+                 desc="%s between a fixed plate and one descending at 0.05 m/s; xi = dhat = 0.5 mm, mu 0.3, dt 0.01, "
+                      "Newton tol 1e-2; %d vertices" % (d, X.shape[0]))
+
+
+def _train(make, systems, epochs, steps, hidden=16, budget_s=150.0):
+    """Learned correction trained on `systems` (Hessian, residual, Newton step)
+    triples that the plain mixed block-Jacobi solver generates on smaller members
+    of a scene family: make(full=False, seed=k) for seeds 1, 2, ..., each over
+    the first `steps` steps (the window the full-size comparison runs), until the
+    count is reached or the capture has run budget_s seconds."""
+    import cipc_ffi as F
+    pc = F.Precond(hidden=hidden, layers=2, seed=0)
+    t0 = time.perf_counter()
+    seed, nsteps = 0, 0
+    while pc.num_systems() < systems and time.perf_counter() - t0 < budget_s and seed < 1000:
+        seed += 1
+        scene = make(full=False, seed=seed)
+        s, prm = scene.sim(F.MIXED)
+        F.sim_capture_systems(s, pc, systems)
+        for k in range(steps):
+            scene.run(s, prm, k, 1)
+            nsteps += 1
+            if pc.num_systems() >= systems or time.perf_counter() - t0 >= budget_s:
+                break
+        F.sim_capture_systems(s, None, 0)
+        s.close()
+    _log("%s: captured %d systems in %d steps of %d seeds" % (scene.desc, pc.num_systems(), nsteps, seed))
+    t1 = time.perf_counter()
+    lb, la = pc.train(epochs=epochs, batch=8, lr=1e-3, seed=0)
+    _log("trained %d epochs in %.1f s" % (epochs, time.perf_counter() - t1))
+    return pc, {"systems": pc.num_systems(), "capture_steps": nsteps, "family_seeds": seed,
+                "family_member": scene.desc + "; seeds 1-%d, first %d steps each" % (seed, steps), "epochs": epochs,
+                "train_s": round(time.perf_counter() - t1, 2), "loss_before": round(lb, 4),
+                "loss_after": round(la, 4)}
+
+
+VARIANTS = {  # name: (precision, preconditioner, forcing)
+    "fp64_block_jacobi": ("fp64", 0, 0), "mixed_block_jacobi": ("mixed", 0, 0), "mixed_learned": ("mixed", 1, 0),
+    "mixed_aggregate": ("mixed", 2, 0), "fp64_block_jacobi_inexact": ("fp64", 0, 1),
+    "mixed_aggregate_inexact": ("mixed", 2, 1)}
+
+
+def compare(scene, names, k0, steps, x0=None, v0=None, k2=None, pc=None):
+    """Runs each variant from the same state over the same steps; speed-ups are
+    against fp64_block_jacobi (the plain FP64 block-Jacobi PCG path) at the same
+    Newton tolerance."""
+    import cipc_ffi as F
+    out = {}
+    for name in names:
+        prec, pre, forcing = VARIANTS[name]
+        s, prm = scene.sim(F.MIXED if prec == "mixed" else F.FP64, pre, forcing)
+        if pre == 1:
+            F.sim_set_precond(s, pc)
+        if x0 is not None:
+            s.set_state(x0, v0)
+            s.set_kappa(k2[0], k2[1])
+        out[name] = _stats(scene.run(s, prm, k0, steps))
+        s.close()
+        _log("%s %s: %.1f ms/step, %.1f Newton, %.0f PCG per step" % (scene.name, name, out[name]["ms_per_step"],
+                                                                     out[name]["newton_per_step"],
+                                                                     out[name]["pcg_per_step"]))
+    base = out["fp64_block_jacobi"]["ms_per_step"]
+    for name in names:
+        if name != "fp64_block_jacobi":
+            out["speedup_%s_vs_fp64" % name.replace("_block_jacobi", "")] = round(base / out[name]["ms_per_step"], 3)
+    return out
+
+
+def timestep_variants(args):
+    """ms/timestep of the cloth-on-rotating-sphere scene (200x200 cloth, 2 m,
+    sphere r 0.5 m at 2 rad/s, mu 0.4, xi 0.5 mm, dhat 1 mm, dt 0.02, Newton tol
+    1e-3): plain FP64 block-Jacobi PCG against FP32 Hessians + FP64 refinement
+    with block Jacobi, the learned correction (trained on the systems the plain
+    mixed solver captured while draping) and aggregate block Jacobi, and with
+    inexact-Newton forcing.  Every variant starts from the same draped state and
+    advances the same ts_steps steps."""
+    import cipc_ffi as F
+
+    sc = sphere_scene(n=args.ts_n)
+    s, prm = sc.sim(F.MIXED)
+    pc = F.Precond(hidden=16, layers=2, seed=0)
+    cap_from = max(0, args.ts_warm - 6)
+    for k in range(args.ts_warm):
+        if k == cap_from:
+            F.sim_capture_systems(s, pc, 512)
+        sc.run(s, prm, k, 1)
+    F.sim_capture_systems(s, None, 0)
+    x0, v0 = s.state()
+    k0 = s.kappa()
+    s.close()
+    t0 = time.perf_counter()
+    loss_before, loss_after = pc.train(epochs=args.ts_epochs, batch=8, lr=1e-3, seed=0)
+    out = {"workload": "cloth on rotating sphere, %s, %d steps from step %d" % (sc.desc, args.ts_steps, args.ts_warm),
+           "unit": "ms/timestep", "newton_tol": 1e-3, "pcg_tol": 1e-4,
+           "learned": {"systems": pc.num_systems(), "epochs": args.ts_epochs,
+                       "train_s": round(time.perf_counter() - t0, 2), "loss_before": round(loss_before, 4),
+                       "loss_after": round(loss_after, 4)}}
+    names = ["fp64_block_jacobi", "mixed_block_jacobi", "mixed_learned", "mixed_aggregate"]
+    if args.ts_inexact:
+        names += ["fp64_block_jacobi_inexact", "mixed_aggregate_inexact"]
+    out.update(compare(sc, names, args.ts_warm, args.ts_steps, x0, v0, k0, pc))
+    out["note"] = ("aggregate: exact inverses of the diagonal blocks of vertex aggregates (CIPC_PRECOND_AGGREGATE); "
+                   "*_inexact (--ts-inexact): Eisenstat-Walker forcing term (cipc_step_params.forcing = 1); the "
+                   "Newton tolerance is the same for every variant; the forcing term is not combined with the "
+                   "learned correction")
+    pc.close()
+    return out
+
+
+def learned_scenes(args):
+    """The mixed codimensional scene and the stacked shells at full size, each
+    with the learned correction trained on (Hessian, residual, Newton step)
+    triples that the plain mixed block-Jacobi solver generated on a smaller
+    member of the same scene family: plain FP64 block-Jacobi PCG against mixed
+    precision with block Jacobi, the learned correction and aggregate block
+    Jacobi, from the initial state over the same steps."""
+    out = {}
+    names = ["fp64_block_jacobi", "mixed_block_jacobi", "mixed_learned", "mixed_aggregate"]
+    for key, make, systems, steps in (("rods_particles_on_cloth", codim_scene, args.codim_systems, args.sc_steps),
+                                      ("stacked_shells_8x180", stacked_scene, args.stack_systems, args.sc_steps)):
+        pc, info = _train(make, systems, args.sc_epochs, steps)
+        full = make(full=True)
+        r = {"workload": "%s; first %d steps" % (full.desc, steps), "learned": info}
+        r.update(compare(full, names, 0, steps, pc=pc))
+        pc.close()
+        out[key] = r
+    return out
+
+
+def cube_scene(args):
+    """Absolute steps/s of the 40x40 cloth falling on a fixed 0.3 m cube (StVK,
+    dt 0.04, Newton tol 1e-2; FP64 and mixed), with the CPU oracle on its first
+    steps."""
     import cipc_ffi as F
     import workloads
 
-    ok = (F.CIPC_ERR_NOT_CONVERGED,)
-
-    def run(sim, prm, dbc, tgt, steps):
-        rows = []
-        for k in range(steps):
-            sim.set_dbc(dbc, tgt(k))
-            rows.append(sim.step(prm, allow=ok).as_dict())
-        return rows
-
-    out = {"precond": "block Jacobi", "pcg_tol": 1e-4}
-    # cloth on cube
     X, T, dbc = workloads.cloth_on_box(n=40)
     c1 = {"workload": "40x40 cloth (1 m, StVK E 1e5, t 1 mm) falling 0.1 m onto a fixed 0.3 m cube, dt 0.04, "
                       "xi = dhat = 1 mm, Newton tol 1e-2, %d vertices incl. the cube" % X.shape[0]}
@@ -347,9 +478,12 @@ def scene_runs(args):
         s = F.Sim(X, T, 200.0, 1e5, 0.3, 1e-3, nh=False)
         _, dhat2 = s.init_oipc(1e-3)
         prm = F.make_params(0.04, dhat2, 1e-3, newton_tol=1e-2, precision=prec, pcg_tol=1e-4)
-        rows = run(s, prm, dbc, lambda k: X[dbc], args.c1_steps)
+        rows = []
+        for k in range(args.c1_steps):
+            s.set_dbc(dbc, X[dbc])
+            rows.append(s.step(prm, allow=(F.CIPC_ERR_NOT_CONVERGED,)).as_dict())
         s.close()
-        c1[name] = _scene_stats(rows)
+        c1[name] = _stats(rows)
         c1[name]["first_%d_ms_per_step" % args.c1_cpu_steps] = round(
             float(np.mean([r["ms"] for r in rows[:args.c1_cpu_steps]])), 2)
     if not args.no_cpu_baseline and args.c1_cpu_steps > 0:
@@ -367,40 +501,76 @@ def scene_runs(args):
                             "newton_per_step": round(float(np.mean(newton)), 2),
                             "sample": "first %d steps, direct (skyline LDL^T) Newton solves" % args.c1_cpu_steps}
         c1["speedup_mixed_vs_cpu_oracle"] = round(cpu_ms / c1["mixed"]["first_%d_ms_per_step" % args.c1_cpu_steps], 1)
-    out["cloth_on_cube_40"] = c1
-    # mixed codimensional scene
-    X, T, S, P, corners = workloads.rods_particles_on_cloth_full()
-    codim = dict(segments=S, rod_E=1e7, rod_rho=1000.0, rod_thickness=1e-3, particles=P, particle_rho=1000.0,
-                 particle_thickness=4e-3)
-    s = F.Sim(X, T, 200.0, 1e5, 0.3, 1e-3, codim=codim)
-    _, dhat2 = s.init_oipc(1e-3)
-    prm = F.make_params(0.01, dhat2, 1e-3, mu=0.2, epsv2=1e-6, fric_iters=1, newton_tol=1e-2, precision=F.MIXED,
-                        pcg_tol=1e-4)
-    rows = run(s, prm, corners, lambda k: X[corners], args.sc_steps)
-    s.close()
-    out["rods_particles_on_cloth"] = dict(
-        workload="1000 rods x 100 segments (0.5 m, E 1e7, 5 layers of 200 with seeded directions), 20000 particles "
-                 "(4 mm), 120x120 cloth pinned at its corners; %d vertices; dt 0.01, xi = dhat = 1 mm, mu 0.2; "
-                 "first %d steps, mixed precision" % (X.shape[0], args.sc_steps), **_scene_stats(rows))
-    # stacked shells
-    X, T, dbc, top = workloads.stacked_shells()
-    s = F.Sim(X, T, 200.0, 1e5, 0.3, 1e-3)
-    _, dhat2 = s.init_oipc(5e-4)
-    prm = F.make_params(0.01, dhat2, 5e-4, mu=0.3, epsv2=1e-6, fric_iters=1, newton_tol=1e-2, precision=F.MIXED,
-                        pcg_tol=1e-4)
-    istop = np.isin(dbc, top)
+    return c1
 
-    def plate(k):
-        Y = X[dbc].copy()
-        Y[istop, 1] -= 0.05 * 0.01 * (k + 1)
-        return Y
 
-    rows = run(s, prm, dbc, plate, args.sc_steps)
+def cpu_family(args):
+    """The CPU oracle (the reference's algorithm restated, direct skyline LDL^T
+    Newton solves, OpenMP on the host cores) against the GPU paths on smaller
+    members of the three scene families, first args.family_steps steps from the
+    initial state: the full-size scenes' direct factorizations take minutes per
+    Newton iteration on the host."""
+    import cipc_ffi as F
+    from oracle import oracle_ffi as orc
+
+    out = {}
+    for sc in (sphere_scene(n=40, size=0.4, radius=0.1, gap=0.002, subdiv=3), codim_scene(full=False),
+               stacked_scene(full=False)):
+        sh, k2, dhat2 = sc.oracle()
+        x, v = sc.X.copy(), np.zeros_like(sc.X)
+        newton = []
+        t0 = time.perf_counter()
+        for k in range(args.family_steps):
+            rc, st = sh.step(x, v, k2, sc.dbc, sc.target(k), sc.dt, dhat2, sc.xi, mu=sc.mu, epsv2=1e-6, fric_iters=1,
+                             tol=sc.newton_tol)
+            newton.append(st["newton_iters"])
+        cpu_ms = (time.perf_counter() - t0) * 1e3 / args.family_steps
+        _log("%s family member: CPU oracle %.1f ms/step" % (sc.name, cpu_ms))
+        r = {"workload": "%s; first %d steps" % (sc.desc, args.family_steps),
+             "cpu_oracle": {"kind": "port", "cores": orc.num_threads(), "ms_per_step": round(cpu_ms, 1),
+                            "newton_per_step": round(float(np.mean(newton)), 2)}}
+        for name, prec in (("fp64_block_jacobi", F.FP64), ("mixed_block_jacobi", F.MIXED)):
+            s, prm = sc.sim(prec)
+            r[name] = _stats(sc.run(s, prm, 0, args.family_steps))
+            s.close()
+            r["speedup_%s_vs_cpu_oracle" % name.replace("_block_jacobi", "")] = round(
+                cpu_ms / r[name]["ms_per_step"], 1)
+        out[sc.name] = r
+    return out
+
+
+def sphere_cpu_steps(args):
+    """The CPU oracle on the full 200x200 cloth-on-sphere scene from the GPU's
+    draped state (args.ts_warm draping steps), args.ts_cpu_steps steps, beside the
+    GPU variants over the same steps (minutes per step on the host)."""
+    import cipc_ffi as F
+
+    sc = sphere_scene(n=args.ts_n)
+    s, prm = sc.sim(F.MIXED)
+    sc.run(s, prm, 0, args.ts_warm)
+    x0, v0 = s.state()
+    k0 = s.kappa()
     s.close()
-    out["stacked_shells_8x180"] = dict(
-        workload="8 layers of 180x180 cloth (1 m, 5 mm apart, 1 mm seeded in-plane jitter) between a fixed plate and "
-                 "a plate descending at 0.05 m/s; %d vertices; dt 0.01, xi = dhat = 0.5 mm, mu 0.3; first %d steps, "
-                 "mixed precision" % (X.shape[0], args.sc_steps), **_scene_stats(rows))
+    sh, _, dhat2 = sc.oracle()
+    x, v, k2 = x0.copy(), v0.copy(), np.array(k0, float)
+    newton = []
+    t0 = time.perf_counter()
+    for k in range(args.ts_warm, args.ts_warm + args.ts_cpu_steps):
+        rc, st = sh.step(x, v, k2, sc.dbc, sc.target(k), sc.dt, dhat2, sc.xi, mu=sc.mu, epsv2=1e-6, fric_iters=1,
+                         tol=sc.newton_tol)
+        newton.append(st["newton_iters"])
+    from oracle import oracle_ffi as orc
+    cpu_ms = (time.perf_counter() - t0) * 1e3 / args.ts_cpu_steps
+    out = {"workload": "%s; %d steps from step %d (state draped by the GPU)" % (sc.desc, args.ts_cpu_steps,
+                                                                                args.ts_warm),
+           "cpu_oracle": {"kind": "port", "cores": orc.num_threads(), "ms_per_step": round(cpu_ms, 1),
+                          "newton_per_step": round(float(np.mean(newton)), 2),
+                          "sample": "direct (skyline LDL^T) Newton solves"}}
+    out.update(compare(sc, ["fp64_block_jacobi", "mixed_block_jacobi", "mixed_aggregate"], args.ts_warm,
+                       args.ts_cpu_steps, x0, v0, k0))
+    for name in ("fp64_block_jacobi", "mixed_block_jacobi", "mixed_aggregate"):
+        out["speedup_%s_vs_cpu_oracle" % name.replace("_block_jacobi", "")] = round(cpu_ms / out[name]["ms_per_step"],
+                                                                                     1)
     return out
 
 
@@ -568,8 +738,13 @@ def run_ours(args):
         }
         if ws == 1 and not args.no_timestep:
             line["timestep"] = timestep_variants(args)
+            if args.ts_cpu_steps > 0:
+                line["timestep"]["cpu_oracle_steps"] = sphere_cpu_steps(args)
         if ws == 1 and not args.no_scenes:
-            line["scenes"] = scene_runs(args)
+            line["scenes"] = {"pcg_tol": 1e-4, "cloth_on_cube_40": cube_scene(args)}
+            line["scenes"].update(learned_scenes(args))
+            if not args.no_cpu_baseline and args.family_steps > 0:
+                line["scenes"]["cpu_family"] = cpu_family(args)
         print(json.dumps(line))
     if ws > 1:
         dist.barrier()
@@ -590,16 +765,27 @@ def main():
     ap.add_argument("--no-timestep", action="store_true", help="skip the cloth-on-sphere ms/timestep variants")
     ap.add_argument("--ts-n", type=int, default=200, help="cloth resolution of the time-step variants")
     ap.add_argument("--ts-warm", type=int, default=10, help="draping steps before the measured steps")
-    ap.add_argument("--ts-steps", type=int, default=6, help="measured steps per variant")
+    ap.add_argument("--ts-steps", type=int, default=50, help="measured steps per variant")
     ap.add_argument("--ts-epochs", type=int, default=20, help="training epochs of the learned correction")
-    ap.add_argument("--no-scenes", action="store_true", help="skip the cube / codimensional / stacked-shell scenes")
+    ap.add_argument("--ts-inexact", action="store_true", help="add the inexact-Newton (forcing term) variants")
+    ap.add_argument("--ts-cpu-steps", type=int, default=0,
+                    help="steps of the CPU oracle on the full cloth-on-sphere scene from the draped state (minutes "
+                         "per step)")
+    ap.add_argument("--no-scenes", action="store_true",
+                    help="skip the cube, codimensional and stacked-shell scenes and the CPU scene-family runs")
+    ap.add_argument("--codim-systems", type=int, default=2000,
+                    help="training triples of the learned correction for the codimensional scene")
+    ap.add_argument("--stack-systems", type=int, default=1000,
+                    help="training triples of the learned correction for the stacked shells")
+    ap.add_argument("--sc-epochs", type=int, default=8, help="training epochs for the two scene families")
+    ap.add_argument("--family-steps", type=int, default=3, help="steps of the CPU oracle on each scene-family member")
     ap.add_argument("--trace-scene", type=int, default=0,
                     help="only step the cloth-on-sphere scene at this resolution (profiling workload)")
     ap.add_argument("--trace-steps", type=int, default=12)
     ap.add_argument("--trace-precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--c1-steps", type=int, default=50, help="steps of the cloth-on-cube scene")
     ap.add_argument("--c1-cpu-steps", type=int, default=8, help="cloth-on-cube steps run by the CPU oracle")
-    ap.add_argument("--sc-steps", type=int, default=6, help="steps of the codimensional and stacked scenes")
+    ap.add_argument("--sc-steps", type=int, default=10, help="steps of the codimensional and stacked scenes")
     args = ap.parse_args()
     if args.trace_scene > 0:
         trace_scene(args)

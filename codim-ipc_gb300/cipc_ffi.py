@@ -25,6 +25,9 @@ CIPC_ERR_TIMEOUT = 9
 
 FP64 = 0
 MIXED = 1
+PRECOND_BLOCK_JACOBI = 0
+PRECOND_LEARNED = 1
+PRECOND_AGGREGATE = 2
 MEM_HOST = 0
 MEM_DEVICE = 1
 

@@ -75,7 +75,7 @@ struct SimParams {
     int precision = 0;        // 0 FP64 Hessians / PCG, 1 FP32 Hessians + FP32 PCG with FP64 refinement
     double pcg_tol = 1e-6;    // relative residual of the Newton system (FP64)
     int pcg_maxit = 10000;
-    int precond = 0;          // 0 block-Jacobi, 1 learned correction (when a model is loaded)
+    int precond = 0;          // 0 block-Jacobi, 1 learned correction (when a model is loaded), 2 aggregate block Jacobi
     int forcing = 0;          // 1: inexact Newton (Eisenstat-Walker forcing term)
     int elastic = 0;          // 1: elastic IPC (no offset, barrier scaled by 1/dhat^4, kappa fixed)
     long long accd_max_iter = 1 << 20;  // ACCD steps per pair in the step-size search
@@ -169,6 +169,11 @@ struct Sim {
     bool folded = false;
     DBuf<char> hval_op;
     DBuf<int> crest, frest, fold_cnt;
+    // aggregate block Jacobi (sim_aggregate.cu): vertex aggregates built once per
+    // mesh and the inverses of their diagonal blocks; agg_ready: the inverses
+    // belong to the current Newton system
+    void* agg = nullptr;
+    bool agg_ready = false;
     // scratch
     DBuf<double> red;               // reduction partials
     DBuf<unsigned long long> cnt;   // counters

@@ -68,4 +68,20 @@ int linear_solve(Sim* s, const double* rhs, double* sol, int* iters);
 int fold_constraints(Sim* s);
 bool fold_enabled();
 
+// sim_aggregate.cu: aggregate block Jacobi.  agg_setup builds (once per mesh) the
+// vertex aggregates and, for the current Newton system (after fold_constraints),
+// the inverses of the aggregates' diagonal blocks; sets s->agg_ready, or returns
+// CIPC_ERR_NOT_CONVERGED when a block is not positive definite (the caller then
+// uses block Jacobi).  agg_view fills the solver's view of the inverses.
+int agg_setup(Sim* s);
+struct AggView {
+    int nagg;
+    const int* voff;        // nagg + 1 offsets into verts
+    const int* verts;       // vertices by aggregate
+    const long long* boff;  // nagg + 1 offsets of the dense inverse blocks (entries)
+    const void* inv;        // inverses (float or double per precision), symmetric m x m, m = 3 x vertices
+};
+AggView agg_view(const Sim* s);
+void agg_release(Sim* s);
+
 }  // namespace cipc

@@ -9,22 +9,22 @@
 // Constraints whose blocks were folded into the rows (sim_fold.cu) are left out of
 // the two constraint sums, which then run over the listed rest.
 // The preconditioner is a 3x3 block per vertex (block Jacobi, or any other
-// block-diagonal M^-1 written into the same array).
+// block-diagonal M^-1 written into the same array), or the inverses of the
+// aggregates' diagonal blocks (aggregate block Jacobi, sim_aggregate.cu).
 //
 // Iteration k (standard PCG arithmetic, p_k = z_k + beta_k p_{k-1}), two phases
 // separated by grid barriers:
 //   apply    p_k is formed on the fly from z and p_{k-1} wherever it is
-//            gathered; q_e = H_elastic p_k one scalar row per thread (plain
-//            stores), the contact and friction parts are accumulated into q_c
-//            with atomics, and p_k^T H p_k is summed element by element.
+//            gathered; q_e = H_rows p_k one scalar row per thread (plain
+//            stores), the matrix-free contact and friction parts are accumulated
+//            into q_c with atomics, and p_k^T H p_k is summed element by element.
 //   update   alpha = (r,z)/(p,Hp); x += alpha p; r -= alpha (q_e + q_c); q_c = 0;
-//            z = M^-1 r; (r,z) and (r,r).
-// Each phase ends with a grid-wide sum: every block adds its block sum into a
-// triple-buffered FP64 accumulator with fire-and-forget reductions, arrives on a
-// monotone counter with release semantics and polls it with acquire loads; the
-// totals are then read from the accumulator, so every block reads the same value
-// and takes the same stop decision (the order of the additions, and so the last
-// bits of a total, may differ from run to run).  Data written by other blocks
+//            z = M^-1 r (per vertex, or per aggregate by one warp); (r,z), (r,r).
+// Each phase ends with a grid-wide sum (grid_allreduce): per-block partials, a
+// release/acquire arrival counter, and a fixed-order sum of the partials read by
+// every block, so every block takes the same stop decision.  The atomics of the
+// matrix-free constraint part add in arrival order, so the last bits of q_c (and
+// of the iterates) can differ from run to run.  Data written by other blocks
 // during the solve is read through L2 (ld.global.cg), never from a stale L1 line.
 #include <cuda_runtime.h>
 
@@ -95,6 +95,13 @@ struct PcgArgs {
     const double* fM;
     const uint8_t* proj;
     const PT* pinv;
+    // aggregate block Jacobi (nagg > 0): vertices of aggregate g at
+    // averts[avoff[g] .. avoff[g + 1]), its symmetric inverse block at ainv + aboff[g]
+    int nagg;
+    const int* avoff;
+    const int* averts;
+    const long long* aboff;
+    const PT* ainv;
     const XT* b;
     XT* x;
     XT* r;
@@ -131,10 +138,6 @@ __device__ __forceinline__ T ldcg(const T* p)
     return __ldcg(p);
 }
 
-__device__ __forceinline__ void red_add_f64(double* p, double v)
-{
-    asm volatile("red.relaxed.gpu.global.add.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
-}
 __device__ __forceinline__ void red_release_add_u32(unsigned int* p, unsigned int v)
 {
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
@@ -153,8 +156,8 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p)
 // on a monotone counter with release semantics and polls it (acquire) until every
 // block of reduction `epoch` has arrived; then warp 0 of every block adds all
 // blocks' partials in one fixed order (lane l takes blocks l, l + 32, ...; then a
-// fixed shuffle tree), so the totals are identical in every block and in every
-// run: the solver is deterministic.  part[epoch % 2] is rewritten only by
+// fixed shuffle tree), so the totals are identical in every block and do not
+// depend on the order in which blocks arrive.  part[epoch % 2] is rewritten only by
 // reduction epoch + 2, which no block can reach before every block has passed
 // reduction epoch + 1, i.e. finished reading it.  Returns false if the wait gave
 // up (err set; the kernel returns).  Warp-level sums of the thread values run in
@@ -219,6 +222,65 @@ __device__ __forceinline__ bool grid_allreduce(const AT (&v)[N], double (&out)[N
 #pragma unroll
     for (int k = 0; k < N; ++k) out[k] = res[k];
     return true;
+}
+
+// Aggregate block Jacobi, one aggregate per warp (up to 32 vertices, lane v owns
+// vertex v): rfun(j) performs the phase's update of scalar row j and returns r_j,
+// the warp stages the aggregate's r in shared memory and forms z = B r row by row
+// (B symmetric: lane `row` reads column entries of consecutive rows, coalesced);
+// z_j goes to zout[j].x.  Adds the lanes' shares of (r, z) and (r, r).
+constexpr int kAggRows = 96;
+template <typename VT, typename XT, typename PT, typename XT2, typename RF>
+__device__ __forceinline__ void agg_phase(const PcgArgs<VT, XT, PT>& a, XT2* zout, const RF& rfun, XT& rz, XT& rr)
+{
+    __shared__ XT rs[kPcgThreads / 32][kAggRows];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    for (int g = blockIdx.x * (blockDim.x >> 5) + wib; g < a.nagg; g += nw) {
+        const int v0 = __ldg(a.avoff + g), sv = __ldg(a.avoff + g + 1) - v0, m = 3 * sv;
+        if (lane < sv) {
+            const int i = __ldg(a.averts + v0 + lane);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const XT r = rfun(3 * i + c);
+                rs[wib][3 * lane + c] = r;
+                rr += r * r;
+            }
+        }
+        __syncwarp();
+        const PT* B = a.ainv + __ldg(a.aboff + g);
+        for (int row = lane; row < m; row += 32) {
+            // twelve independent loads in flight per step: the blocks are read
+            // from L2 and the loop is latency-bound otherwise
+            const PT* Bc = B + row;
+            XT z0 = 0, z1 = 0, z2 = 0, z3 = 0;
+            int c = 0;
+            for (; c + 12 <= m; c += 12) {
+                PT b[12];
+#pragma unroll
+                for (int u = 0; u < 12; ++u) b[u] = __ldg(Bc + (size_t)(c + u) * m);
+#pragma unroll
+                for (int u = 0; u < 12; u += 4) {
+                    z0 += (XT)b[u] * rs[wib][c + u];
+                    z1 += (XT)b[u + 1] * rs[wib][c + u + 1];
+                    z2 += (XT)b[u + 2] * rs[wib][c + u + 2];
+                    z3 += (XT)b[u + 3] * rs[wib][c + u + 3];
+                }
+            }
+            for (; c < m; c += 3) {
+                const PT b0 = __ldg(Bc + (size_t)c * m), b1 = __ldg(Bc + (size_t)(c + 1) * m),
+                         b2 = __ldg(Bc + (size_t)(c + 2) * m);
+                z0 += (XT)b0 * rs[wib][c];
+                z1 += (XT)b1 * rs[wib][c + 1];
+                z2 += (XT)b2 * rs[wib][c + 2];
+            }
+            const XT z = (z0 + z1) + (z2 + z3);
+            const int i = __ldg(a.averts + v0 + row / 3);
+            zout[3 * i + row % 3].x = z;
+            rz += rs[wib][row] * z;
+        }
+        __syncwarp();
+    }
 }
 
 // z = M^-1 r for vertex i
@@ -368,7 +430,24 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     // r = b, x = 0, q_c = 0, z = M^-1 r
     double tot[2];
-    {
+    if (a.nagg > 0) {
+        XT rz0 = 0, rr0 = 0;
+        agg_phase(
+            a, a.zp[0],
+            [&](int j) {
+                const XT r = a.b[j];
+                a.r[j] = r;
+                a.x[j] = 0;
+                a.qc[j] = 0;
+                return r;
+            },
+            rz0, rr0);
+        const XT v0[2] = {rz0, rr0};
+        double v[2];
+        if (!grid_allreduce<2>(v0, v, d, epoch, a.wait_polls, a.part)) return;
+        tot[0] = v[0];
+        tot[1] = v[1];
+    } else {
         double v[2] = {0, 0};
         for (int i = gtid; i < a.nv; i += gstride) {
             XT r[3], z[3];
@@ -426,6 +505,18 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
         }
         const XT alpha = (XT)(rz / pq);
         XT rz_t = 0, rr_t = 0;
+        if (a.nagg > 0)
+            agg_phase(
+                a, zp_next,
+                [&](int j) {
+                    a.x[j] = ldcg(a.x + j) + alpha * ldcg(&zp_next[j].y);
+                    const XT r = ldcg(a.r + j) - alpha * (ldcg(a.qe + j) + ldcg(a.qc + j));
+                    a.r[j] = r;
+                    a.qc[j] = 0;
+                    return r;
+                },
+                rz_t, rr_t);
+        else
         for (int i = gtid; i < a.nv; i += gstride) {
             XT r[3], z[3];
 #pragma unroll
@@ -582,6 +673,14 @@ int solve(Sim* s, const XT* b, XT* x, double tol, int maxit, int* iters, double*
     a.maxit = maxit;
     a.ncon = s->prm.withCollision ? s->ncon : 0;
     a.nfric = (s->prm.withCollision && s->prm.mu > 0) ? s->nfric : 0;
+    if (s->prm.precond == 2 && s->agg_ready) {
+        const AggView av = agg_view(s);
+        a.nagg = av.nagg;
+        a.avoff = av.voff;
+        a.averts = av.verts;
+        a.aboff = av.boff;
+        a.ainv = reinterpret_cast<const PT*>(av.inv);
+    }
     if (s->folded) {
         a.clist = s->crest.p;
         a.flist = s->frest.p;

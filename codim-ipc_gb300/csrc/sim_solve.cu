@@ -360,12 +360,31 @@ int linear_solve(Sim* s, const double* rhs, double* sol, int* iters)
         const int frc = fold_constraints(s);
         if (frc) return frc;
     }
+    // aggregate block Jacobi: the inverses of the aggregates' diagonal blocks of
+    // this system (after folding); a block that is not positive definite in the
+    // solver's precision leaves the solve to block Jacobi
+    s->agg_ready = false;
+    bool aggregate = false;
+    if (s->prm.precond == 2) {
+        const int arc = agg_setup(s);
+        if (arc && arc != CIPC_ERR_NOT_CONVERGED) return arc;
+        aggregate = arc == CIPC_OK;
+        if (!aggregate) ++s->solve_fallbacks;
+    }
     int total = 0, it = 0;
     const int maxit = s->prm.pcg_maxit;
     if (learned) s->prm.pcg_maxit = std::min(maxit, std::max(100, 3 * s->bj_last_iters));
     int rc = solve_with_precond(s, rhs, sol, &it);
     s->prm.pcg_maxit = maxit;
     total += it;
+    if (aggregate && (rc == CIPC_ERR_NOT_CONVERGED || rc == CIPC_ERR_NAN)) {
+        // breakdown with the aggregate inverses (an FP32 inverse can lose
+        // definiteness): block Jacobi solves the same system
+        ++s->solve_fallbacks;
+        s->agg_ready = false;
+        rc = solve_with_precond(s, rhs, sol, &it);
+        total += it;
+    }
     if (learned) {
         ++s->solve_learned;
         if (rc == CIPC_ERR_NOT_CONVERGED || rc == CIPC_ERR_NAN) {

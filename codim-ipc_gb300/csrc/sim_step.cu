@@ -773,6 +773,11 @@ void sim_destroy(Sim* s)
     if (!s) return;
     cudaStreamSynchronize(s->stream);
     pcg_release(s);
+    agg_release(s);
+    s->hval_op.release();
+    s->crest.release();
+    s->frest.release();
+    s->fold_cnt.release();
     for (DBuf<int>* b : {&s->tri, &s->hinge, &s->bnode, &s->bedge, &s->btri, &s->dbc_idx, &s->col,
                          &s->diag, &s->tri_slot, &s->hinge_slot, &s->ckind, &s->cmult, &s->fkind, &s->fmult,
                          &s->rseg, &s->rhinge, &s->rseg_slot, &s->rhinge_slot, &s->tet, &s->tet_slot,
@@ -1070,7 +1075,8 @@ static int step_entry(cipc_sim* h, const cipc_step_params* p, cipc_step_stats* s
 {
     if (int rc = check_sim(h)) return rc;
     if (!p || !(p->h > 0) || !(p->dhat2 > 0) || !(p->xi >= 0) || !(p->newton_tol > 0) ||
-        (p->precision != CIPC_PRECISION_FP64 && p->precision != CIPC_PRECISION_MIXED))
+        (p->precision != CIPC_PRECISION_FP64 && p->precision != CIPC_PRECISION_MIXED) ||
+        p->preconditioner < CIPC_PRECOND_BLOCK_JACOBI || p->preconditioner > CIPC_PRECOND_AGGREGATE)
         return set_error(CIPC_ERR_INVALID_ARG, "cipc_sim_step: bad parameters");
     Sim* s = h->s;
     const int old_prec = s->prm.precision;

@@ -52,6 +52,9 @@ extern "C" {
 #define CIPC_PRECISION_MIXED 1
 #define CIPC_BARRIER_OFFSET 0  /* offset IPC (C-IPC): barrier on d^2 - xi^2 */
 #define CIPC_BARRIER_ELASTIC 1 /* elastic IPC: no offset, barrier normalised by dhat */
+#define CIPC_PRECOND_BLOCK_JACOBI 0
+#define CIPC_PRECOND_LEARNED 1
+#define CIPC_PRECOND_AGGREGATE 2
 
 #define CIPC_MEM_HOST 0
 #define CIPC_MEM_DEVICE 1
@@ -175,7 +178,11 @@ typedef struct cipc_step_params {
     int precision;         /* CIPC_PRECISION_FP64 or CIPC_PRECISION_MIXED */
     double pcg_tol;        /* relative residual of each Newton system (0 = 1e-6) */
     int pcg_max_iters;     /* 0 = 10000 */
-    int preconditioner;    /* 0 block-Jacobi, 1 learned correction when a model is set */
+    int preconditioner;    /* CIPC_PRECOND_BLOCK_JACOBI (0), CIPC_PRECOND_LEARNED (1: the
+                              learned correction when a model is set, else block Jacobi) or
+                              CIPC_PRECOND_AGGREGATE (2: exact inverses of the diagonal blocks
+                              of vertex aggregates of up to 32 mesh neighbours; block Jacobi
+                              for a system where one is not positive definite) */
     int forcing;           /* 0: every Newton system to pcg_tol; 1: inexact Newton, the
                               Eisenstat-Walker forcing term (choice 2, gamma 0.9, alpha 2)
                               clamped to [pcg_tol, 0.1], pcg_tol once RMS(step)/h < 10 tol;

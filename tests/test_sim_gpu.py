@@ -107,8 +107,9 @@ def test_ccd_step_size_matches(cuda, trajectory):
         assert abs(ag - ao) <= 1e-12 * max(ao, 1e-300), (k, ag, ao)
 
 
-@pytest.mark.parametrize("nh", [True, False])
-def test_steps_match_direct_solve(cuda, orc, nh):
+@pytest.mark.parametrize("nh,precond", [(True, F.PRECOND_BLOCK_JACOBI), (False, F.PRECOND_BLOCK_JACOBI),
+                                        (True, F.PRECOND_AGGREGATE)])
+def test_steps_match_direct_solve(cuda, orc, nh, precond):
     """Single steps from the oracle's states: GPU positions within 1e-8 of the
     bounding-box diagonal of the oracle's direct-solve Newton after the same
     number of Newton iterations.  The oracle stops at a Newton tolerance of 1e-7;
@@ -121,7 +122,9 @@ def test_steps_match_direct_solve(cuda, orc, nh):
     so on long contact steps (60+ iterations, 100+ line-search halvings decided on
     FP64 energy differences) two GPU runs from the same state can themselves end
     ~1e-8 apart: each step is run twice and the bar is 1e-8 of the diagonal plus
-    twice that measured spread (exactly 1e-8 when the runs agree)."""
+    twice that measured spread (exactly 1e-8 when the runs agree).  The linear
+    solves run with block Jacobi and with the aggregate block-Jacobi preconditioner:
+    a preconditioner changes iteration counts, not the solution."""
     X, T, dbc = scene(n=8, y=-0.095)
     sh = orc.Shell(X, T, **MAT, nh=nh)
     k2o, dhat2 = sh.init_oipc(DHAT)
@@ -136,7 +139,8 @@ def test_steps_match_direct_solve(cuda, orc, nh):
         x_start, v_start, k_start = xo.copy(), vo.copy(), k2o.copy()
         rc, sto = sh.step(xo, vo, k2o, dbc, X[dbc], DT, dhat2, XI, tol=1e-7, max_iter=400)
         assert rc == 0
-        prm = F.make_params(DT, dhat2, XI, newton_tol=1e-30, pcg_tol=1e-12, max_newton_iters=sto["newton_iters"])
+        prm = F.make_params(DT, dhat2, XI, newton_tol=1e-30, pcg_tol=1e-12, max_newton_iters=sto["newton_iters"],
+                            preconditioner=precond)
         xs = []
         for rerun in range(2):
             s.set_state(x_start, v_start)
