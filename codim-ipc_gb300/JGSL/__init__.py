@@ -659,9 +659,14 @@ def _advance(elastic, split, a):
     if out:
         os.makedirs(out, exist_ok=True)
         _F.sim_set_output(sim, out)
+    # the GPU path's own choices, set by Set_Parameter: precision ("fp64" or
+    # "mixed") and preconditioner (0 block Jacobi, 2 aggregate block Jacobi)
+    prec = _F.MIXED if str(Get_Parameter("cipc_precision", "fp64")) == "mixed" else _F.FP64
+    pre = int(Get_Parameter("cipc_preconditioner", _F.PRECOND_BLOCK_JACOBI))
     prm = _F.make_params(float(a["dt"]), float(a["dHat2"]), float(a["thickness"]), mu=float(a["mu"]),
                          epsv2=float(a["epsv2"]), fric_iters=int(a["fricIterAmt"]), newton_tol=float(a["PNTol"]),
-                         with_collision=bool(a["withCollision"]), elastic_ipc=elastic)
+                         with_collision=bool(a["withCollision"]), elastic_ipc=elastic, precision=prec,
+                         preconditioner=pre)
     if elastic:
         sim.set_kappa(float(kappa[0]), float(kappa[0]))
     st = (sim.step_split if split else sim.step)(prm, allow=(_F.CIPC_ERR_NOT_CONVERGED,))
