@@ -586,7 +586,7 @@ def trace_scene(args):
     s = F.Sim(X, T, 200.0, 1e5, 0.3, 1e-3)
     _, dhat2 = s.init_oipc(1e-3)
     prm = F.make_params(0.02, dhat2, 5e-4, mu=0.4, epsv2=1e-6, fric_iters=1, newton_tol=1e-3, precision=prec,
-                        pcg_tol=1e-4)
+                        pcg_tol=1e-4, preconditioner=args.trace_precond)
     for k in range(args.trace_steps):
         s.set_dbc(dbc, workloads.rotate_y(X[dbc], c, 2.0 * 0.02 * (k + 1)))
         st = s.step(prm, allow=(F.CIPC_ERR_NOT_CONVERGED,))
@@ -783,6 +783,8 @@ def main():
                     help="only step the cloth-on-sphere scene at this resolution (profiling workload)")
     ap.add_argument("--trace-steps", type=int, default=12)
     ap.add_argument("--trace-precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--trace-precond", type=int, default=0, choices=[0, 2],
+                    help="preconditioner of the traced steps (0 block Jacobi, 2 aggregate block Jacobi)")
     ap.add_argument("--c1-steps", type=int, default=50, help="steps of the cloth-on-cube scene")
     ap.add_argument("--c1-cpu-steps", type=int, default=8, help="cloth-on-cube steps run by the CPU oracle")
     ap.add_argument("--sc-steps", type=int, default=10, help="steps of the codimensional and stacked scenes")
