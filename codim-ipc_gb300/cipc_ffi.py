@@ -258,7 +258,7 @@ class StepStats(ctypes.Structure):
     _fields_ = [("newton_iters", ctypes.c_int), ("pcg_iters", ctypes.c_int), ("line_search_trials", ctypes.c_int),
                 ("n_constraints", ctypes.c_int), ("status", ctypes.c_int), ("min_dist2", ctypes.c_double),
                 ("kappa", ctypes.c_double), ("ms", ctypes.c_double), ("precond_fallbacks", ctypes.c_int),
-                ("learned_solves", ctypes.c_int)]
+                ("learned_solves", ctypes.c_int), ("solve_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -94,6 +94,7 @@ struct StepStats {
     double ms = 0;
     int precond_fallbacks = 0;
     int learned_solves = 0;
+    double solve_ms = 0;      // device time of the PCG kernels
 };
 
 struct Sim {
@@ -189,6 +190,7 @@ struct Sim {
     void* learned = nullptr;
     void* capture = nullptr;
     int solve_fallbacks = 0, solve_learned = 0;  // counts of the current step
+    double solve_ms = 0;                         // device time of the current step's PCG kernels
     int bj_last_iters = 0;                       // iterations of the step's latest block-Jacobi solve (0: none yet)
     double solve_tol = 0;                        // relative tolerance of the next linear solve (0: prm.pcg_tol)
     std::vector<double> host_mass;

@@ -571,10 +571,13 @@ struct PcgState {
     DBuf<PcgScalars> dsc;        // device scalars
     DBuf<double> part;           // block partial sums of the grid reductions
     PcgScalars* host = nullptr;  // pinned copy of the results
+    cudaEvent_t ev[2] = {nullptr, nullptr};  // around each launch: the solve's device time
     int grid[2] = {0, 0};        // co-resident grid per precision (0 FP64, 1 FP32)
     ~PcgState()
     {
         if (host) cudaFreeHost(host);
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
         vec.release();
         dsc.release();
         part.release();
@@ -608,7 +611,8 @@ int state(Sim* s, PcgState** out)
     if (!s->pcg) {
         PcgState* st = new PcgState();
         if (st->dsc.alloc(1) != cudaSuccess || cudaMemset(st->dsc.p, 0, sizeof(PcgScalars)) != cudaSuccess ||
-            cudaMallocHost((void**)&st->host, sizeof(PcgScalars)) != cudaSuccess) {
+            cudaMallocHost((void**)&st->host, sizeof(PcgScalars)) != cudaSuccess ||
+            cudaEventCreate(&st->ev[0]) != cudaSuccess || cudaEventCreate(&st->ev[1]) != cudaSuccess) {
             delete st;
             return set_error(CIPC_ERR_CUDA, "PCG state allocation");
         }
@@ -694,12 +698,16 @@ int solve(Sim* s, const XT* b, XT* x, double tol, int maxit, int* iters, double*
     // barrier state starts clear (a previous solve may have given up mid-way)
     cudaError_t e = cudaMemsetAsync(st->dsc.p, 0, sizeof(PcgScalars), str);
     void* args[] = {&a};
+    if (e == cudaSuccess) e = cudaEventRecord(st->ev[0], str);
     if (e == cudaSuccess)
         e = cudaLaunchCooperativeKernel((const void*)k_pcg_solve<VT, XT, PT>, dim3(g), dim3(kPcgThreads), args, 0,
                                         str);
+    if (e == cudaSuccess) e = cudaEventRecord(st->ev[1], str);
     if (e == cudaSuccess) e = cudaMemcpyAsync(st->host, st->dsc.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, str);
     if (e == cudaSuccess) e = cudaStreamSynchronize(str);
     if (e != cudaSuccess) return set_cuda_error(e, "PCG");
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, st->ev[0], st->ev[1]) == cudaSuccess) s->solve_ms += ms;
     const PcgScalars* h = st->host;
     *iters = h->it;
     *rel = h->bb > 0 ? std::sqrt(h->rr / h->bb) : 0.0;

@@ -243,9 +243,9 @@ static void log_step(Sim* s, const StepStats& S, bool with_collision)
     log_line(s, "steps.jsonl",
              "{\"step\": %d, \"newton_iters\": %d, \"pcg_iters\": %d, \"line_search_trials\": %d, "
              "\"n_constraints\": %d, \"status\": %d, \"min_dist2\": %.17g, \"kappa\": %.17g, \"ms\": %.3f, "
-             "\"precond_fallbacks\": %d, \"learned_solves\": %d}\n",
+             "\"precond_fallbacks\": %d, \"learned_solves\": %d, \"solve_ms\": %.3f}\n",
              s->step_count, S.newton_iters, S.pcg_iters, S.line_search_trials, S.n_constraints, S.status, S.min_dist2,
-             S.kappa, S.ms, S.precond_fallbacks, S.learned_solves);
+             S.kappa, S.ms, S.precond_fallbacks, S.learned_solves, S.solve_ms);
 }
 
 // 1 in *flag when some entry is NaN or infinite
@@ -295,6 +295,7 @@ int sim_step(Sim* s, StepStats* st)
     StepStats S;
     s->solve_fallbacks = 0;
     s->solve_learned = 0;
+    s->solve_ms = 0;
     s->bj_last_iters = 0;  // the step's first solve is block Jacobi: a fresh yardstick
     s->sl_have_prev = false;  // strain history is per step (IMPLICIT_EULER.h:444)
     const SimParams& P = s->prm;
@@ -565,6 +566,7 @@ int sim_step(Sim* s, StepStats* st)
     S.ms = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
     S.precond_fallbacks = s->solve_fallbacks;
     S.learned_solves = s->solve_learned;
+    S.solve_ms = s->solve_ms;
     if (s->trace)
         std::fprintf(stderr,
                      "cipc step: %.2f ms  setup %.2f  sets %.2f  fbasis %.2f  energy %.2f  gradhess %.2f  solve %.2f  "
@@ -626,6 +628,7 @@ int sim_step_split(Sim* s, StepStats* st)
     } restore{s};
     s->solve_fallbacks = 0;
     s->solve_learned = 0;
+    s->solve_ms = 0;
     s->bj_last_iters = 0;
     s->dbc_stiff = 0;
     double dbcPenaltyXn = 0;
@@ -763,6 +766,7 @@ int sim_step_split(Sim* s, StepStats* st)
     S.ms = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
     S.precond_fallbacks = s->solve_fallbacks;
     S.learned_solves = s->solve_learned;
+    S.solve_ms = s->solve_ms;
     if (!s->out_dir.empty()) log_step(s, S, P.withCollision != 0);
     *st = S;
     return rc;
@@ -1096,6 +1100,7 @@ static int step_entry(cipc_sim* h, const cipc_step_params* p, cipc_step_stats* s
         stats->ms = S.ms;
         stats->precond_fallbacks = S.precond_fallbacks;
         stats->learned_solves = S.learned_solves;
+        stats->solve_ms = S.solve_ms;
     }
     return rc;
 }

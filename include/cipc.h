@@ -212,6 +212,8 @@ typedef struct cipc_step_stats {
     double ms;              /* wall time of the step */
     int precond_fallbacks;  /* linear solves where the learned preconditioner stalled and block Jacobi re-solved */
     int learned_solves;     /* linear solves that used the learned preconditioner */
+    double solve_ms;        /* device time of the step's PCG kernels (CUDA events on the
+                               simulation's stream around each launch) */
 } cipc_step_stats;
 
 typedef struct cipc_sim cipc_sim;
