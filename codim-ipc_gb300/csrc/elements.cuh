@@ -348,4 +348,107 @@ CIPC_HD void dihedral_hess(const d3 (&x)[4], double (&H)[12][12])
         }
 }
 
+// Hessian of theta (12x12) in T from the hinge's edge vectors (taken in FP64 by
+// the caller: e0 = x2 - x1, e1 = x0 - x1, e2 = x3 - x1, e3 = x0 - x2, e4 = x3 - x2),
+// the same expressions as dihedral_hess: the FP32 form for the mixed-precision
+// Hessians, whose FP64 form is GB300-FP64-pipe bound
+template <typename T>
+CIPC_HD void dihedral_hess_t(const T (&E)[5][3], T (&H)[12][12])
+{
+    auto crs = [](const T* a, const T* b, T* o) {
+        o[0] = a[1] * b[2] - a[2] * b[1];
+        o[1] = a[2] * b[0] - a[0] * b[2];
+        o[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    auto dt = [](const T* a, const T* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+    const T *e0 = E[0], *e1 = E[1], *e2 = E[2], *e3 = E[3], *e4 = E[4];
+    T nA[3], nB[3];
+    crs(e0, e1, nA);
+    crs(e2, e0, nB);
+    const T nAs = dt(nA, nA), nBs = dt(nB, nB), e0n = sqrt(dt(e0, e0));
+#pragma unroll
+    for (int i = 0; i < 12; ++i)
+#pragma unroll
+        for (int j = 0; j < 12; ++j) H[i][j] = 0;
+    auto skewm = [](const T* v, T (&S)[3][3], T s) {
+        S[0][0] = 0; S[0][1] = -v[2] * s; S[0][2] = v[1] * s;
+        S[1][0] = v[2] * s; S[1][1] = 0; S[1][2] = -v[0] * s;
+        S[2][0] = -v[1] * s; S[2][1] = v[0] * s; S[2][2] = 0;
+    };
+    T Dn1[4][3][3], Dn2[4][3][3];
+    {
+        T A[3][3], B[3][3];
+        skewm(e0, Dn1[0], T(1));
+        skewm(e1, Dn1[2], T(-1));
+        skewm(e0, A, T(-1));
+        skewm(e1, B, T(1));
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                Dn1[1][i][j] = A[i][j] + B[i][j];
+                Dn1[3][i][j] = 0;
+            }
+        skewm(e0, Dn2[3], T(-1));
+        skewm(e2, Dn2[2], T(1));
+        skewm(e0, A, T(1));
+        skewm(e2, B, T(-1));
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                Dn2[1][i][j] = A[i][j] + B[i][j];
+                Dn2[0][i][j] = 0;
+            }
+    }
+    T Du1[4][3][3], Du2[4][3][3];
+    const T iA = T(1) / nAs, iB = T(1) / nBs;
+    for (int v = 0; v < 4; ++v)
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                T t1 = 0, t2 = 0;
+                for (int k = 0; k < 3; ++k) {
+                    t1 += nA[k] * Dn1[v][k][j];
+                    t2 += nB[k] * Dn2[v][k][j];
+                }
+                Du1[v][i][j] = Dn1[v][i][j] * iA - 2 * nA[i] * t1 * iA * iA;
+                Du2[v][i][j] = Dn2[v][i][j] * iB - 2 * nB[i] * t2 * iB * iB;
+            }
+    const T u1[3] = {nA[0] * iA, nA[1] * iA, nA[2] * iA}, u2[3] = {nB[0] * iB, nB[1] * iB, nB[2] * iB};
+    const T ie0 = T(1) / e0n;
+    const T ue0[3] = {e0[0] * ie0, e0[1] * ie0, e0[2] * ie0};
+    auto ratio_grad = [&](const T* w, int a, int b, T (&gs)[12]) {
+        for (int k = 0; k < 12; ++k) gs[k] = 0;
+        const T ew = dt(e0, w);
+        for (int d = 0; d < 3; ++d) {
+            const T de0 = w[d] * ie0 - ue0[d] * ew * ie0 * ie0;
+            gs[6 + d] += de0;
+            gs[3 + d] -= de0;
+            const T dw = e0[d] * ie0;
+            gs[3 * a + d] += dw;
+            gs[3 * b + d] -= dw;
+        }
+    };
+    auto add_term = [&](int row, T sc, const T* gsv, const T (&u)[3], const T (&Du)[4][3][3]) {
+        for (int i = 0; i < 3; ++i)
+            for (int v = 0; v < 4; ++v)
+                for (int j = 0; j < 3; ++j) H[3 * row + i][3 * v + j] += u[i] * gsv[3 * v + j] + sc * Du[v][i][j];
+    };
+    T gs[12];
+    T mge0[12] = {0, 0, 0, ue0[0], ue0[1], ue0[2], -ue0[0], -ue0[1], -ue0[2], 0, 0, 0};
+    add_term(0, -e0n, mge0, u1, Du1);
+    add_term(3, -e0n, mge0, u2, Du2);
+    ratio_grad(e3, 0, 2, gs);
+    for (int k = 0; k < 12; ++k) gs[k] = -gs[k];
+    add_term(1, -dt(e0, e3) * ie0, gs, u1, Du1);
+    ratio_grad(e4, 3, 2, gs);
+    for (int k = 0; k < 12; ++k) gs[k] = -gs[k];
+    add_term(1, -dt(e0, e4) * ie0, gs, u2, Du2);
+    ratio_grad(e1, 0, 1, gs);
+    add_term(2, dt(e0, e1) * ie0, gs, u1, Du1);
+    ratio_grad(e2, 3, 1, gs);
+    add_term(2, dt(e0, e2) * ie0, gs, u2, Du2);
+    for (int i = 0; i < 12; ++i)
+        for (int j = i + 1; j < 12; ++j) {
+            const T s = T(0.5) * (H[i][j] + H[j][i]);
+            H[i][j] = H[j][i] = s;
+        }
+}
+
 }  // namespace cipc
