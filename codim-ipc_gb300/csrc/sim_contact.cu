@@ -88,13 +88,23 @@ static void scan_exclusive(const int* in, int* out, int n, int* tmp, cudaStream_
 // ---------------------------------------------------------------------------
 // hash grid
 // ---------------------------------------------------------------------------
+// One (cell, item) entry of the grid, sorted by bucket: everything a query needs
+// to test the item is in this 64-byte record (one cache line, read with four
+// 16-byte loads and no dependent gather): the item id, its cell range (for the
+// once-per-pair test) and its FP32 box (for the prefilter; zero when the grid
+// was built without boxes)
+struct __align__(16) GridEntry {
+    int4 a;    // item, lo x, lo y, lo z
+    int4 b;    // hi x, hi y, hi z, -
+    float4 c;  // box lo x, lo y, lo z, hi x
+    float4 d;  // box hi y, hi z, -, -
+};
+
 struct Grid {
-    double inv;       // 1 / cell size
-    unsigned mask;    // bucket count - 1
-    const int* lo;    // 3 per item: cell range
-    const int* hi;
-    const int* bstart;  // bucket start (mask + 2 entries)
-    const int* items;   // item ids sorted by bucket
+    double inv;              // 1 / cell size
+    unsigned mask;           // bucket count - 1
+    const int* bstart;       // bucket start (mask + 2 entries)
+    const GridEntry* ent;    // entries sorted by bucket
 };
 
 __device__ __forceinline__ unsigned cell_hash(int i, int j, int k, unsigned mask)
@@ -177,12 +187,24 @@ __global__ void k_item_emit(int n, const int* lo, const int* hi, const int* off,
 }
 
 __global__ void k_bucket_scatter(int ne, const unsigned* ebucket, const int* eitem, const int* bstart, int* cursor,
-                                 int* items)
+                                 const int* lo, const int* hi, const float* box, GridEntry* ent)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ne) return;
     const unsigned b = ebucket[e];
-    items[bstart[b] + atomicAdd(cursor + b, 1)] = eitem[e];
+    const int t = eitem[e];
+    GridEntry g;
+    g.a = make_int4(t, lo[3 * t], lo[3 * t + 1], lo[3 * t + 2]);
+    g.b = make_int4(hi[3 * t], hi[3 * t + 1], hi[3 * t + 2], 0);
+    if (box) {
+        const float* q = box + 6 * (size_t)t;
+        g.c = make_float4(q[0], q[1], q[2], q[3]);
+        g.d = make_float4(q[4], q[5], 0.f, 0.f);
+    } else {
+        g.c = make_float4(0.f, 0.f, 0.f, 0.f);
+        g.d = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    ent[bstart[b] + atomicAdd(cursor + b, 1)] = g;
 }
 
 // simple bump allocator over the sim scratch buffer
@@ -208,9 +230,10 @@ static int ensure_scratch(Sim* s, size_t bytes)
 
 static size_t grid_bytes(int n, int cells_per_item);
 
-// Builds a grid over n items; returns the Grid view (valid until the arena is reused)
+// Builds a grid over n items (box: their FP32 boxes, 6 per item, copied into the
+// entries; may be null); returns the Grid view (valid until the arena is reused)
 static int build_grid(Sim* s, Arena& ar, int n, int nvi, const int* verts, const double* x, const double* dir,
-                      double alpha, Grid& G)
+                      double alpha, const float* box, Grid& G)
 {
     cudaStream_t st = s->stream;
     const double inv = 1.0 / s->cell;
@@ -233,13 +256,8 @@ static int build_grid(Sim* s, Arena& ar, int n, int nvi, const int* verts, const
     cudaStreamSynchronize(st);
     if (hw > kMaxGridEntries) return kSpanTooLarge;  // before the int scan could overflow
     scan_exclusive(cnt, off, std::max(n, 1), tmp, st);
-    int total = 0;
-    cudaMemcpyAsync(&total, off + std::max(n, 1), sizeof(int), cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);
-    if (ar.used > ar.cap) {
-        s->scratch_bytes = 2 * ar.used;
-        return kNeedScratch;
-    }
+    // every item's count is below the cap here, so the scanned total is hw
+    const int total = (int)hw;
     unsigned nb = 1024;
     while (nb < 2u * (unsigned)std::max(total, 1)) nb <<= 1;
     unsigned* eb = ar.take<unsigned>((size_t)total + 1);
@@ -247,7 +265,7 @@ static int build_grid(Sim* s, Arena& ar, int n, int nvi, const int* verts, const
     int* bcount = ar.take<int>((size_t)nb + 1);
     int* bstart = ar.take<int>((size_t)nb + 2);
     int* cursor = ar.take<int>((size_t)nb + 1);
-    int* items = ar.take<int>((size_t)total + 1);
+    GridEntry* ent = ar.take<GridEntry>((size_t)total + 1);
     int* tmp2 = ar.take<int>(2 * ((size_t)nb / 1024 + 8) + 64);
     if (ar.used > ar.cap) {
         s->scratch_bytes = ar.used + ar.used / 2;
@@ -257,13 +275,12 @@ static int build_grid(Sim* s, Arena& ar, int n, int nvi, const int* verts, const
     cudaMemsetAsync(cursor, 0, sizeof(int) * (nb + 1), st);
     if (n > 0) k_item_emit<<<nblk(n, 256), 256, 0, st>>>(n, lo, hi, off, nb - 1, eb, ei, bcount);
     scan_exclusive(bcount, bstart, (int)nb, tmp2, st);
-    if (total > 0) k_bucket_scatter<<<nblk(total, 256), 256, 0, st>>>(total, eb, ei, bstart, cursor, items);
+    if (total > 0)
+        k_bucket_scatter<<<nblk(total, 256), 256, 0, st>>>(total, eb, ei, bstart, cursor, lo, hi, box, ent);
     G.inv = inv;
     G.mask = nb - 1;
-    G.lo = lo;
-    G.hi = hi;
     G.bstart = bstart;
-    G.items = items;
+    G.ent = ent;
     return CIPC_OK;
 }
 
@@ -282,7 +299,7 @@ static size_t grid_bytes(int n, int cells_per_item)
     size_t total = (size_t)n * cells_per_item + 16;
     size_t nb = 1024;
     while (nb < 2 * total) nb <<= 1;
-    return 4 * (size_t)(10 * n + 4 * total + 4 * nb) + (1 << 16);
+    return 4 * (size_t)(10 * n + 4 * total + 4 * nb) + sizeof(GridEntry) * (total + 1) + (1 << 16);
 }
 
 // ---------------------------------------------------------------------------
@@ -385,7 +402,8 @@ __device__ __forceinline__ bool any_gt3(d3 a, double d) { return a.x > d || a.y 
 __device__ __forceinline__ d3 vmin3(d3 a, d3 b) { return mk(fmin(a.x, b.x), fmin(a.y, b.y), fmin(a.z, b.z)); }
 __device__ __forceinline__ d3 vmax3(d3 a, d3 b) { return mk(fmax(a.x, b.x), fmax(a.y, b.y), fmax(a.z, b.z)); }
 
-// iterate the candidates of a query cell range [ql, qh]; calls f(item) once per pair
+// iterate the candidates of a query cell range [ql, qh]; calls f(item, box) once
+// per pair, box = the item's FP32 box from its grid entry
 template <typename F>
 __device__ __forceinline__ void grid_query(const Grid& G, const int (&ql)[3], const int (&qh)[3], F&& f)
 {
@@ -393,14 +411,17 @@ __device__ __forceinline__ void grid_query(const Grid& G, const int (&ql)[3], co
         for (int j = ql[1]; j <= qh[1]; ++j)
             for (int k = ql[2]; k <= qh[2]; ++k) {
                 const unsigned b = cell_hash(i, j, k, G.mask);
-                for (int e = G.bstart[b]; e < G.bstart[b + 1]; ++e) {
-                    const int t = G.items[e];
-                    const int l0 = G.lo[3 * t], l1 = G.lo[3 * t + 1], l2 = G.lo[3 * t + 2];
-                    if (i < l0 || j < l1 || k < l2) continue;
-                    if (i > G.hi[3 * t] || j > G.hi[3 * t + 1] || k > G.hi[3 * t + 2]) continue;
+                const int e1 = __ldg(G.bstart + b + 1);
+                for (int e = __ldg(G.bstart + b); e < e1; ++e) {
+                    const GridEntry* g = G.ent + e;
+                    const int4 A = __ldg(&g->a), B = __ldg(&g->b);
+                    const float4 C = __ldg(&g->c), D = __ldg(&g->d);
+                    if (i < A.y || j < A.z || k < A.w) continue;
+                    if (i > B.x || j > B.y || k > B.z) continue;
                     // first cell of the intersection of both ranges
-                    if (i != max(ql[0], l0) || j != max(ql[1], l1) || k != max(ql[2], l2)) continue;
-                    f(t);
+                    if (i != max(ql[0], A.y) || j != max(ql[1], A.z) || k != max(ql[2], A.w)) continue;
+                    const float bx[6] = {C.x, C.y, C.z, C.w, D.x, D.y};
+                    f(A.x, bx);
                 }
             }
 }
@@ -420,8 +441,8 @@ __global__ void k_cs_pt(CsArgs a)
     qh[2] = cellc(p.z + a.dHat, a.G.inv);
     const float pb[6] = {__double2float_rd(p.x), __double2float_rd(p.y), __double2float_rd(p.z),
                          __double2float_ru(p.x), __double2float_ru(p.y), __double2float_ru(p.z)};
-    grid_query(a.G, ql, qh, [&](int t) {
-        if (box_apart(pb, a.tbox + 6 * (size_t)t, a.dHat_f)) return;
+    grid_query(a.G, ql, qh, [&](int t, const float (&bx)[6]) {
+        if (box_apart(pb, bx, a.dHat_f)) return;
         const int t0i = a.btri[3 * t], t1i = a.btri[3 * t + 1], t2i = a.btri[3 * t + 2];
         if (vI == t0i || vI == t1i || vI == t2i) return;
         if (a.dbc[vI] && a.dbc[t0i] && a.dbc[t1i] && a.dbc[t2i]) return;
@@ -458,9 +479,9 @@ __global__ void k_cs_ee(CsArgs a)
     float eb[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) eb[k] = a.ebox[6 * (size_t)eI + k];
-    grid_query(a.G, ql, qh, [&](int eJ) {
+    grid_query(a.G, ql, qh, [&](int eJ, const float (&bx)[6]) {
         if (eJ <= eI) return;
-        if (box_apart(eb, a.ebox + 6 * (size_t)eJ, a.dHat_f)) return;
+        if (box_apart(eb, bx, a.dHat_f)) return;
         const int b0 = a.bedge[2 * eJ], b1 = a.bedge[2 * eJ + 1];
         if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
         if (a.dbc[a0] && a.dbc[a1] && a.dbc[b0] && a.dbc[b1]) return;
@@ -560,7 +581,7 @@ __global__ void k_cs_codim_pe(CsArgs a, int sv_begin, int e_begin)
     qh[0] = cellc(p.x + a.dHat, a.G.inv);
     qh[1] = cellc(p.y + a.dHat, a.G.inv);
     qh[2] = cellc(p.z + a.dHat, a.G.inv);
-    grid_query(a.G, ql, qh, [&](int el) {
+    grid_query(a.G, ql, qh, [&](int el, const float (&)[6]) {
         const int eI = e_begin + el;
         const int e0 = a.bedge[2 * eI], e1 = a.bedge[2 * eI + 1];
         if (vI == e0 || vI == e1) return;
@@ -591,7 +612,7 @@ __global__ void k_cs_codim_pp(CsArgs a, int sv_begin)
     qh[0] = cellc(p.x + a.dHat, a.G.inv);
     qh[1] = cellc(p.y + a.dHat, a.G.inv);
     qh[2] = cellc(p.z + a.dHat, a.G.inv);
-    grid_query(a.G, ql, qh, [&](int svJ) {
+    grid_query(a.G, ql, qh, [&](int svJ, const float (&)[6]) {
         if (svJ <= sv) return;
         const int vJ = a.bnode[svJ];
         if (a.dbc[vI] && a.dbc[vJ]) return;
@@ -638,7 +659,7 @@ int build_constraints(Sim* s, const double* x)
         ConSink S{s->ckind.p, s->cverts.p, s->cmult.p, s->cap_con, s->cnt.p, tkeys, tcount, tsz - 1};
         size_t mark = ar.used;
         Grid G;
-        rc = static_grid(build_grid(s, ar, s->nbt, 3, s->btri.p, x, nullptr, 0, G));
+        rc = static_grid(build_grid(s, ar, s->nbt, 3, s->btri.p, x, nullptr, 0, tbox, G));
         if (rc == kNeedScratch) {
             if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
             continue;
@@ -648,7 +669,7 @@ int build_constraints(Sim* s, const double* x)
                  tbox, ebox, float_up(dHat)};
         k_cs_pt<<<nblk(s->nbn, 128), 128, 0, st>>>(a);
         ar.used = mark;
-        rc = static_grid(build_grid(s, ar, s->nbe, 2, s->bedge.p, x, nullptr, 0, G));
+        rc = static_grid(build_grid(s, ar, s->nbe, 2, s->bedge.p, x, nullptr, 0, ebox, G));
         if (rc == kNeedScratch) {
             if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
             continue;
@@ -660,7 +681,8 @@ int build_constraints(Sim* s, const double* x)
         if (s->nrod_e > 0 && s->nbn > s->codim0) {
             ar.used = mark;
             const int e_begin = s->nbe - s->nrod_e;
-            rc = static_grid(build_grid(s, ar, s->nrod_e, 2, s->bedge.p + 2 * (size_t)e_begin, x, nullptr, 0, G));
+            rc = static_grid(
+                build_grid(s, ar, s->nrod_e, 2, s->bedge.p + 2 * (size_t)e_begin, x, nullptr, 0, nullptr, G));
             if (rc == kNeedScratch) {
                 if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
                 again = true;
@@ -673,7 +695,7 @@ int build_constraints(Sim* s, const double* x)
         }
         if (!again && s->nbn > s->codim1) {
             ar.used = mark;
-            rc = static_grid(build_grid(s, ar, s->nbn, 1, s->bnode.p, x, nullptr, 0, G));
+            rc = static_grid(build_grid(s, ar, s->nbn, 1, s->bnode.p, x, nullptr, 0, nullptr, G));
             if (rc == kNeedScratch) {
                 if ((rc = ensure_scratch(s, s->scratch_bytes))) return rc;
                 again = true;
@@ -1228,8 +1250,8 @@ __global__ void k_ccd_pt(CcdCand c)
     const float pb[6] = {__double2float_rd(fmin(p.x, pf.x)), __double2float_rd(fmin(p.y, pf.y)),
                          __double2float_rd(fmin(p.z, pf.z)), __double2float_ru(fmax(p.x, pf.x)),
                          __double2float_ru(fmax(p.y, pf.y)), __double2float_ru(fmax(p.z, pf.z))};
-    grid_query(c.G, ql, qh, [&](int t) {
-        if (box_apart(pb, c.tbox + 6 * (size_t)t, c.xi_f)) return;
+    grid_query(c.G, ql, qh, [&](int t, const float (&bx)[6]) {
+        if (box_apart(pb, bx, c.xi_f)) return;
         const int t0i = c.btri[3 * t], t1i = c.btri[3 * t + 1], t2i = c.btri[3 * t + 2];
         if (vI == t0i || vI == t1i || vI == t2i) return;
         if (c.dbc[vI] && c.dbc[t0i] && c.dbc[t1i] && c.dbc[t2i]) return;
@@ -1262,9 +1284,9 @@ __global__ void k_ccd_ee(CcdCand c)
     float eb[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) eb[k] = c.ebox[6 * (size_t)eI + k];
-    grid_query(c.G, ql, qh, [&](int eJ) {
+    grid_query(c.G, ql, qh, [&](int eJ, const float (&bx)[6]) {
         if (eJ <= eI) return;
-        if (box_apart(eb, c.ebox + 6 * (size_t)eJ, c.xi_f)) return;
+        if (box_apart(eb, bx, c.xi_f)) return;
         const int b0 = c.bedge[2 * eJ], b1 = c.bedge[2 * eJ + 1];
         if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
         if (c.dbc[a0] && c.dbc[a1] && c.dbc[b0] && c.dbc[b1]) return;
@@ -1297,7 +1319,7 @@ __global__ void k_ccd_codim(CcdCand c, int sv_begin, int e_begin)
     qh[1] = cellc(mx.y + c.xi, c.G.inv);
     qh[2] = cellc(mx.z + c.xi, c.G.inv);
     const d3 mxp = vmax3(p, p + dp), mnp = vmin3(p, p + dp);
-    grid_query(c.G, ql, qh, [&](int it) {
+    grid_query(c.G, ql, qh, [&](int it, const float (&)[6]) {
         if (e_begin >= 0) {
             const int eI = e_begin + it;
             const int e0 = c.bedge[2 * eI], e1 = c.bedge[2 * eI + 1];
@@ -1360,7 +1382,7 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         cudaMemsetAsync(ctr, 0, 8 * sizeof(unsigned long long), st);
         size_t mark = ar.used;
         Grid G;
-        rc = build_grid(s, ar, s->nbt, 3, s->btri.p, x, p, alpha, G);
+        rc = build_grid(s, ar, s->nbt, 3, s->btri.p, x, p, alpha, tbox, G);
         if (rc == kSpanTooLarge) {
             if (++shrink > 60) return set_error(CIPC_ERR_NOT_CONVERGED, "CCD: swept boxes span too many cells");
             alpha *= 0.5;  // a smaller trial step: the bound stays conservative
@@ -1376,7 +1398,7 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
                   ptype, pidx, cap, ctr, tbox, ebox, float_up(s->prm.xi)};
         k_ccd_pt<<<nblk(s->nbn, 128), 128, 0, st>>>(c);
         ar.used = mark;
-        rc = build_grid(s, ar, s->nbe, 2, s->bedge.p, x, p, alpha, G);
+        rc = build_grid(s, ar, s->nbe, 2, s->bedge.p, x, p, alpha, ebox, G);
         if (rc == kSpanTooLarge) {
             if (++shrink > 60) return set_error(CIPC_ERR_NOT_CONVERGED, "CCD: swept boxes span too many cells");
             alpha *= 0.5;  // a smaller trial step: the bound stays conservative
@@ -1394,7 +1416,7 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         if (s->nrod_e > 0 && s->nbn > s->codim1) {
             ar.used = mark;
             const int e_begin = s->nbe - s->nrod_e;
-            rc = build_grid(s, ar, s->nrod_e, 2, s->bedge.p + 2 * (size_t)e_begin, x, p, alpha, G);
+            rc = build_grid(s, ar, s->nrod_e, 2, s->bedge.p + 2 * (size_t)e_begin, x, p, alpha, nullptr, G);
             if (rc == kSpanTooLarge) {
                 if (++shrink > 60) return set_error(CIPC_ERR_NOT_CONVERGED, "CCD: swept boxes span too many cells");
                 alpha *= 0.5;  // a smaller trial step: the bound stays conservative
@@ -1413,7 +1435,7 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         }
         if (!again && s->nbn > s->codim1) {
             ar.used = mark;
-            rc = build_grid(s, ar, s->nbn, 1, s->bnode.p, x, p, alpha, G);
+            rc = build_grid(s, ar, s->nbn, 1, s->bnode.p, x, p, alpha, nullptr, G);
             if (rc == kSpanTooLarge) {
                 if (++shrink > 60) return set_error(CIPC_ERR_NOT_CONVERGED, "CCD: swept boxes span too many cells");
                 alpha *= 0.5;  // a smaller trial step: the bound stays conservative
