@@ -146,6 +146,7 @@ struct Sim {
     DBuf<char> hval;  // BSR values, float or double per precision
     // contact constraint list
     int ncon = 0, cap_con = 0;
+    int cap_cand = 0;  // capacity of the broad phase's candidate-pair lists (grown on overflow)
     DBuf<int> ckind, cmult;
     DBuf<int4> cverts;
     DBuf<char> chess;  // 78 entries per constraint (float/double)

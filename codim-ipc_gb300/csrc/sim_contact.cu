@@ -13,6 +13,7 @@
 // against edges of higher index, emitting PT / EE / mollified EE-PE-PP directly
 // and PP / PE through a device hash table keyed by the reference's code, which
 // merges duplicates into a multiplicity (IPC.h:571-661).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -426,7 +427,39 @@ __device__ __forceinline__ void grid_query(const Grid& G, const int (&ql)[3], co
             }
 }
 
-__global__ void k_cs_pt(CsArgs a)
+// Candidate lists between the grid traversal and the FP64 tests.  The traversal
+// kernels (one thread per query primitive) keep only the cheap integer and FP32
+// tests and append the surviving pairs here; the evaluation kernels then run the
+// FP64 box test, the classification and the distance one thread per pair, with
+// every lane of a warp busy (in the traversal the candidate counts differ from
+// lane to lane: 3-5 of 32 lanes were active, and the FP64 pipe, which counts warp
+// instructions, was 70-82% busy).  Appends are aggregated over the lanes that
+// arrive together; a list that overflows its capacity is counted and the caller
+// reruns with a larger one.
+struct CandList {
+    int2* v;
+    unsigned long long* n;
+    int cap;
+};
+
+__device__ __forceinline__ void push_cand(const CandList& L, int x, int y)
+{
+    namespace cg = cooperative_groups;
+    const cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(L.n, (unsigned long long)g.size());
+    base = g.shfl(base, 0);
+    const unsigned long long i = base + g.thread_rank();
+    if (i < (unsigned long long)L.cap) L.v[i] = make_int2(x, y);
+}
+
+__device__ __forceinline__ int cand_count(const CandList& L)
+{
+    const unsigned long long n = *L.n;
+    return (int)(n < (unsigned long long)L.cap ? n : (unsigned long long)L.cap);
+}
+
+__global__ void k_cs_pt(CsArgs a, CandList L)
 {
     const int sv = blockIdx.x * blockDim.x + threadIdx.x;
     if (sv >= a.nbn) return;
@@ -446,9 +479,23 @@ __global__ void k_cs_pt(CsArgs a)
         const int t0i = a.btri[3 * t], t1i = a.btri[3 * t + 1], t2i = a.btri[3 * t + 2];
         if (vI == t0i || vI == t1i || vI == t2i) return;
         if (a.dbc[vI] && a.dbc[t0i] && a.dbc[t1i] && a.dbc[t2i]) return;
+        push_cand(L, vI, t);
+    });
+}
+
+// point-triangle candidates (point vI, boundary triangle t): FP64 box test,
+// classification and distance (IPC.h:19-740)
+__global__ void __launch_bounds__(128) k_cs_pt_eval(CsArgs a, CandList L)
+{
+    const int n = cand_count(L);
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        const int2 q = L.v[c];
+        const int vI = q.x, t = q.y;
+        const d3 p = ld(a.x, vI);
+        const int t0i = a.btri[3 * t], t1i = a.btri[3 * t + 1], t2i = a.btri[3 * t + 2];
         const d3 t0 = ld(a.x, t0i), t1 = ld(a.x, t1i), t2 = ld(a.x, t2i);
         const d3 mx = vmax3(vmax3(t0, t1), t2), mn = vmin3(vmin3(t0, t1), t2);
-        if (any_gt3(p - mx, a.dHat) || any_gt3(mn - p, a.dHat)) return;
+        if (any_gt3(p - mx, a.dHat) || any_gt3(mn - p, a.dHat)) continue;
         const d3 e1 = t1 - t0, e2 = t2 - t0, w = p - t0;
         switch (pt_type_fast(p, t0, t1, t2, w, e1, e2)) {
             case 0: if (n2(w) < a.dh2) emit_merge(a.S, kc_PP, vI, t0i, -1); break;
@@ -459,10 +506,10 @@ __global__ void k_cs_pt(CsArgs a)
             case 5: if (pe_d2(p, t2, t0) < a.dh2) emit_merge(a.S, kc_PE, vI, t2i, t0i); break;
             default: if (pt_d2_w(w, e1, e2) < a.dh2) emit(a.S, kc_PT, vI, t0i, t1i, t2i); break;
         }
-    });
+    }
 }
 
-__global__ void k_cs_ee(CsArgs a)
+__global__ void k_cs_ee(CsArgs a, CandList L)
 {
     const int eI = blockIdx.x * blockDim.x + threadIdx.x;
     if (eI >= a.nbe) return;
@@ -485,66 +532,86 @@ __global__ void k_cs_ee(CsArgs a)
         const int b0 = a.bedge[2 * eJ], b1 = a.bedge[2 * eJ + 1];
         if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
         if (a.dbc[a0] && a.dbc[a1] && a.dbc[b0] && a.dbc[b1]) return;
+        push_cand(L, eI, eJ);
+    });
+}
+
+// edge-edge candidates (boundary edges eI < eJ): FP64 box test, classification,
+// distance and the mollifier test (IPC.h:19-740); the mollifier threshold is
+// formed only for pairs within dHat
+__global__ void __launch_bounds__(128) k_cs_ee_eval(CsArgs a, CandList L)
+{
+    const int n = cand_count(L);
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        const int2 q = L.v[c];
+        const int eI = q.x, eJ = q.y;
+        const int a0 = a.bedge[2 * eI], a1 = a.bedge[2 * eI + 1];
+        const int b0 = a.bedge[2 * eJ], b1 = a.bedge[2 * eJ + 1];
+        const d3 ea0 = ld(a.x, a0), ea1 = ld(a.x, a1);
+        const d3 mna = vmin3(ea0, ea1), mxa = vmax3(ea0, ea1);
         const d3 eb0 = ld(a.x, b0), eb1 = ld(a.x, b1);
         const d3 mnb = vmin3(eb0, eb1), mxb = vmax3(eb0, eb1);
-        if (any_gt3(mna - mxb, a.dHat) || any_gt3(mnb - mxa, a.dHat)) return;
-        const double eps_x = G_MUL(G_MUL(1.0e-3, n2(ld(a.X0, a0) - ld(a.X0, a1))), n2(ld(a.X0, b0) - ld(a.X0, b1)));
+        if (any_gt3(mna - mxb, a.dHat) || any_gt3(mnb - mxa, a.dHat)) continue;
         const d3 u = ea1 - ea0, v = eb1 - eb0, w = ea0 - eb0;
-        const bool moll = n2(cross(u, v)) < eps_x;
+        auto moll = [&]() {
+            const double eps_x =
+                G_MUL(G_MUL(1.0e-3, n2(ld(a.X0, a0) - ld(a.X0, a1))), n2(ld(a.X0, b0) - ld(a.X0, b1)));
+            return n2(cross(u, v)) < eps_x;
+        };
         switch (ee_type_fast(ea0, ea1, eb0, eb1, u, v, w)) {
             case 0:
                 if (n2(w) < a.dh2) {
-                    if (moll) emit(a.S, kc_PPM, a0, a1, b0, b1);
+                    if (moll()) emit(a.S, kc_PPM, a0, a1, b0, b1);
                     else emit_merge(a.S, kc_PP, a0, b0, -1);
                 }
                 break;
             case 1:
                 if (pp_d2(ea0, eb1) < a.dh2) {
-                    if (moll) emit(a.S, kc_PPM, a0, a1, b1, b0);
+                    if (moll()) emit(a.S, kc_PPM, a0, a1, b1, b0);
                     else emit_merge(a.S, kc_PP, a0, b1, -1);
                 }
                 break;
             case 2:
                 if (pe_d2(ea0, eb0, eb1) < a.dh2) {
-                    if (moll) emit(a.S, kc_PEM, a0, a1, b0, b1);
+                    if (moll()) emit(a.S, kc_PEM, a0, a1, b0, b1);
                     else emit_merge(a.S, kc_PE, a0, b0, b1);
                 }
                 break;
             case 3:
                 if (pp_d2(ea1, eb0) < a.dh2) {
-                    if (moll) emit(a.S, kc_PPM, a1, a0, b0, b1);
+                    if (moll()) emit(a.S, kc_PPM, a1, a0, b0, b1);
                     else emit_merge(a.S, kc_PP, a1, b0, -1);
                 }
                 break;
             case 4:
                 if (pp_d2(ea1, eb1) < a.dh2) {
-                    if (moll) emit(a.S, kc_PPM, a1, a0, b1, b0);
+                    if (moll()) emit(a.S, kc_PPM, a1, a0, b1, b0);
                     else emit_merge(a.S, kc_PP, a1, b1, -1);
                 }
                 break;
             case 5:
                 if (pe_d2(ea1, eb0, eb1) < a.dh2) {
-                    if (moll) emit(a.S, kc_PEM, a1, a0, b0, b1);
+                    if (moll()) emit(a.S, kc_PEM, a1, a0, b0, b1);
                     else emit_merge(a.S, kc_PE, a1, b0, b1);
                 }
                 break;
             case 6:
                 if (pe_d2(eb0, ea0, ea1) < a.dh2) {
-                    if (moll) emit(a.S, kc_PEM, b0, b1, a0, a1);
+                    if (moll()) emit(a.S, kc_PEM, b0, b1, a0, a1);
                     else emit_merge(a.S, kc_PE, b0, a0, a1);
                 }
                 break;
             case 7:
                 if (pe_d2(eb1, ea0, ea1) < a.dh2) {
-                    if (moll) emit(a.S, kc_PEM, b1, b0, a0, a1);
+                    if (moll()) emit(a.S, kc_PEM, b1, b0, a0, a1);
                     else emit_merge(a.S, kc_PE, b1, a0, a1);
                 }
                 break;
             default:
-                if (ee_d2_w(u, v, w) < a.dh2) emit(a.S, moll ? kc_EEM : kc_EE, a0, a1, b0, b1);
+                if (ee_d2_w(u, v, w) < a.dh2) emit(a.S, moll() ? kc_EEM : kc_EE, a0, a1, b0, b1);
                 break;
         }
-    });
+    }
 }
 
 __global__ void k_cs_compact(ConSink S)
@@ -642,7 +709,8 @@ int build_constraints(Sim* s, const double* x)
         unsigned tsz = 1024;
         while (tsz < 4u * (unsigned)s->cap_con) tsz <<= 1;
         const size_t need = grid_bytes(std::max(std::max(s->nbt, s->nbe), s->nbn), 16) + (size_t)tsz * 12 +
-                            24 * ((size_t)s->nbt + s->nbe) + (1 << 20);
+                            24 * ((size_t)s->nbt + s->nbe) +
+                            8 * (size_t)std::max(s->cap_cand, std::max(1 << 16, 8 * (s->nbn + s->nbe))) + (1 << 20);
         int rc = ensure_scratch(s, need);
         if (rc) return rc;
         Arena ar{s->scratch.p, s->scratch.n};
@@ -650,7 +718,12 @@ int build_constraints(Sim* s, const double* x)
         int* tcount = ar.take<int>(tsz);
         float* tbox = ar.take<float>(6 * (size_t)s->nbt + 6);
         float* ebox = ar.take<float>(6 * (size_t)s->nbe + 6);
+        if (s->cap_cand == 0) s->cap_cand = std::max(1 << 16, 8 * (s->nbn + s->nbe));
+        int2* cand = ar.take<int2>((size_t)s->cap_cand);
         if (ar.used > ar.cap) return set_error(CIPC_ERR_CUDA, "constraint scratch");
+        // the two candidate lists share one buffer: counts in cnt[4] (PT) and cnt[5] (EE)
+        const CandList Lpt{cand, s->cnt.p + 4, s->cap_cand}, Lee{cand, s->cnt.p + 5, s->cap_cand};
+        const int eval_grid = num_sms() * 8;
         if (s->nbt) k_item_boxes<<<nblk(s->nbt, 256), 256, 0, st>>>(s->nbt, 3, s->btri.p, x, tbox);
         if (s->nbe) k_item_boxes<<<nblk(s->nbe, 256), 256, 0, st>>>(s->nbe, 2, s->bedge.p, x, ebox);
         cudaMemsetAsync(tkeys, 0xFF, sizeof(unsigned long long) * tsz, st);
@@ -667,7 +740,8 @@ int build_constraints(Sim* s, const double* x)
         if (rc) return rc;
         CsArgs a{s->nbn, s->nbe, s->bnode.p, s->bedge.p, s->btri.p, x, s->X0.p, s->dbc.p, dHat, dHat * dHat, G, S,
                  tbox, ebox, float_up(dHat)};
-        k_cs_pt<<<nblk(s->nbn, 128), 128, 0, st>>>(a);
+        k_cs_pt<<<nblk(s->nbn, 128), 128, 0, st>>>(a, Lpt);
+        k_cs_pt_eval<<<eval_grid, 128, 0, st>>>(a, Lpt);
         ar.used = mark;
         rc = static_grid(build_grid(s, ar, s->nbe, 2, s->bedge.p, x, nullptr, 0, ebox, G));
         if (rc == kNeedScratch) {
@@ -676,7 +750,8 @@ int build_constraints(Sim* s, const double* x)
         }
         if (rc) return rc;
         a.G = G;
-        k_cs_ee<<<nblk(s->nbe, 128), 128, 0, st>>>(a);
+        k_cs_ee<<<nblk(s->nbe, 128), 128, 0, st>>>(a, Lee);
+        k_cs_ee_eval<<<eval_grid, 128, 0, st>>>(a, Lee);
         bool again = false;
         if (s->nrod_e > 0 && s->nbn > s->codim0) {
             ar.used = mark;
@@ -708,10 +783,16 @@ int build_constraints(Sim* s, const double* x)
         }
         if (again) continue;
         k_cs_compact<<<nblk(tsz, 256), 256, 0, st>>>(S);
-        unsigned long long c[3];
+        unsigned long long c[6];
         cudaMemcpyAsync(c, s->cnt.p, sizeof(c), cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return set_cuda_error(e, "constraint set");
+        const unsigned long long nc = std::max(c[4], c[5]);
+        if (nc > (unsigned long long)s->cap_cand) {
+            // a candidate list overflowed: rebuild the set with room for all of them
+            s->cap_cand = (int)std::min<unsigned long long>(nc + nc / 2 + 4096, 1ull << 30);
+            continue;
+        }
         if (!c[1] && !c[2]) {
             s->ncon = (int)c[0];
             return CIPC_OK;
@@ -1231,7 +1312,7 @@ __device__ __forceinline__ void add_pair(const CcdCand& c, int tp, int a, int b,
     }
 }
 
-__global__ void k_ccd_pt(CcdCand c)
+__global__ void k_ccd_pt(CcdCand c, CandList L)
 {
     const int sv = blockIdx.x * blockDim.x + threadIdx.x;
     if (sv >= c.nbn) return;
@@ -1255,18 +1336,31 @@ __global__ void k_ccd_pt(CcdCand c)
         const int t0i = c.btri[3 * t], t1i = c.btri[3 * t + 1], t2i = c.btri[3 * t + 2];
         if (vI == t0i || vI == t1i || vI == t2i) return;
         if (c.dbc[vI] && c.dbc[t0i] && c.dbc[t1i] && c.dbc[t2i]) return;
-        // CCD.h:187-211 with the full direction
+        push_cand(L, vI, t);
+    });
+}
+
+// point-triangle CCD candidates: the swept-box test of CCD.h:187-211 with the
+// full direction, in FP64, then the pair list of the narrow phase
+__global__ void __launch_bounds__(128) k_ccd_pt_eval(CcdCand c, CandList L)
+{
+    const int n = cand_count(L);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int2 q = L.v[k];
+        const int vI = q.x, t = q.y;
+        const d3 p = ld(c.x, vI), dp = ld(c.p, vI);
+        const int t0i = c.btri[3 * t], t1i = c.btri[3 * t + 1], t2i = c.btri[3 * t + 2];
         const d3 t0 = ld(c.x, t0i), t1 = ld(c.x, t1i), t2 = ld(c.x, t2i);
         const d3 d0 = ld(c.p, t0i), d1 = ld(c.p, t1i), d2 = ld(c.p, t2i);
         const d3 mxp = vmax3(p, p + dp), mnp = vmin3(p, p + dp);
         const d3 mxt = vmax3(vmax3(vmax3(t0, t1), t2), vmax3(vmax3(t0 + d0, t1 + d1), t2 + d2));
         const d3 mnt = vmin3(vmin3(vmin3(t0, t1), t2), vmin3(vmin3(t0 + d0, t1 + d1), t2 + d2));
-        if (any_gt3(mnp - mxt, c.xi) || any_gt3(mnt - mxp, c.xi)) return;
+        if (any_gt3(mnp - mxt, c.xi) || any_gt3(mnt - mxp, c.xi)) continue;
         add_pair(c, kPT, vI, t0i, t1i, t2i);
-    });
+    }
 }
 
-__global__ void k_ccd_ee(CcdCand c)
+__global__ void k_ccd_ee(CcdCand c, CandList L)
 {
     const int eI = blockIdx.x * blockDim.x + threadIdx.x;
     if (eI >= c.nbe) return;
@@ -1290,14 +1384,28 @@ __global__ void k_ccd_ee(CcdCand c)
         const int b0 = c.bedge[2 * eJ], b1 = c.bedge[2 * eJ + 1];
         if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
         if (c.dbc[a0] && c.dbc[a1] && c.dbc[b0] && c.dbc[b1]) return;
+        push_cand(L, eI, eJ);
+    });
+}
+
+// edge-edge CCD candidates: the FP64 swept-box test (CCD.h), then the pair list
+__global__ void __launch_bounds__(128) k_ccd_ee_eval(CcdCand c, CandList L)
+{
+    const int n = cand_count(L);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int2 q = L.v[k];
+        const int eI = q.x, eJ = q.y;
+        const int a0 = c.bedge[2 * eI], a1 = c.bedge[2 * eI + 1];
+        const int b0 = c.bedge[2 * eJ], b1 = c.bedge[2 * eJ + 1];
+        const d3 ea0 = ld(c.x, a0), ea1 = ld(c.x, a1), da0 = ld(c.p, a0), da1 = ld(c.p, a1);
         const d3 eb0 = ld(c.x, b0), eb1 = ld(c.x, b1), db0 = ld(c.p, b0), db1 = ld(c.p, b1);
         const d3 mxa = vmax3(vmax3(ea0, ea1), vmax3(ea0 + da0, ea1 + da1));
         const d3 mna = vmin3(vmin3(ea0, ea1), vmin3(ea0 + da0, ea1 + da1));
         const d3 mxb = vmax3(vmax3(eb0, eb1), vmax3(eb0 + db0, eb1 + db1));
         const d3 mnb = vmin3(vmin3(eb0, eb1), vmin3(eb0 + db0, eb1 + db1));
-        if (any_gt3(mna - mxb, c.xi) || any_gt3(mnb - mxa, c.xi)) return;
+        if (any_gt3(mna - mxb, c.xi) || any_gt3(mnb - mxa, c.xi)) continue;
         add_pair(c, kEE, a0, a1, b0, b1);
-    });
+    }
 }
 
 // codimensional CCD candidates (IPC.h:2087-2165): particles (boundary nodes from
@@ -1364,7 +1472,8 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
     int shrink = 0;
     for (int attempt = 0; attempt < 8; ++attempt) {
         const size_t need = grid_bytes(std::max(std::max(s->nbt, s->nbe), s->nbn), 32) + (size_t)cap * (16 + 1 + 8 + 1) +
-                            24 * ((size_t)s->nbt + s->nbe) + (1 << 20);
+                            24 * ((size_t)s->nbt + s->nbe) +
+                            8 * (size_t)std::max(s->cap_cand, std::max(1 << 16, 8 * (s->nbn + s->nbe))) + (1 << 20);
         int rc = ensure_scratch(s, need);
         if (rc) return rc;
         Arena ar{s->scratch.p, s->scratch.n};
@@ -1376,7 +1485,12 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         double* amin = ar.take<double>(1);
         float* tbox = ar.take<float>(6 * (size_t)s->nbt + 6);
         float* ebox = ar.take<float>(6 * (size_t)s->nbe + 6);
+        if (s->cap_cand == 0) s->cap_cand = std::max(1 << 16, 8 * (s->nbn + s->nbe));
+        int2* cand = ar.take<int2>((size_t)s->cap_cand);
         if (ar.used > ar.cap) return set_error(CIPC_ERR_CUDA, "CCD scratch");
+        // candidate lists (one buffer, used in turn): counts in ctr[6] (PT) and ctr[7] (EE)
+        const CandList Lpt{cand, ctr + 6, s->cap_cand}, Lee{cand, ctr + 7, s->cap_cand};
+        const int eval_grid = num_sms() * 8;
         if (s->nbt) k_item_swept_boxes<<<nblk(s->nbt, 256), 256, 0, st>>>(s->nbt, 3, s->btri.p, x, p, tbox);
         if (s->nbe) k_item_swept_boxes<<<nblk(s->nbe, 256), 256, 0, st>>>(s->nbe, 2, s->bedge.p, x, p, ebox);
         cudaMemsetAsync(ctr, 0, 8 * sizeof(unsigned long long), st);
@@ -1396,7 +1510,8 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         if (rc) return rc;
         CcdCand c{s->bnode.p, s->bedge.p, s->btri.p, s->nbn, s->nbe, x, p, alpha, s->prm.xi, s->dbc.p, G,
                   ptype, pidx, cap, ctr, tbox, ebox, float_up(s->prm.xi)};
-        k_ccd_pt<<<nblk(s->nbn, 128), 128, 0, st>>>(c);
+        k_ccd_pt<<<nblk(s->nbn, 128), 128, 0, st>>>(c, Lpt);
+        k_ccd_pt_eval<<<eval_grid, 128, 0, st>>>(c, Lpt);
         ar.used = mark;
         rc = build_grid(s, ar, s->nbe, 2, s->bedge.p, x, p, alpha, ebox, G);
         if (rc == kSpanTooLarge) {
@@ -1411,7 +1526,8 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         }
         if (rc) return rc;
         c.G = G;
-        k_ccd_ee<<<nblk(s->nbe, 128), 128, 0, st>>>(c);
+        k_ccd_ee<<<nblk(s->nbe, 128), 128, 0, st>>>(c, Lee);
+        k_ccd_ee_eval<<<eval_grid, 128, 0, st>>>(c, Lee);
         bool again = false;
         if (s->nrod_e > 0 && s->nbn > s->codim1) {
             ar.used = mark;
@@ -1453,10 +1569,16 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
             }
         }
         if (again) continue;
-        unsigned long long cc[2];
+        unsigned long long cc[8];
         cudaMemcpyAsync(cc, ctr, sizeof(cc), cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return set_cuda_error(e, "ccd candidates");
+        const unsigned long long nc = std::max(cc[6], cc[7]);
+        if (nc > (unsigned long long)s->cap_cand) {
+            // a candidate list overflowed: rerun with room for all of them
+            s->cap_cand = (int)std::min<unsigned long long>(nc + nc / 2 + 4096, 1ull << 30);
+            continue;
+        }
         if (cc[1]) {
             cap = (int)std::min<unsigned long long>(cc[0] + cc[0] / 2 + 1024, 1ull << 30);
             continue;
