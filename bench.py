@@ -761,7 +761,8 @@ def run_ours(args):
                        "l2": "inputs (%.2f GB) larger than L2; no flush" % (ccd_bytes / 1e9)},
             "e2e": {"value": round(whole_job_mpairs(e2e_s, n, 1, ws), 2), "unit": "Mpairs/s",
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "gpu_launches": args.steps,
+            # the FP64 pass is two kernels (k_accd_setup, k_accd_steps), the mixed one k_accd_mixed
+            "gpu_launches": args.steps * (2 if prec == F.FP64 else 1),
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
                          "kernel": ("k_accd_mixed" if prec == F.MIXED else
