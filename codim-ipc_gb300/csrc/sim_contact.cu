@@ -427,9 +427,68 @@ __device__ __forceinline__ void grid_query(const Grid& G, const int (&ql)[3], co
             }
 }
 
+// The same query with the whole warp on one query range: lane l takes cells l,
+// l + 32, ... of the range, the warp scans their entry counts, and then every lane
+// takes one entry of the concatenated lists per round (its cell found by a binary
+// search over the lanes' prefix sums), so the lanes stay busy however the entries
+// are spread over the cells.  All 32 lanes of the warp must call it with the same
+// range; f(item, box) runs on the lanes that hold a candidate.
+template <typename F>
+__device__ __forceinline__ void grid_query_warp(const Grid& G, const int (&ql)[3], const int (&qh)[3], F&& f)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int nx = qh[0] - ql[0] + 1, ny = qh[1] - ql[1] + 1, nz = qh[2] - ql[2] + 1;
+    const long long ncell = (long long)nx * ny * nz;
+    for (long long c0 = 0; c0 < ncell; c0 += 32) {
+        const long long c = c0 + lane;
+        int ci = 0, cj = 0, ck = 0, st = 0, n = 0;
+        if (c < ncell) {
+            ck = ql[2] + (int)(c % nz);
+            cj = ql[1] + (int)((c / nz) % ny);
+            ci = ql[0] + (int)(c / ((long long)nz * ny));
+            const unsigned b = cell_hash(ci, cj, ck, G.mask);
+            st = __ldg(G.bstart + b);
+            n = __ldg(G.bstart + b + 1) - st;
+        }
+        int incl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(FULL, incl, 31);
+        for (int t0 = 0; t0 < total; t0 += 32) {
+            const int t = t0 + lane;
+            // owner = the first lane whose inclusive count exceeds t
+            int owner = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                const int v = __shfl_sync(FULL, incl, owner + step - 1);
+                if (t >= v) owner += step;
+            }
+            owner = min(owner, 31);
+            const int o_incl = __shfl_sync(FULL, incl, owner), o_n = __shfl_sync(FULL, n, owner);
+            const int o_st = __shfl_sync(FULL, st, owner);
+            const int i = __shfl_sync(FULL, ci, owner), j = __shfl_sync(FULL, cj, owner),
+                      k = __shfl_sync(FULL, ck, owner);
+            if (t >= total) continue;
+            const GridEntry* g = G.ent + o_st + (t - (o_incl - o_n));
+            const int4 A = __ldg(&g->a), B = __ldg(&g->b);
+            const float4 C = __ldg(&g->c), D = __ldg(&g->d);
+            if (i < A.y || j < A.z || k < A.w) continue;
+            if (i > B.x || j > B.y || k > B.z) continue;
+            // first cell of the intersection of both ranges
+            if (i != max(ql[0], A.y) || j != max(ql[1], A.z) || k != max(ql[2], A.w)) continue;
+            const float bx[6] = {C.x, C.y, C.z, C.w, D.x, D.y};
+            f(A.x, bx);
+        }
+    }
+}
+
 // Candidate lists between the grid traversal and the FP64 tests.  The traversal
-// kernels (one thread per query primitive) keep only the cheap integer and FP32
-// tests and append the surviving pairs here; the evaluation kernels then run the
+// kernels (one warp per query primitive, grid_query_warp) keep only the cheap
+// integer and FP32 tests and append the surviving pairs here; the evaluation kernels then run the
 // FP64 box test, the classification and the distance one thread per pair, with
 // every lane of a warp busy (in the traversal the candidate counts differ from
 // lane to lane: 3-5 of 32 lanes were active, and the FP64 pipe, which counts warp
@@ -461,26 +520,27 @@ __device__ __forceinline__ int cand_count(const CandList& L)
 
 __global__ void k_cs_pt(CsArgs a, CandList L)
 {
-    const int sv = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sv >= a.nbn) return;
-    const int vI = a.bnode[sv];
-    const d3 p = ld(a.x, vI);
-    int ql[3], qh[3];
-    ql[0] = cellc(p.x - a.dHat, a.G.inv);
-    ql[1] = cellc(p.y - a.dHat, a.G.inv);
-    ql[2] = cellc(p.z - a.dHat, a.G.inv);
-    qh[0] = cellc(p.x + a.dHat, a.G.inv);
-    qh[1] = cellc(p.y + a.dHat, a.G.inv);
-    qh[2] = cellc(p.z + a.dHat, a.G.inv);
-    const float pb[6] = {__double2float_rd(p.x), __double2float_rd(p.y), __double2float_rd(p.z),
-                         __double2float_ru(p.x), __double2float_ru(p.y), __double2float_ru(p.z)};
-    grid_query(a.G, ql, qh, [&](int t, const float (&bx)[6]) {
-        if (box_apart(pb, bx, a.dHat_f)) return;
-        const int t0i = a.btri[3 * t], t1i = a.btri[3 * t + 1], t2i = a.btri[3 * t + 2];
-        if (vI == t0i || vI == t1i || vI == t2i) return;
-        if (a.dbc[vI] && a.dbc[t0i] && a.dbc[t1i] && a.dbc[t2i]) return;
-        push_cand(L, vI, t);
-    });
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int sv = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sv < a.nbn; sv += nw) {
+        const int vI = a.bnode[sv];
+        const d3 p = ld(a.x, vI);
+        int ql[3], qh[3];
+        ql[0] = cellc(p.x - a.dHat, a.G.inv);
+        ql[1] = cellc(p.y - a.dHat, a.G.inv);
+        ql[2] = cellc(p.z - a.dHat, a.G.inv);
+        qh[0] = cellc(p.x + a.dHat, a.G.inv);
+        qh[1] = cellc(p.y + a.dHat, a.G.inv);
+        qh[2] = cellc(p.z + a.dHat, a.G.inv);
+        const float pb[6] = {__double2float_rd(p.x), __double2float_rd(p.y), __double2float_rd(p.z),
+                             __double2float_ru(p.x), __double2float_ru(p.y), __double2float_ru(p.z)};
+        grid_query_warp(a.G, ql, qh, [&](int t, const float (&bx)[6]) {
+            if (box_apart(pb, bx, a.dHat_f)) return;
+            const int t0i = a.btri[3 * t], t1i = a.btri[3 * t + 1], t2i = a.btri[3 * t + 2];
+            if (vI == t0i || vI == t1i || vI == t2i) return;
+            if (a.dbc[vI] && a.dbc[t0i] && a.dbc[t1i] && a.dbc[t2i]) return;
+            push_cand(L, vI, t);
+        });
+    }
 }
 
 // point-triangle candidates (point vI, boundary triangle t): FP64 box test,
@@ -511,29 +571,30 @@ __global__ void __launch_bounds__(128) k_cs_pt_eval(CsArgs a, CandList L)
 
 __global__ void k_cs_ee(CsArgs a, CandList L)
 {
-    const int eI = blockIdx.x * blockDim.x + threadIdx.x;
-    if (eI >= a.nbe) return;
-    const int a0 = a.bedge[2 * eI], a1 = a.bedge[2 * eI + 1];
-    const d3 ea0 = ld(a.x, a0), ea1 = ld(a.x, a1);
-    const d3 mna = vmin3(ea0, ea1), mxa = vmax3(ea0, ea1);
-    int ql[3], qh[3];
-    ql[0] = cellc(mna.x - a.dHat, a.G.inv);
-    ql[1] = cellc(mna.y - a.dHat, a.G.inv);
-    ql[2] = cellc(mna.z - a.dHat, a.G.inv);
-    qh[0] = cellc(mxa.x + a.dHat, a.G.inv);
-    qh[1] = cellc(mxa.y + a.dHat, a.G.inv);
-    qh[2] = cellc(mxa.z + a.dHat, a.G.inv);
-    float eb[6];
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int eI = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; eI < a.nbe; eI += nw) {
+        const int a0 = a.bedge[2 * eI], a1 = a.bedge[2 * eI + 1];
+        const d3 ea0 = ld(a.x, a0), ea1 = ld(a.x, a1);
+        const d3 mna = vmin3(ea0, ea1), mxa = vmax3(ea0, ea1);
+        int ql[3], qh[3];
+        ql[0] = cellc(mna.x - a.dHat, a.G.inv);
+        ql[1] = cellc(mna.y - a.dHat, a.G.inv);
+        ql[2] = cellc(mna.z - a.dHat, a.G.inv);
+        qh[0] = cellc(mxa.x + a.dHat, a.G.inv);
+        qh[1] = cellc(mxa.y + a.dHat, a.G.inv);
+        qh[2] = cellc(mxa.z + a.dHat, a.G.inv);
+        float eb[6];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) eb[k] = a.ebox[6 * (size_t)eI + k];
-    grid_query(a.G, ql, qh, [&](int eJ, const float (&bx)[6]) {
-        if (eJ <= eI) return;
-        if (box_apart(eb, bx, a.dHat_f)) return;
-        const int b0 = a.bedge[2 * eJ], b1 = a.bedge[2 * eJ + 1];
-        if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
-        if (a.dbc[a0] && a.dbc[a1] && a.dbc[b0] && a.dbc[b1]) return;
-        push_cand(L, eI, eJ);
-    });
+        for (int k = 0; k < 6; ++k) eb[k] = a.ebox[6 * (size_t)eI + k];
+        grid_query_warp(a.G, ql, qh, [&](int eJ, const float (&bx)[6]) {
+            if (eJ <= eI) return;
+            if (box_apart(eb, bx, a.dHat_f)) return;
+            const int b0 = a.bedge[2 * eJ], b1 = a.bedge[2 * eJ + 1];
+            if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
+            if (a.dbc[a0] && a.dbc[a1] && a.dbc[b0] && a.dbc[b1]) return;
+            push_cand(L, eI, eJ);
+        });
+    }
 }
 
 // edge-edge candidates (boundary edges eI < eJ): FP64 box test, classification,
@@ -740,7 +801,7 @@ int build_constraints(Sim* s, const double* x)
         if (rc) return rc;
         CsArgs a{s->nbn, s->nbe, s->bnode.p, s->bedge.p, s->btri.p, x, s->X0.p, s->dbc.p, dHat, dHat * dHat, G, S,
                  tbox, ebox, float_up(dHat)};
-        k_cs_pt<<<nblk(s->nbn, 128), 128, 0, st>>>(a, Lpt);
+        k_cs_pt<<<eval_grid, 256, 0, st>>>(a, Lpt);
         k_cs_pt_eval<<<eval_grid, 128, 0, st>>>(a, Lpt);
         ar.used = mark;
         rc = static_grid(build_grid(s, ar, s->nbe, 2, s->bedge.p, x, nullptr, 0, ebox, G));
@@ -750,7 +811,7 @@ int build_constraints(Sim* s, const double* x)
         }
         if (rc) return rc;
         a.G = G;
-        k_cs_ee<<<nblk(s->nbe, 128), 128, 0, st>>>(a, Lee);
+        k_cs_ee<<<eval_grid, 256, 0, st>>>(a, Lee);
         k_cs_ee_eval<<<eval_grid, 128, 0, st>>>(a, Lee);
         bool again = false;
         if (s->nrod_e > 0 && s->nbn > s->codim0) {
@@ -1314,30 +1375,31 @@ __device__ __forceinline__ void add_pair(const CcdCand& c, int tp, int a, int b,
 
 __global__ void k_ccd_pt(CcdCand c, CandList L)
 {
-    const int sv = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sv >= c.nbn) return;
-    const int vI = c.bnode[sv];
-    const d3 p = ld(c.x, vI), dp = ld(c.p, vI);
-    const d3 pe = p + scl(dp, c.alpha);
-    const d3 mn = vmin3(p, pe), mx = vmax3(p, pe);
-    int ql[3], qh[3];
-    ql[0] = cellc(mn.x - c.xi, c.G.inv);
-    ql[1] = cellc(mn.y - c.xi, c.G.inv);
-    ql[2] = cellc(mn.z - c.xi, c.G.inv);
-    qh[0] = cellc(mx.x + c.xi, c.G.inv);
-    qh[1] = cellc(mx.y + c.xi, c.G.inv);
-    qh[2] = cellc(mx.z + c.xi, c.G.inv);
-    const d3 pf = p + dp;
-    const float pb[6] = {__double2float_rd(fmin(p.x, pf.x)), __double2float_rd(fmin(p.y, pf.y)),
-                         __double2float_rd(fmin(p.z, pf.z)), __double2float_ru(fmax(p.x, pf.x)),
-                         __double2float_ru(fmax(p.y, pf.y)), __double2float_ru(fmax(p.z, pf.z))};
-    grid_query(c.G, ql, qh, [&](int t, const float (&bx)[6]) {
-        if (box_apart(pb, bx, c.xi_f)) return;
-        const int t0i = c.btri[3 * t], t1i = c.btri[3 * t + 1], t2i = c.btri[3 * t + 2];
-        if (vI == t0i || vI == t1i || vI == t2i) return;
-        if (c.dbc[vI] && c.dbc[t0i] && c.dbc[t1i] && c.dbc[t2i]) return;
-        push_cand(L, vI, t);
-    });
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int sv = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sv < c.nbn; sv += nw) {
+        const int vI = c.bnode[sv];
+        const d3 p = ld(c.x, vI), dp = ld(c.p, vI);
+        const d3 pe = p + scl(dp, c.alpha);
+        const d3 mn = vmin3(p, pe), mx = vmax3(p, pe);
+        int ql[3], qh[3];
+        ql[0] = cellc(mn.x - c.xi, c.G.inv);
+        ql[1] = cellc(mn.y - c.xi, c.G.inv);
+        ql[2] = cellc(mn.z - c.xi, c.G.inv);
+        qh[0] = cellc(mx.x + c.xi, c.G.inv);
+        qh[1] = cellc(mx.y + c.xi, c.G.inv);
+        qh[2] = cellc(mx.z + c.xi, c.G.inv);
+        const d3 pf = p + dp;
+        const float pb[6] = {__double2float_rd(fmin(p.x, pf.x)), __double2float_rd(fmin(p.y, pf.y)),
+                             __double2float_rd(fmin(p.z, pf.z)), __double2float_ru(fmax(p.x, pf.x)),
+                             __double2float_ru(fmax(p.y, pf.y)), __double2float_ru(fmax(p.z, pf.z))};
+        grid_query_warp(c.G, ql, qh, [&](int t, const float (&bx)[6]) {
+            if (box_apart(pb, bx, c.xi_f)) return;
+            const int t0i = c.btri[3 * t], t1i = c.btri[3 * t + 1], t2i = c.btri[3 * t + 2];
+            if (vI == t0i || vI == t1i || vI == t2i) return;
+            if (c.dbc[vI] && c.dbc[t0i] && c.dbc[t1i] && c.dbc[t2i]) return;
+            push_cand(L, vI, t);
+        });
+    }
 }
 
 // point-triangle CCD candidates: the swept-box test of CCD.h:187-211 with the
@@ -1362,30 +1424,31 @@ __global__ void __launch_bounds__(128) k_ccd_pt_eval(CcdCand c, CandList L)
 
 __global__ void k_ccd_ee(CcdCand c, CandList L)
 {
-    const int eI = blockIdx.x * blockDim.x + threadIdx.x;
-    if (eI >= c.nbe) return;
-    const int a0 = c.bedge[2 * eI], a1 = c.bedge[2 * eI + 1];
-    const d3 ea0 = ld(c.x, a0), ea1 = ld(c.x, a1), da0 = ld(c.p, a0), da1 = ld(c.p, a1);
-    const d3 s0 = ea0 + scl(da0, c.alpha), s1 = ea1 + scl(da1, c.alpha);
-    const d3 mn = vmin3(vmin3(ea0, ea1), vmin3(s0, s1)), mx = vmax3(vmax3(ea0, ea1), vmax3(s0, s1));
-    int ql[3], qh[3];
-    ql[0] = cellc(mn.x - c.xi, c.G.inv);
-    ql[1] = cellc(mn.y - c.xi, c.G.inv);
-    ql[2] = cellc(mn.z - c.xi, c.G.inv);
-    qh[0] = cellc(mx.x + c.xi, c.G.inv);
-    qh[1] = cellc(mx.y + c.xi, c.G.inv);
-    qh[2] = cellc(mx.z + c.xi, c.G.inv);
-    float eb[6];
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int eI = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; eI < c.nbe; eI += nw) {
+        const int a0 = c.bedge[2 * eI], a1 = c.bedge[2 * eI + 1];
+        const d3 ea0 = ld(c.x, a0), ea1 = ld(c.x, a1), da0 = ld(c.p, a0), da1 = ld(c.p, a1);
+        const d3 s0 = ea0 + scl(da0, c.alpha), s1 = ea1 + scl(da1, c.alpha);
+        const d3 mn = vmin3(vmin3(ea0, ea1), vmin3(s0, s1)), mx = vmax3(vmax3(ea0, ea1), vmax3(s0, s1));
+        int ql[3], qh[3];
+        ql[0] = cellc(mn.x - c.xi, c.G.inv);
+        ql[1] = cellc(mn.y - c.xi, c.G.inv);
+        ql[2] = cellc(mn.z - c.xi, c.G.inv);
+        qh[0] = cellc(mx.x + c.xi, c.G.inv);
+        qh[1] = cellc(mx.y + c.xi, c.G.inv);
+        qh[2] = cellc(mx.z + c.xi, c.G.inv);
+        float eb[6];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) eb[k] = c.ebox[6 * (size_t)eI + k];
-    grid_query(c.G, ql, qh, [&](int eJ, const float (&bx)[6]) {
-        if (eJ <= eI) return;
-        if (box_apart(eb, bx, c.xi_f)) return;
-        const int b0 = c.bedge[2 * eJ], b1 = c.bedge[2 * eJ + 1];
-        if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
-        if (c.dbc[a0] && c.dbc[a1] && c.dbc[b0] && c.dbc[b1]) return;
-        push_cand(L, eI, eJ);
-    });
+        for (int k = 0; k < 6; ++k) eb[k] = c.ebox[6 * (size_t)eI + k];
+        grid_query_warp(c.G, ql, qh, [&](int eJ, const float (&bx)[6]) {
+            if (eJ <= eI) return;
+            if (box_apart(eb, bx, c.xi_f)) return;
+            const int b0 = c.bedge[2 * eJ], b1 = c.bedge[2 * eJ + 1];
+            if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
+            if (c.dbc[a0] && c.dbc[a1] && c.dbc[b0] && c.dbc[b1]) return;
+            push_cand(L, eI, eJ);
+        });
+    }
 }
 
 // edge-edge CCD candidates: the FP64 swept-box test (CCD.h), then the pair list
@@ -1510,7 +1573,7 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         if (rc) return rc;
         CcdCand c{s->bnode.p, s->bedge.p, s->btri.p, s->nbn, s->nbe, x, p, alpha, s->prm.xi, s->dbc.p, G,
                   ptype, pidx, cap, ctr, tbox, ebox, float_up(s->prm.xi)};
-        k_ccd_pt<<<nblk(s->nbn, 128), 128, 0, st>>>(c, Lpt);
+        k_ccd_pt<<<eval_grid, 256, 0, st>>>(c, Lpt);
         k_ccd_pt_eval<<<eval_grid, 128, 0, st>>>(c, Lpt);
         ar.used = mark;
         rc = build_grid(s, ar, s->nbe, 2, s->bedge.p, x, p, alpha, ebox, G);
@@ -1526,7 +1589,7 @@ int ccd_step_size(Sim* s, const double* x, const double* p, double alpha, double
         }
         if (rc) return rc;
         c.G = G;
-        k_ccd_ee<<<nblk(s->nbe, 128), 128, 0, st>>>(c, Lee);
+        k_ccd_ee<<<eval_grid, 256, 0, st>>>(c, Lee);
         k_ccd_ee_eval<<<eval_grid, 128, 0, st>>>(c, Lee);
         bool again = false;
         if (s->nrod_e > 0 && s->nbn > s->codim1) {
