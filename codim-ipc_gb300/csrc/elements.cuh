@@ -350,8 +350,9 @@ CIPC_HD void dihedral_hess(const d3 (&x)[4], double (&H)[12][12])
 
 // Hessian of theta (12x12) in T from the hinge's edge vectors (taken in FP64 by
 // the caller: e0 = x2 - x1, e1 = x0 - x1, e2 = x3 - x1, e3 = x0 - x2, e4 = x3 - x2),
-// the same expressions as dihedral_hess: the FP32 form for the mixed-precision
-// Hessians, whose FP64 form is GB300-FP64-pipe bound
+// the same expressions as dihedral_hess, formed in the caller's Hessian array:
+// the bending kernel's form in both precisions (FP32 for the mixed-precision
+// Hessians, which takes it off GB300's narrow FP64 pipe)
 template <typename T>
 CIPC_HD void dihedral_hess_t(const T (&E)[5][3], T (&H)[12][12])
 {

@@ -140,34 +140,26 @@ __global__ void __launch_bounds__(128) k_bending(ElasticArgs a, HT* hval)
 #pragma unroll
                         for (int d = 0; d < 3; ++d) atomicAdd(a.g + 3 * vid[v] + d, 2 * c * dth * gt[3 * v + d]);
                 if (hval) {
+                    // Hessian of theta in HT (FP32 in mixed precision) from FP64 edge
+                    // vectors, formed in place in H
                     HT H[12][12];
-                    if constexpr (sizeof(HT) == 4) {
-                        // FP32 Hessian of theta from FP64 edge vectors
-                        const d3 ev[5] = {x[2] - x[1], x[0] - x[1], x[3] - x[1], x[0] - x[2], x[3] - x[2]};
-                        float E[5][3];
+                    const d3 ev[5] = {x[2] - x[1], x[0] - x[1], x[3] - x[1], x[0] - x[2], x[3] - x[2]};
+                    HT E[5][3];
 #pragma unroll
-                        for (int k = 0; k < 5; ++k) {
-                            E[k][0] = (float)ev[k].x;
-                            E[k][1] = (float)ev[k].y;
-                            E[k][2] = (float)ev[k].z;
-                        }
-                        dihedral_hess_t<float>(E, H);
-                        const float c2 = (float)(2 * c), fd = (float)dth;
-                        float gf[12];
-#pragma unroll
-                        for (int i = 0; i < 12; ++i) gf[i] = (float)gt[i];
-#pragma unroll
-                        for (int i = 0; i < 12; ++i)
-#pragma unroll
-                            for (int j = 0; j < 12; ++j) H[i][j] = c2 * (gf[i] * gf[j] + fd * H[i][j]);
-                    } else {
-                        double Ht[12][12];
-                        dihedral_hess(x, Ht);
-#pragma unroll
-                        for (int i = 0; i < 12; ++i)
-#pragma unroll
-                            for (int j = 0; j < 12; ++j) H[i][j] = (HT)(2 * c * (gt[i] * gt[j] + dth * Ht[i][j]));
+                    for (int k = 0; k < 5; ++k) {
+                        E[k][0] = (HT)ev[k].x;
+                        E[k][1] = (HT)ev[k].y;
+                        E[k][2] = (HT)ev[k].z;
                     }
+                    dihedral_hess_t<HT>(E, H);
+                    const HT c2 = (HT)(2 * c), fd = (HT)dth;
+                    HT gf[12];
+#pragma unroll
+                    for (int i = 0; i < 12; ++i) gf[i] = (HT)gt[i];
+#pragma unroll
+                    for (int i = 0; i < 12; ++i)
+#pragma unroll
+                        for (int j = 0; j < 12; ++j) H[i][j] = c2 * (gf[i] * gf[j] + fd * H[i][j]);
                     project_translation_free<HT, 4>(H);
                     scatter_blocks<HT>(hval, a.hinge_slot + 16 * t, a.proj, vid, 4, &H[0][0], 12);
                 }
