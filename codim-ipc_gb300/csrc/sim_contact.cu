@@ -486,6 +486,33 @@ __device__ __forceinline__ void grid_query_warp(const Grid& G, const int (&ql)[3
     }
 }
 
+// Query set-up values of lane k, broadcast to the warp: the set-up (cell range,
+// FP32 box, ids) is computed one query per lane for kQueryChunk queries, so its
+// FP64 work is shared by that many queries, and the warp then runs the queries
+// one after another (a warp per query paid it 32 times over: the FP64 pipe was
+// 80% busy; a chunk of 32 left too few warps in flight)
+constexpr int kQueryChunk = 8;
+struct QuerySetup {
+    int ql[3], qh[3];
+    float box[6];
+    int id[3];
+};
+
+__device__ __forceinline__ QuerySetup bcast_setup(const QuerySetup& q, int k)
+{
+    const unsigned FULL = 0xffffffffu;
+    QuerySetup r;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        r.ql[d] = __shfl_sync(FULL, q.ql[d], k);
+        r.qh[d] = __shfl_sync(FULL, q.qh[d], k);
+        r.id[d] = __shfl_sync(FULL, q.id[d], k);
+    }
+#pragma unroll
+    for (int d = 0; d < 6; ++d) r.box[d] = __shfl_sync(FULL, q.box[d], k);
+    return r;
+}
+
 // Candidate lists between the grid traversal and the FP64 tests.  The traversal
 // kernels (one warp per query primitive, grid_query_warp) keep only the cheap
 // integer and FP32 tests and append the surviving pairs here; the evaluation kernels then run the
@@ -520,26 +547,39 @@ __device__ __forceinline__ int cand_count(const CandList& L)
 
 __global__ void k_cs_pt(CsArgs a, CandList L)
 {
+    const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int sv = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sv < a.nbn; sv += nw) {
-        const int vI = a.bnode[sv];
-        const d3 p = ld(a.x, vI);
-        int ql[3], qh[3];
-        ql[0] = cellc(p.x - a.dHat, a.G.inv);
-        ql[1] = cellc(p.y - a.dHat, a.G.inv);
-        ql[2] = cellc(p.z - a.dHat, a.G.inv);
-        qh[0] = cellc(p.x + a.dHat, a.G.inv);
-        qh[1] = cellc(p.y + a.dHat, a.G.inv);
-        qh[2] = cellc(p.z + a.dHat, a.G.inv);
-        const float pb[6] = {__double2float_rd(p.x), __double2float_rd(p.y), __double2float_rd(p.z),
-                             __double2float_ru(p.x), __double2float_ru(p.y), __double2float_ru(p.z)};
-        grid_query_warp(a.G, ql, qh, [&](int t, const float (&bx)[6]) {
-            if (box_apart(pb, bx, a.dHat_f)) return;
-            const int t0i = a.btri[3 * t], t1i = a.btri[3 * t + 1], t2i = a.btri[3 * t + 2];
-            if (vI == t0i || vI == t1i || vI == t2i) return;
-            if (a.dbc[vI] && a.dbc[t0i] && a.dbc[t1i] && a.dbc[t2i]) return;
-            push_cand(L, vI, t);
-        });
+    for (int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kQueryChunk; base < a.nbn;
+         base += nw * kQueryChunk) {
+        QuerySetup mine{};
+        const int sv = base + lane;
+        if (lane < kQueryChunk && sv < a.nbn) {
+            const int vI = a.bnode[sv];
+            const d3 p = ld(a.x, vI);
+            mine.ql[0] = cellc(p.x - a.dHat, a.G.inv);
+            mine.ql[1] = cellc(p.y - a.dHat, a.G.inv);
+            mine.ql[2] = cellc(p.z - a.dHat, a.G.inv);
+            mine.qh[0] = cellc(p.x + a.dHat, a.G.inv);
+            mine.qh[1] = cellc(p.y + a.dHat, a.G.inv);
+            mine.qh[2] = cellc(p.z + a.dHat, a.G.inv);
+            const float pb[6] = {__double2float_rd(p.x), __double2float_rd(p.y), __double2float_rd(p.z),
+                                 __double2float_ru(p.x), __double2float_ru(p.y), __double2float_ru(p.z)};
+#pragma unroll
+            for (int d = 0; d < 6; ++d) mine.box[d] = pb[d];
+            mine.id[0] = vI;
+        }
+        const int nq = min(kQueryChunk, a.nbn - base);
+        for (int k = 0; k < nq; ++k) {
+            const QuerySetup q = bcast_setup(mine, k);
+            const int vI = q.id[0];
+            grid_query_warp(a.G, q.ql, q.qh, [&](int t, const float (&bx)[6]) {
+                if (box_apart(q.box, bx, a.dHat_f)) return;
+                const int t0i = a.btri[3 * t], t1i = a.btri[3 * t + 1], t2i = a.btri[3 * t + 2];
+                if (vI == t0i || vI == t1i || vI == t2i) return;
+                if (a.dbc[vI] && a.dbc[t0i] && a.dbc[t1i] && a.dbc[t2i]) return;
+                push_cand(L, vI, t);
+            });
+        }
     }
 }
 
@@ -571,29 +611,41 @@ __global__ void __launch_bounds__(128) k_cs_pt_eval(CsArgs a, CandList L)
 
 __global__ void k_cs_ee(CsArgs a, CandList L)
 {
+    const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int eI = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; eI < a.nbe; eI += nw) {
-        const int a0 = a.bedge[2 * eI], a1 = a.bedge[2 * eI + 1];
-        const d3 ea0 = ld(a.x, a0), ea1 = ld(a.x, a1);
-        const d3 mna = vmin3(ea0, ea1), mxa = vmax3(ea0, ea1);
-        int ql[3], qh[3];
-        ql[0] = cellc(mna.x - a.dHat, a.G.inv);
-        ql[1] = cellc(mna.y - a.dHat, a.G.inv);
-        ql[2] = cellc(mna.z - a.dHat, a.G.inv);
-        qh[0] = cellc(mxa.x + a.dHat, a.G.inv);
-        qh[1] = cellc(mxa.y + a.dHat, a.G.inv);
-        qh[2] = cellc(mxa.z + a.dHat, a.G.inv);
-        float eb[6];
+    for (int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kQueryChunk; base < a.nbe;
+         base += nw * kQueryChunk) {
+        QuerySetup mine{};
+        const int e = base + lane;
+        if (lane < kQueryChunk && e < a.nbe) {
+            const int a0 = a.bedge[2 * e], a1 = a.bedge[2 * e + 1];
+            const d3 ea0 = ld(a.x, a0), ea1 = ld(a.x, a1);
+            const d3 mna = vmin3(ea0, ea1), mxa = vmax3(ea0, ea1);
+            mine.ql[0] = cellc(mna.x - a.dHat, a.G.inv);
+            mine.ql[1] = cellc(mna.y - a.dHat, a.G.inv);
+            mine.ql[2] = cellc(mna.z - a.dHat, a.G.inv);
+            mine.qh[0] = cellc(mxa.x + a.dHat, a.G.inv);
+            mine.qh[1] = cellc(mxa.y + a.dHat, a.G.inv);
+            mine.qh[2] = cellc(mxa.z + a.dHat, a.G.inv);
 #pragma unroll
-        for (int k = 0; k < 6; ++k) eb[k] = a.ebox[6 * (size_t)eI + k];
-        grid_query_warp(a.G, ql, qh, [&](int eJ, const float (&bx)[6]) {
-            if (eJ <= eI) return;
-            if (box_apart(eb, bx, a.dHat_f)) return;
-            const int b0 = a.bedge[2 * eJ], b1 = a.bedge[2 * eJ + 1];
-            if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
-            if (a.dbc[a0] && a.dbc[a1] && a.dbc[b0] && a.dbc[b1]) return;
-            push_cand(L, eI, eJ);
-        });
+            for (int d = 0; d < 6; ++d) mine.box[d] = a.ebox[6 * (size_t)e + d];
+            mine.id[0] = e;
+            mine.id[1] = a0;
+            mine.id[2] = a1;
+        }
+        const int nq = min(kQueryChunk, a.nbe - base);
+        for (int k = 0; k < nq; ++k) {
+            const QuerySetup q = bcast_setup(mine, k);
+            const int eI = q.id[0], a0 = q.id[1], a1 = q.id[2];
+            grid_query_warp(a.G, q.ql, q.qh, [&](int eJ, const float (&bx)[6]) {
+                if (eJ <= eI) return;
+                if (box_apart(q.box, bx, a.dHat_f)) return;
+                const int b0 = a.bedge[2 * eJ], b1 = a.bedge[2 * eJ + 1];
+                if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
+                if (a.dbc[a0] && a.dbc[a1] && a.dbc[b0] && a.dbc[b1]) return;
+                push_cand(L, eI, eJ);
+            });
+        }
     }
 }
 
@@ -1375,30 +1427,43 @@ __device__ __forceinline__ void add_pair(const CcdCand& c, int tp, int a, int b,
 
 __global__ void k_ccd_pt(CcdCand c, CandList L)
 {
+    const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int sv = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sv < c.nbn; sv += nw) {
-        const int vI = c.bnode[sv];
-        const d3 p = ld(c.x, vI), dp = ld(c.p, vI);
-        const d3 pe = p + scl(dp, c.alpha);
-        const d3 mn = vmin3(p, pe), mx = vmax3(p, pe);
-        int ql[3], qh[3];
-        ql[0] = cellc(mn.x - c.xi, c.G.inv);
-        ql[1] = cellc(mn.y - c.xi, c.G.inv);
-        ql[2] = cellc(mn.z - c.xi, c.G.inv);
-        qh[0] = cellc(mx.x + c.xi, c.G.inv);
-        qh[1] = cellc(mx.y + c.xi, c.G.inv);
-        qh[2] = cellc(mx.z + c.xi, c.G.inv);
-        const d3 pf = p + dp;
-        const float pb[6] = {__double2float_rd(fmin(p.x, pf.x)), __double2float_rd(fmin(p.y, pf.y)),
-                             __double2float_rd(fmin(p.z, pf.z)), __double2float_ru(fmax(p.x, pf.x)),
-                             __double2float_ru(fmax(p.y, pf.y)), __double2float_ru(fmax(p.z, pf.z))};
-        grid_query_warp(c.G, ql, qh, [&](int t, const float (&bx)[6]) {
-            if (box_apart(pb, bx, c.xi_f)) return;
-            const int t0i = c.btri[3 * t], t1i = c.btri[3 * t + 1], t2i = c.btri[3 * t + 2];
-            if (vI == t0i || vI == t1i || vI == t2i) return;
-            if (c.dbc[vI] && c.dbc[t0i] && c.dbc[t1i] && c.dbc[t2i]) return;
-            push_cand(L, vI, t);
-        });
+    for (int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kQueryChunk; base < c.nbn;
+         base += nw * kQueryChunk) {
+        QuerySetup mine{};
+        const int sv = base + lane;
+        if (lane < kQueryChunk && sv < c.nbn) {
+            const int vI = c.bnode[sv];
+            const d3 p = ld(c.x, vI), dp = ld(c.p, vI);
+            const d3 pe = p + scl(dp, c.alpha);
+            const d3 mn = vmin3(p, pe), mx = vmax3(p, pe);
+            mine.ql[0] = cellc(mn.x - c.xi, c.G.inv);
+            mine.ql[1] = cellc(mn.y - c.xi, c.G.inv);
+            mine.ql[2] = cellc(mn.z - c.xi, c.G.inv);
+            mine.qh[0] = cellc(mx.x + c.xi, c.G.inv);
+            mine.qh[1] = cellc(mx.y + c.xi, c.G.inv);
+            mine.qh[2] = cellc(mx.z + c.xi, c.G.inv);
+            const d3 pf = p + dp;
+            const float pb[6] = {__double2float_rd(fmin(p.x, pf.x)), __double2float_rd(fmin(p.y, pf.y)),
+                                 __double2float_rd(fmin(p.z, pf.z)), __double2float_ru(fmax(p.x, pf.x)),
+                                 __double2float_ru(fmax(p.y, pf.y)), __double2float_ru(fmax(p.z, pf.z))};
+#pragma unroll
+            for (int d = 0; d < 6; ++d) mine.box[d] = pb[d];
+            mine.id[0] = vI;
+        }
+        const int nq = min(kQueryChunk, c.nbn - base);
+        for (int k = 0; k < nq; ++k) {
+            const QuerySetup q = bcast_setup(mine, k);
+            const int vI = q.id[0];
+            grid_query_warp(c.G, q.ql, q.qh, [&](int t, const float (&bx)[6]) {
+                if (box_apart(q.box, bx, c.xi_f)) return;
+                const int t0i = c.btri[3 * t], t1i = c.btri[3 * t + 1], t2i = c.btri[3 * t + 2];
+                if (vI == t0i || vI == t1i || vI == t2i) return;
+                if (c.dbc[vI] && c.dbc[t0i] && c.dbc[t1i] && c.dbc[t2i]) return;
+                push_cand(L, vI, t);
+            });
+        }
     }
 }
 
@@ -1424,30 +1489,42 @@ __global__ void __launch_bounds__(128) k_ccd_pt_eval(CcdCand c, CandList L)
 
 __global__ void k_ccd_ee(CcdCand c, CandList L)
 {
+    const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int eI = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; eI < c.nbe; eI += nw) {
-        const int a0 = c.bedge[2 * eI], a1 = c.bedge[2 * eI + 1];
-        const d3 ea0 = ld(c.x, a0), ea1 = ld(c.x, a1), da0 = ld(c.p, a0), da1 = ld(c.p, a1);
-        const d3 s0 = ea0 + scl(da0, c.alpha), s1 = ea1 + scl(da1, c.alpha);
-        const d3 mn = vmin3(vmin3(ea0, ea1), vmin3(s0, s1)), mx = vmax3(vmax3(ea0, ea1), vmax3(s0, s1));
-        int ql[3], qh[3];
-        ql[0] = cellc(mn.x - c.xi, c.G.inv);
-        ql[1] = cellc(mn.y - c.xi, c.G.inv);
-        ql[2] = cellc(mn.z - c.xi, c.G.inv);
-        qh[0] = cellc(mx.x + c.xi, c.G.inv);
-        qh[1] = cellc(mx.y + c.xi, c.G.inv);
-        qh[2] = cellc(mx.z + c.xi, c.G.inv);
-        float eb[6];
+    for (int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kQueryChunk; base < c.nbe;
+         base += nw * kQueryChunk) {
+        QuerySetup mine{};
+        const int e = base + lane;
+        if (lane < kQueryChunk && e < c.nbe) {
+            const int a0 = c.bedge[2 * e], a1 = c.bedge[2 * e + 1];
+            const d3 ea0 = ld(c.x, a0), ea1 = ld(c.x, a1), da0 = ld(c.p, a0), da1 = ld(c.p, a1);
+            const d3 s0 = ea0 + scl(da0, c.alpha), s1 = ea1 + scl(da1, c.alpha);
+            const d3 mn = vmin3(vmin3(ea0, ea1), vmin3(s0, s1)), mx = vmax3(vmax3(ea0, ea1), vmax3(s0, s1));
+            mine.ql[0] = cellc(mn.x - c.xi, c.G.inv);
+            mine.ql[1] = cellc(mn.y - c.xi, c.G.inv);
+            mine.ql[2] = cellc(mn.z - c.xi, c.G.inv);
+            mine.qh[0] = cellc(mx.x + c.xi, c.G.inv);
+            mine.qh[1] = cellc(mx.y + c.xi, c.G.inv);
+            mine.qh[2] = cellc(mx.z + c.xi, c.G.inv);
 #pragma unroll
-        for (int k = 0; k < 6; ++k) eb[k] = c.ebox[6 * (size_t)eI + k];
-        grid_query_warp(c.G, ql, qh, [&](int eJ, const float (&bx)[6]) {
-            if (eJ <= eI) return;
-            if (box_apart(eb, bx, c.xi_f)) return;
-            const int b0 = c.bedge[2 * eJ], b1 = c.bedge[2 * eJ + 1];
-            if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
-            if (c.dbc[a0] && c.dbc[a1] && c.dbc[b0] && c.dbc[b1]) return;
-            push_cand(L, eI, eJ);
-        });
+            for (int d = 0; d < 6; ++d) mine.box[d] = c.ebox[6 * (size_t)e + d];
+            mine.id[0] = e;
+            mine.id[1] = a0;
+            mine.id[2] = a1;
+        }
+        const int nq = min(kQueryChunk, c.nbe - base);
+        for (int k = 0; k < nq; ++k) {
+            const QuerySetup q = bcast_setup(mine, k);
+            const int eI = q.id[0], a0 = q.id[1], a1 = q.id[2];
+            grid_query_warp(c.G, q.ql, q.qh, [&](int eJ, const float (&bx)[6]) {
+                if (eJ <= eI) return;
+                if (box_apart(q.box, bx, c.xi_f)) return;
+                const int b0 = c.bedge[2 * eJ], b1 = c.bedge[2 * eJ + 1];
+                if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
+                if (c.dbc[a0] && c.dbc[a1] && c.dbc[b0] && c.dbc[b1]) return;
+                push_cand(L, eI, eJ);
+            });
+        }
     }
 }
 
