@@ -347,34 +347,51 @@ __device__ __forceinline__ XT apply_phase(const PcgArgs<VT, XT, PT>& a, XT beta,
         const auto v = ldcg(zp + j);
         return beta == XT(0) ? v.x : v.x + beta * v.y;
     };
-    // work items: elastic scalar rows, then 4 lanes per contact constraint
-    // (starting 4-aligned, so a constraint's lanes are 4 aligned lanes of one warp:
-    // the grid stride is a multiple of 32), then friction constraints
+    // work items: the scalar rows of the 3x3 block rows, two per thread and step in
+    // the FP32 solver (both rows' loads in flight: on large systems a thread has
+    // several rows and the loop is latency-bound otherwise), then 4 lanes per matrix-free contact
+    // constraint (starting 4-aligned, so a constraint's lanes are 4 aligned lanes of
+    // one warp: the grid stride is a multiple of 32), then friction constraints
     const int nrow = 3 * a.nv;
     const int cbeg = (nrow + 3) & ~3, cend = cbeg + 4 * ncon;
     const int total = cend + nfric;
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     XT v = 0;  // this thread's share, in the solver's precision; block sums are FP64
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < total; w += gridDim.x * blockDim.x) {
-        if (w < nrow) {
-            // one scalar row of the elastic 3x3 block rows per thread: row 3i + r
-            const int i = w / 3, r = w - 3 * i;
-            XT acc = 0;
-            const int K = a.ell_k, nv = a.nv;
-#pragma unroll 8
+    {
+        const int K = a.ell_k, nv = a.nv;
+        // (the FP64 solver keeps one row per step: its doubled registers spill)
+        constexpr int RS = sizeof(XT) == 4 ? 2 : 1;
+        for (int w = gtid; w < nrow; w += RS * gstride) {
+            const int wb = w + gstride;
+            const bool two = RS == 2 && wb < nrow;
+            const int i0 = w / 3, r0 = w - 3 * i0;
+            const int i1 = two ? wb / 3 : i0, r1 = two ? wb - 3 * i1 : r0;
+            XT acc0 = 0, acc1 = 0;
+#pragma unroll 4
             for (int k = 0; k < K; ++k) {
-                const size_t e = (size_t)k * nv + i;
-                const int j = __ldg(a.col + e);
-                const VT* B = a.val + 9 * e + 3 * r;
-                acc += (XT)__ldg(B) * pget(3 * j) + (XT)__ldg(B + 1) * pget(3 * j + 1) +
-                       (XT)__ldg(B + 2) * pget(3 * j + 2);
+                const size_t e0 = (size_t)k * nv + i0, e1 = (size_t)k * nv + i1;
+                const int j0 = __ldg(a.col + e0), j1 = __ldg(a.col + e1);
+                const VT* B0 = a.val + 9 * e0 + 3 * r0;
+                const VT* B1 = a.val + 9 * e1 + 3 * r1;
+                acc0 += (XT)__ldg(B0) * pget(3 * j0) + (XT)__ldg(B0 + 1) * pget(3 * j0 + 1) +
+                        (XT)__ldg(B0 + 2) * pget(3 * j0 + 2);
+                acc1 += (XT)__ldg(B1) * pget(3 * j1) + (XT)__ldg(B1 + 1) * pget(3 * j1 + 1) +
+                        (XT)__ldg(B1 + 2) * pget(3 * j1 + 2);
             }
-            const XT pw = pget(w);
-            zp_next[w].y = pw;
-            a.qe[w] = acc;
-            v += pw * acc;
-        } else if (w < cbeg) {
-            continue;
-        } else if (w < cend) {
+            const XT pw0 = pget(w);
+            zp_next[w].y = pw0;
+            a.qe[w] = acc0;
+            v += pw0 * acc0;
+            if (two) {
+                const XT pw1 = pget(wb);
+                zp_next[wb].y = pw1;
+                a.qe[wb] = acc1;
+                v += pw1 * acc1;
+            }
+        }
+    }
+    for (int w = cbeg + gtid; w < total; w += gstride) {
+        if (w < cend) {
             // contact constraint c, lane k of its group of 4
             const int j = (w - cbeg) >> 2, k = (w - cbeg) & 3;
             const int c = a.clist ? __ldg(a.clist + j) : j;
