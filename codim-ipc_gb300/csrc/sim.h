@@ -129,6 +129,8 @@ struct Sim {
     // blocks are zero with the row's own column; nnzb = ell_k * nv
     int nnzb = 0, ell_k = 0;
     DBuf<int> col, diag, tri_slot, hinge_slot;
+    DBuf<int> rowlen;  // real blocks per row: the rest of a row is zero padding that products skip
+    bool rows_uniform = false;  // at least 90% of the row slots are real blocks (products keep the fixed length)
     // rods: segments (2 ints, info E L t), hinges (3 ints, info E*bendMult lsum t), block slots
     int nrs = 0, nrh = 0;
     DBuf<int> rseg, rhinge, rseg_slot, rhinge_slot;

@@ -37,6 +37,7 @@ struct HostScene {
     // their own column and zero blocks
     int ell_k = 0;
     std::vector<int> col, diag, tri_slot, hinge_slot;
+    std::vector<int> rowlen;  // real blocks of each row (the rest of the row is zero padding)
     // rods: segments (2 each) with (E, L, t), hinges (3 each) with (E bendMult, lsum, t)
     std::vector<int> rseg, rhinge, rseg_slot, rhinge_slot;
     std::vector<double> rinfo, rhinfo;

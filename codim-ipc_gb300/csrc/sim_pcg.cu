@@ -83,6 +83,7 @@ struct PcgArgs {
     using XT2 = typename Pair<XT>::T;
     int nv, ell_k;
     const int* col;
+    const int* rowlen;  // real blocks of each row (a row's later slots are zero padding)
     const VT* val;
     const int* ckind;
     const int4* cverts;
@@ -358,7 +359,7 @@ __device__ __forceinline__ XT apply_phase(const PcgArgs<VT, XT, PT>& a, XT beta,
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     XT v = 0;  // this thread's share, in the solver's precision; block sums are FP64
     {
-        const int K = a.ell_k, nv = a.nv;
+        const int nv = a.nv;
         // (the FP64 solver keeps one row per step: its doubled registers spill)
         constexpr int RS = sizeof(XT) == 4 ? 2 : 1;
         for (int w = gtid; w < nrow; w += RS * gstride) {
@@ -367,16 +368,32 @@ __device__ __forceinline__ XT apply_phase(const PcgArgs<VT, XT, PT>& a, XT beta,
             const int i0 = w / 3, r0 = w - 3 * i0;
             const int i1 = two ? wb / 3 : i0, r1 = two ? wb - 3 * i1 : r0;
             XT acc0 = 0, acc1 = 0;
+            auto blk = [&](int k, int i, int r) -> XT {
+                const size_t e = (size_t)k * nv + i;
+                const int j = __ldg(a.col + e);
+                const VT* B = a.val + 9 * e + 3 * r;
+                return (XT)__ldg(B) * pget(3 * j) + (XT)__ldg(B + 1) * pget(3 * j + 1) +
+                       (XT)__ldg(B + 2) * pget(3 * j + 2);
+            };
+            if (!a.rowlen) {
+                // every row has the full length (uniform meshes): no per-row test in
+                // the loop (it costs time there); the second row repeats the first at
+                // the tail
+                const int K = a.ell_k;
 #pragma unroll 4
-            for (int k = 0; k < K; ++k) {
-                const size_t e0 = (size_t)k * nv + i0, e1 = (size_t)k * nv + i1;
-                const int j0 = __ldg(a.col + e0), j1 = __ldg(a.col + e1);
-                const VT* B0 = a.val + 9 * e0 + 3 * r0;
-                const VT* B1 = a.val + 9 * e1 + 3 * r1;
-                acc0 += (XT)__ldg(B0) * pget(3 * j0) + (XT)__ldg(B0 + 1) * pget(3 * j0 + 1) +
-                        (XT)__ldg(B0 + 2) * pget(3 * j0 + 2);
-                acc1 += (XT)__ldg(B1) * pget(3 * j1) + (XT)__ldg(B1 + 1) * pget(3 * j1 + 1) +
-                        (XT)__ldg(B1 + 2) * pget(3 * j1 + 2);
+                for (int k = 0; k < K; ++k) {
+                    acc0 += blk(k, i0, r0);
+                    acc1 += blk(k, i1, r1);
+                }
+            } else {
+                // only the real blocks of each row (on meshes that mix cloth, rods and
+                // particles most slots of the widest row's length are padding)
+                const int L0 = __ldg(a.rowlen + i0), L1 = two ? __ldg(a.rowlen + i1) : 0;
+#pragma unroll 4
+                for (int k = 0; k < max(L0, L1); ++k) {
+                    if (k < L0) acc0 += blk(k, i0, r0);
+                    if (k < L1) acc1 += blk(k, i1, r1);
+                }
             }
             const XT pw0 = pget(w);
             zp_next[w].y = pw0;
@@ -670,6 +687,7 @@ int solve(Sim* s, const XT* b, XT* x, double tol, int maxit, int* iters, double*
     a.nv = s->nv;
     a.ell_k = s->ell_k;
     a.col = s->col.p;
+    a.rowlen = s->rows_uniform ? nullptr : s->rowlen.p;
     a.val = reinterpret_cast<const VT*>(s->folded ? s->hval_op.p : s->hval.p);
     a.ckind = s->ckind.p;
     a.cverts = s->cverts.p;

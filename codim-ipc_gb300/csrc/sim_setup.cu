@@ -325,6 +325,8 @@ int build_host_scene(HostScene& S, int nv, const double* X, int nt, const int* t
     S.ell_k = K;
     S.col.assign((size_t)K * nv, 0);
     S.diag.resize(nv);
+    S.rowlen.resize(nv);
+    for (int i = 0; i < nv; ++i) S.rowlen[i] = (int)adj[i].size();
     for (int i = 0; i < nv; ++i)
         for (int k = 0; k < K; ++k) {
             S.col[(size_t)k * nv + i] = k < (int)adj[i].size() ? adj[i][k] : i;
@@ -395,12 +397,17 @@ int sim_upload(Sim* s, const HostScene& S)
     s->cell = S.cell;
     s->nnzb = (int)S.col.size();
     s->ell_k = S.ell_k;
+    {
+        long long real = 0;
+        for (int L : S.rowlen) real += L;
+        s->rows_uniform = 10 * real >= 9 * (long long)S.ell_k * S.nv;
+    }
     cudaError_t e = cudaSuccess;
 #define UP(a, b)                       \
     if (e == cudaSuccess) e = up(a, b);
     UP(s->tri, S.tri) UP(s->hinge, S.hinge) UP(s->bnode, S.bnode) UP(s->bedge, S.bedge) UP(s->btri, S.btri)
     UP(s->P, S.P) UP(s->vol, S.vol) UP(s->hinfo, S.hinfo) UP(s->mass, S.mass) UP(s->b, S.b) UP(s->X0, S.X0)
-    UP(s->col, S.col) UP(s->diag, S.diag) UP(s->tri_slot, S.tri_slot)
+    UP(s->col, S.col) UP(s->diag, S.diag) UP(s->rowlen, S.rowlen) UP(s->tri_slot, S.tri_slot)
     UP(s->hinge_slot, S.hinge_slot)
     UP(s->rseg, S.rseg) UP(s->rhinge, S.rhinge) UP(s->rseg_slot, S.rseg_slot) UP(s->rhinge_slot, S.rhinge_slot)
     UP(s->rinfo, S.rinfo) UP(s->rhinfo, S.rhinfo)

@@ -33,14 +33,15 @@ namespace cipc {
 static inline int nblk(long long n, int bs) { return n > 0 ? (int)((n + bs - 1) / bs) : 1; }
 
 template <typename VT, typename XT>
-__global__ void __launch_bounds__(256) k_bsr_spmv(int nv, int ell_k, const int* __restrict__ col,
+__global__ void __launch_bounds__(256) k_bsr_spmv(int nv, const int* __restrict__ rowlen, const int* __restrict__ col,
                                                   const VT* __restrict__ val, const XT* __restrict__ x,
                                                   XT* __restrict__ y)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
     XT a0 = 0, a1 = 0, a2 = 0;
-    for (int k = 0; k < ell_k; ++k) {
+    const int L = rowlen[i];  // the row's real blocks (the rest is zero padding)
+    for (int k = 0; k < L; ++k) {
         const size_t e = (size_t)k * nv + i;
         const int j = col[e];
         const VT* B = val + 9 * e;
@@ -239,7 +240,7 @@ static void apply_H(SolveCtx& C, const XT* x, XT* y)
 {
     Sim* s = C.s;
     const bool fo = s->folded;
-    k_bsr_spmv<VT, XT><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, s->ell_k, s->col.p,
+    k_bsr_spmv<VT, XT><<<nblk(s->nv, 256), 256, 0, C.st>>>(s->nv, s->rowlen.p, s->col.p,
                                                             (const VT*)(fo ? s->hval_op.p : s->hval.p), x, y);
     const int ncon = s->prm.withCollision ? s->ncon : 0;
     const int nfric = (s->prm.withCollision && s->prm.mu > 0) ? s->nfric : 0;

@@ -782,7 +782,7 @@ void sim_destroy(Sim* s)
     s->crest.release();
     s->frest.release();
     s->fold_cnt.release();
-    for (DBuf<int>* b : {&s->tri, &s->hinge, &s->bnode, &s->bedge, &s->btri, &s->dbc_idx, &s->col,
+    for (DBuf<int>* b : {&s->tri, &s->hinge, &s->bnode, &s->bedge, &s->btri, &s->dbc_idx, &s->col, &s->rowlen,
                          &s->diag, &s->tri_slot, &s->hinge_slot, &s->ckind, &s->cmult, &s->fkind, &s->fmult,
                          &s->rseg, &s->rhinge, &s->rseg_slot, &s->rhinge_slot, &s->tet, &s->tet_slot,
                          &s->pkind})

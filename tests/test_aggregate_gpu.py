@@ -50,15 +50,23 @@ def _step(draped, precision, precond, newton_tol, pcg_tol, max_newton=200):
 
 @pytest.mark.parametrize("precision", [F.FP64, F.MIXED])
 def test_aggregate_steps_match_block_jacobi(cuda, draped, precision):
+    """Bar: 1e-7 of the bounding-box diagonal plus twice the spread of two
+    block-Jacobi runs of the same step.  The step takes ~70 Newton iterations of
+    sliding contact with friction; the gradient and Hessian are summed with
+    atomics, so two runs of one preconditioner differ in their last bits, and
+    over such a step that spread grows to ~1e-6 of the diagonal in mixed
+    precision (two preconditioners differ by the same mechanism)."""
     X = draped[0]
     diag = np.linalg.norm(X.max(0) - X.min(0))
     st_bj, x_bj = _step(draped, precision, F.PRECOND_BLOCK_JACOBI, 1e-6, 1e-10)
+    _, x_bj2 = _step(draped, precision, F.PRECOND_BLOCK_JACOBI, 1e-6, 1e-10, max_newton=st_bj.newton_iters)
     st_ag, x_ag = _step(draped, precision, F.PRECOND_AGGREGATE, 1e-6, 1e-10, max_newton=st_bj.newton_iters)
     assert st_ag.precond_fallbacks == 0
     assert st_ag.min_dist2 > 0 and st_bj.min_dist2 > 0
     assert st_ag.newton_iters == st_bj.newton_iters
+    spread = np.abs(x_bj2 - x_bj).max() / diag
     err = np.abs(x_ag - x_bj).max() / diag
-    assert err < 1e-7, (err, st_bj.as_dict(), st_ag.as_dict())
+    assert err < 1e-7 + 2 * spread, (err, spread, st_bj.as_dict(), st_ag.as_dict())
 
 
 def test_aggregate_needs_fewer_iterations(cuda, draped):
