@@ -2,8 +2,8 @@
 of the diagonal blocks of vertex aggregates of up to 32 mesh neighbours.
 
 Checks, on a draped cloth-on-sphere scene (60x60 cloth, contact and friction):
-  * from the same state, the step solved with aggregate block Jacobi ends where the
-    block-Jacobi step ends (tight Newton and PCG tolerances: the preconditioner
+  * from the same state, three Newton iterations solved with aggregate block Jacobi
+    end where they end with block Jacobi (tight PCG tolerance: the preconditioner
     changes iteration counts, not the solution), in FP64 and in mixed precision;
   * it needs fewer PCG iterations than block Jacobi (the reason it exists), and
     no solve falls back to block Jacobi.
@@ -50,23 +50,25 @@ def _step(draped, precision, precond, newton_tol, pcg_tol, max_newton=200):
 
 @pytest.mark.parametrize("precision", [F.FP64, F.MIXED])
 def test_aggregate_steps_match_block_jacobi(cuda, draped, precision):
-    """Bar: 1e-7 of the bounding-box diagonal plus twice the spread of two
-    block-Jacobi runs of the same step.  The step takes ~70 Newton iterations of
-    sliding contact with friction; the gradient and Hessian are summed with
-    atomics, so two runs of one preconditioner differ in their last bits, and
-    over such a step that spread grows to ~1e-6 of the diagonal in mixed
-    precision (two preconditioners differ by the same mechanism)."""
+    """The first three Newton iterations of a step (each linear solve to a relative
+    residual of 1e-10) with aggregate block Jacobi end where they end with block
+    Jacobi.  Bar: 1e-8 of the bounding-box diagonal plus twice the spread of two
+    block-Jacobi runs (gradient and Hessian are summed with atomics, so two runs
+    differ in their last bits).  Whole steps are not compared: on this sliding,
+    frictional contact a step takes 70-135 Newton iterations and 100+ line-search
+    halvings decided on FP64 energy differences, and two solves that agree to
+    1e-10 can end such a step ~1e-7 of the diagonal apart."""
     X = draped[0]
     diag = np.linalg.norm(X.max(0) - X.min(0))
-    st_bj, x_bj = _step(draped, precision, F.PRECOND_BLOCK_JACOBI, 1e-6, 1e-10)
-    _, x_bj2 = _step(draped, precision, F.PRECOND_BLOCK_JACOBI, 1e-6, 1e-10, max_newton=st_bj.newton_iters)
-    st_ag, x_ag = _step(draped, precision, F.PRECOND_AGGREGATE, 1e-6, 1e-10, max_newton=st_bj.newton_iters)
+    st_bj, x_bj = _step(draped, precision, F.PRECOND_BLOCK_JACOBI, 1e-30, 1e-10, max_newton=3)
+    _, x_bj2 = _step(draped, precision, F.PRECOND_BLOCK_JACOBI, 1e-30, 1e-10, max_newton=3)
+    st_ag, x_ag = _step(draped, precision, F.PRECOND_AGGREGATE, 1e-30, 1e-10, max_newton=3)
     assert st_ag.precond_fallbacks == 0
     assert st_ag.min_dist2 > 0 and st_bj.min_dist2 > 0
-    assert st_ag.newton_iters == st_bj.newton_iters
+    assert st_ag.newton_iters == st_bj.newton_iters == 3
     spread = np.abs(x_bj2 - x_bj).max() / diag
     err = np.abs(x_ag - x_bj).max() / diag
-    assert err < 1e-7 + 2 * spread, (err, spread, st_bj.as_dict(), st_ag.as_dict())
+    assert err < 1e-8 + 2 * spread, (err, spread, st_bj.as_dict(), st_ag.as_dict())
 
 
 def test_aggregate_needs_fewer_iterations(cuda, draped):
