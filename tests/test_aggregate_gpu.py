@@ -52,9 +52,12 @@ def _step(draped, precision, precond, newton_tol, pcg_tol, max_newton=200):
 def test_aggregate_steps_match_block_jacobi(cuda, draped, precision):
     """The first three Newton iterations of a step (each linear solve to a relative
     residual of 1e-10) with aggregate block Jacobi end where they end with block
-    Jacobi.  Bar: 1e-8 of the bounding-box diagonal plus twice the spread of two
+    Jacobi.  Bar: 1e-7 of the bounding-box diagonal plus twice the spread of two
     block-Jacobi runs (gradient and Hessian are summed with atomics, so two runs
-    differ in their last bits).  Whole steps are not compared: on this sliding,
+    differ in their last bits).  Two solves that each reach a relative residual of
+    1e-10 differ by up to cond(H) x 1e-10 relative in the solution, and the
+    contact-stiffened Newton systems here have cond(H) ~ 1e5-1e6: the FP64 runs
+    end ~2e-8 of the diagonal apart.  Whole steps are not compared: on this sliding,
     frictional contact a step takes 70-135 Newton iterations and 100+ line-search
     halvings decided on FP64 energy differences, and two solves that agree to
     1e-10 can end such a step ~1e-7 of the diagonal apart."""
@@ -68,7 +71,7 @@ def test_aggregate_steps_match_block_jacobi(cuda, draped, precision):
     assert st_ag.newton_iters == st_bj.newton_iters == 3
     spread = np.abs(x_bj2 - x_bj).max() / diag
     err = np.abs(x_ag - x_bj).max() / diag
-    assert err < 1e-8 + 2 * spread, (err, spread, st_bj.as_dict(), st_ag.as_dict())
+    assert err < 1e-7 + 2 * spread, (err, spread, st_bj.as_dict(), st_ag.as_dict())
 
 
 def test_aggregate_needs_fewer_iterations(cuda, draped):
