@@ -473,14 +473,15 @@ def timestep_variants(args):
            "learned": {"systems": pc.num_systems(), "epochs": args.ts_epochs,
                        "train_s": round(time.perf_counter() - t0, 2), "loss_before": round(loss_before, 4),
                        "loss_after": round(loss_after, 4)}}
-    names = ["fp64_block_jacobi", "mixed_block_jacobi", "mixed_learned", "mixed_aggregate"]
+    names = ["fp64_block_jacobi", "mixed_block_jacobi", "mixed_learned", "mixed_aggregate", "mixed_aggregate_inexact"]
     if args.ts_inexact:
-        names += ["fp64_block_jacobi_inexact", "mixed_aggregate_inexact"]
+        names += ["fp64_block_jacobi_inexact"]
     out.update(compare(sc, names, args.ts_warm, args.ts_steps, x0, v0, k0, pc))
     out["roofline_pcg"] = {"mixed_block_jacobi": pcg_roofline(sc, out["mixed_block_jacobi"], True),
                            "fp64_block_jacobi": pcg_roofline(sc, out["fp64_block_jacobi"], False)}
     out["note"] = ("aggregate: exact inverses of the diagonal blocks of vertex aggregates (CIPC_PRECOND_AGGREGATE); "
-                   "*_inexact (--ts-inexact): Eisenstat-Walker forcing term (cipc_step_params.forcing = 1); the "
+                   "*_inexact: Eisenstat-Walker forcing term (cipc_step_params.forcing = 1; the FP64 one with "
+                   "--ts-inexact); the "
                    "Newton tolerance is the same for every variant; the forcing term is not combined with the "
                    "learned correction")
     pc.close()
@@ -811,7 +812,7 @@ def main():
     ap.add_argument("--ts-warm", type=int, default=10, help="draping steps before the measured steps")
     ap.add_argument("--ts-steps", type=int, default=50, help="measured steps per variant")
     ap.add_argument("--ts-epochs", type=int, default=20, help="training epochs of the learned correction")
-    ap.add_argument("--ts-inexact", action="store_true", help="add the inexact-Newton (forcing term) variants")
+    ap.add_argument("--ts-inexact", action="store_true", help="add the FP64 inexact-Newton (forcing term) variant")
     ap.add_argument("--ts-cpu-steps", type=int, default=0,
                     help="steps of the CPU oracle on the full cloth-on-sphere scene from the draped state (minutes "
                          "per step)")
