@@ -14,7 +14,11 @@
 //
 // Layout in HBM: vertices by aggregate (voff / verts), the dense m x m inverse of
 // aggregate a (m = 3 x its vertices, <= 96) at inv + boff[a], symmetric, so row
-// and column order coincide and a warp's loads of one column are coalesced.  The
+// and column order coincide and a warp's loads of one column are coalesced.
+// Vertices with no neighbour in the rows (free particles) are packed 32 to an
+// aggregate that keeps only each vertex's own 3x3 block (9 entries per vertex,
+// boff[a + 1] - boff[a] = 9 x its vertices): block Jacobi for them, without the
+// mostly-zero dense block; contact blocks between two of them are left out there.  The
 // blocks are assembled in FP64 (atomic adds into the zeroed FP64 staging copy),
 // scaled to unit diagonal and inverted by Gauss-Jordan elimination without
 // pivoting (the blocks are symmetric positive definite) in shared memory, one CTA
@@ -64,7 +68,8 @@ inline int nblk(long long n, int bs) { return n > 0 ? (int)((n + bs - 1) / bs) :
 // kAggMax); (2) a remaining vertex joins the aggregate most of its neighbours
 // belong to while it has room, else starts a new one; (3) vertices with no
 // neighbours are packed in index order, kAggMax to an aggregate.
-void aggregate(int nv, int K, const std::vector<int>& col, std::vector<int>& agg, int& nagg)
+void aggregate(int nv, int K, const std::vector<int>& col, std::vector<int>& agg, int& nagg,
+               std::vector<uint8_t>& packed)
 {
     agg.assign(nv, -1);
     std::vector<int> size;
@@ -116,12 +121,14 @@ void aggregate(int nv, int K, const std::vector<int>& col, std::vector<int>& agg
         agg[i] = best;
         ++size[best];
     }
+    packed.assign(nagg, 0);
     int open = -1;
     for (int i = 0; i < nv; ++i) {
         if (agg[i] >= 0) continue;
         if (open < 0 || size[open] >= kAggMax) {
             open = nagg++;
             size.push_back(0);
+            packed.push_back(1);
         }
         agg[i] = open;
         ++size[open];
@@ -135,8 +142,9 @@ int build_state(Sim* s, AggState* st)
     cudaError_t e = cudaMemcpy(col.data(), s->col.p, sizeof(int) * col.size(), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return set_cuda_error(e, "aggregate set-up");
     std::vector<int> agg;
+    std::vector<uint8_t> packed;
     int nagg = 0;
-    aggregate(nv, K, col, agg, nagg);
+    aggregate(nv, K, col, agg, nagg, packed);
     std::vector<int> voff(nagg + 1, 0), verts(nv), vloc(nv);
     for (int i = 0; i < nv; ++i) ++voff[agg[i] + 1];
     for (int a = 0; a < nagg; ++a) voff[a + 1] += voff[a];
@@ -152,7 +160,7 @@ int build_state(Sim* s, AggState* st)
     for (int a = 0; a < nagg; ++a) {
         const int m = 3 * (voff[a + 1] - voff[a]);
         max_m = std::max(max_m, m);
-        boff[a + 1] = boff[a] + (long long)m * m;
+        boff[a + 1] = boff[a] + (packed[a] ? 3LL * m : (long long)m * m);
     }
     if (boff[nagg] >= (1ll << 31)) return set_error(CIPC_ERR_INVALID_ARG, "aggregate blocks exceed 2^31 entries");
     std::vector<int> ellmap((size_t)K * nv, -1);
@@ -162,6 +170,10 @@ int build_state(Sim* s, AggState* st)
         // onto the diagonal block and add nothing)
         if (j < 0 || j >= nv || agg[i] != agg[j]) continue;
         const int a = agg[i], m = 3 * (voff[a + 1] - voff[a]);
+        if (packed[a]) {
+            if (j == i) ellmap[q] = (int)(boff[a] + 9LL * vloc[i]);
+            continue;
+        }
         ellmap[q] = (int)(boff[a] + (long long)(3 * vloc[i]) * m + 3 * vloc[j]);
     }
     st->nv = nv;
@@ -184,18 +196,27 @@ int build_state(Sim* s, AggState* st)
     return CIPC_OK;
 }
 
+// stored block layout of aggregate a: dense m x m (rows m apart), or for a pack of
+// isolated vertices their 3x3 blocks one after another (rows 3 apart)
+__device__ __forceinline__ bool agg_packed(const int* voff, const long long* boff, int a)
+{
+    const int sv = voff[a + 1] - voff[a];
+    return sv > 1 && boff[a + 1] - boff[a] == 9LL * sv;
+}
+
 // elastic rows: ELL entry q = k nv + i lands at A[ellmap[q]] (rows of the
-// aggregate block are m apart)
+// aggregate block are m apart, 3 in a pack of isolated vertices)
 template <typename VT>
 __global__ void k_agg_ell(long long n, int nv, const int* __restrict__ ellmap, const int* __restrict__ vagg,
-                          const int* __restrict__ voff, const VT* __restrict__ val, double* A)
+                          const int* __restrict__ voff, const long long* __restrict__ boff,
+                          const VT* __restrict__ val, double* A)
 {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     const int o = ellmap[q];
     if (o < 0) return;
     const int i = (int)(q % nv), a = vagg[i];
-    const int m = 3 * (voff[a + 1] - voff[a]);
+    const int m = agg_packed(voff, boff, a) ? 3 : 3 * (voff[a + 1] - voff[a]);
     const VT* B = val + 9 * q;
 #pragma unroll
     for (int r = 0; r < 3; ++r)
@@ -222,10 +243,13 @@ __device__ __forceinline__ void agg_add_blocks(const AggMaps& M, const int (&id)
     for (int p = 0; p < cnv; ++p) {
         if (M.proj[id[p]]) continue;
         const int a = M.vagg[id[p]];
-        const int m = 3 * (M.voff[a + 1] - M.voff[a]);
+        const bool pk = agg_packed(M.voff, M.boff, a);
+        const int m = pk ? 3 : 3 * (M.voff[a + 1] - M.voff[a]);
         for (int q = 0; q < cnv; ++q) {
             if (M.proj[id[q]] || M.vagg[id[q]] != a) continue;
-            double* D = A + M.boff[a] + (size_t)(3 * M.vloc[id[p]]) * m + 3 * M.vloc[id[q]];
+            if (pk && id[q] != id[p]) continue;  // a pack keeps each vertex's own block only
+            double* D = pk ? A + M.boff[a] + 9 * (size_t)M.vloc[id[p]]
+                           : A + M.boff[a] + (size_t)(3 * M.vloc[id[p]]) * m + 3 * M.vloc[id[q]];
             for (int r = 0; r < 3; ++r)
                 for (int t = 0; t < 3; ++t) {
                     const double v = blk(p, q, r, t);
@@ -285,11 +309,32 @@ __global__ void __launch_bounds__(kInvThreads) k_agg_invert(const int* __restric
     GT* S = reinterpret_cast<GT*>(smem_raw);
     const int a = blockIdx.x;
     const int m = 3 * (voff[a + 1] - voff[a]);
+    const double* Ab = A + boff[a];
+    if (agg_packed(voff, boff, a)) {
+        // pack of isolated vertices: each vertex's 3x3 block (FP64 cofactors)
+        PT* out = inv + boff[a];
+        for (int v = threadIdx.x; v < m / 3; v += blockDim.x) {
+            const double* B = Ab + 9 * v;
+            const double c00 = B[4] * B[8] - B[5] * B[7], c01 = B[5] * B[6] - B[3] * B[8],
+                         c02 = B[3] * B[7] - B[4] * B[6];
+            const double det = B[0] * c00 + B[1] * c01 + B[2] * c02;
+            if (!(B[0] > 0) || !(det > 0) || !(det < INFINITY)) {
+                atomicExch(flag, 1);
+                continue;
+            }
+            const double id = 1.0 / det;
+            const double I[9] = {c00 * id, (B[2] * B[7] - B[1] * B[8]) * id, (B[1] * B[5] - B[2] * B[4]) * id,
+                                 c01 * id, (B[0] * B[8] - B[2] * B[6]) * id, (B[2] * B[3] - B[0] * B[5]) * id,
+                                 c02 * id, (B[1] * B[6] - B[0] * B[7]) * id, (B[0] * B[4] - B[1] * B[3]) * id};
+            for (int r = 0; r < 3; ++r)
+                for (int t = 0; t < 3; ++t) out[9 * v + 3 * r + t] = (PT)(0.5 * (I[3 * r + t] + I[3 * t + r]));
+        }
+        return;
+    }
     GT* fcol = S + (size_t)m * m;
     __shared__ double dsc[3 * kAggMax];
     __shared__ GT piv;
     __shared__ int bad;
-    const double* Ab = A + boff[a];
     // symmetric diagonal scaling (unit diagonal) before the elimination: the
     // contact blocks make the rows' scales differ by orders of magnitude
     for (int i = threadIdx.x; i < m; i += blockDim.x) {
@@ -345,7 +390,8 @@ int setup_impl(Sim* s, AggState* st)
     if (e != cudaSuccess) return set_cuda_error(e, "aggregate set-up");
     const VT* val = reinterpret_cast<const VT*>(s->folded ? s->hval_op.p : s->hval.p);
     const long long ne = (long long)s->ell_k * s->nv;
-    k_agg_ell<VT><<<nblk(ne, 256), 256, 0, str>>>(ne, s->nv, st->ellmap.p, st->vagg.p, st->voff.p, val, st->A.p);
+    k_agg_ell<VT><<<nblk(ne, 256), 256, 0, str>>>(ne, s->nv, st->ellmap.p, st->vagg.p, st->voff.p, st->boff.p, val,
+                                                  st->A.p);
     AggMaps M{st->vagg.p, st->vloc.p, st->voff.p, st->boff.p, s->proj.p};
     const int ncon = s->prm.withCollision ? s->ncon : 0;
     const int nfric = (s->prm.withCollision && s->prm.mu > 0) ? s->nfric : 0;

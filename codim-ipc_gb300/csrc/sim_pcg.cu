@@ -228,7 +228,8 @@ __device__ __forceinline__ bool grid_allreduce(const AT (&v)[N], double (&out)[N
 // Aggregate block Jacobi, one aggregate per warp (up to 32 vertices, lane v owns
 // vertex v): rfun(j) performs the phase's update of scalar row j and returns r_j,
 // the warp stages the aggregate's r in shared memory and forms z = B r row by row
-// (B symmetric: lane `row` reads column entries of consecutive rows, coalesced);
+// (B symmetric: lane `row` reads column entries of consecutive rows, coalesced),
+// or, for a pack of isolated vertices, lane v applies vertex v's own 3x3 block;
 // z_j goes to zout[j].x.  Adds the lanes' shares of (r, z) and (r, r).
 constexpr int kAggRows = 96;
 template <typename VT, typename XT, typename PT, typename XT2, typename RF>
@@ -249,7 +250,24 @@ __device__ __forceinline__ void agg_phase(const PcgArgs<VT, XT, PT>& a, XT2* zou
             }
         }
         __syncwarp();
-        const PT* B = a.ainv + __ldg(a.aboff + g);
+        const long long bo = __ldg(a.aboff + g);
+        const PT* B = a.ainv + bo;
+        if (sv > 1 && __ldg(a.aboff + g + 1) - bo == 9LL * sv) {
+            // a pack of isolated vertices: each vertex's own 3x3 block
+            if (lane < sv) {
+                const int i = __ldg(a.averts + v0 + lane);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const PT* Bc = B + 9 * lane + 3 * c;
+                    const XT z = (XT)__ldg(Bc) * rs[wib][3 * lane] + (XT)__ldg(Bc + 1) * rs[wib][3 * lane + 1] +
+                                 (XT)__ldg(Bc + 2) * rs[wib][3 * lane + 2];
+                    zout[3 * i + c].x = z;
+                    rz += rs[wib][3 * lane + c] * z;
+                }
+            }
+            __syncwarp();
+            continue;
+        }
         for (int row = lane; row < m; row += 32) {
             // twelve independent loads in flight per step: the blocks are read
             // from L2 and the loop is latency-bound otherwise
