@@ -8,9 +8,10 @@
 // and inverts, for every Newton system, each aggregate's whole diagonal block of
 // the operator: the elastic rows (with the folded constraints) plus the
 // intra-aggregate blocks of the constraints still applied matrix-free.  The
-// solver applies z_I = (H_II)^-1 r_I one aggregate per warp inside its update
-// phase, so it costs no extra grid-wide barrier; on the draped 200x200 cloth it
-// halves the PCG iterations of block Jacobi.
+// solver applies z_I = (H_II)^-1 r_I inside its update phase (each block owns a
+// balanced range of aggregates, agg_rounds), so it costs no extra grid-wide
+// barrier; on the draped 200x200 cloth it halves the PCG iterations of block
+// Jacobi.
 //
 // Layout in HBM: vertices by aggregate (voff / verts), the dense m x m inverse of
 // aggregate a (m = 3 x its vertices, <= 96) at inv + boff[a], symmetric, so row
@@ -47,13 +48,17 @@ struct AggState {
     long long entries = 0;
     DBuf<int> voff, verts, vagg, vloc, ellmap, flag;
     DBuf<long long> boff;
+    std::vector<int> h_voff;        // host copies for the solver's rounds
+    std::vector<long long> h_boff;
+    int rk_grid = 0, rk_rows = 0, rk_max = 0, rk_loads = 0;  // limits the rounds were built for
+    DBuf<int> bround, rstart;
     DBuf<double> A;   // assembled blocks
     DBuf<char> inv;   // inverses (float or double)
     int* flag_host = nullptr;
     ~AggState()
     {
         if (flag_host) cudaFreeHost(flag_host);
-        for (DBuf<int>* b : {&voff, &verts, &vagg, &vloc, &ellmap, &flag}) b->release();
+        for (DBuf<int>* b : {&voff, &verts, &vagg, &vloc, &ellmap, &flag, &bround, &rstart}) b->release();
         boff.release();
         A.release();
         inv.release();
@@ -179,6 +184,8 @@ int build_state(Sim* s, AggState* st)
     st->nv = nv;
     st->nagg = nagg;
     st->max_m = max_m;
+    st->h_voff = voff;
+    st->h_boff = boff;
     st->entries = boff[nagg];
     if (st->voff.alloc(nagg + 1) || st->verts.alloc(nv) || st->vagg.alloc(nv) || st->vloc.alloc(nv) ||
         st->ellmap.alloc(ellmap.size()) || st->boff.alloc(nagg + 1) || st->flag.alloc(1) ||
@@ -451,6 +458,65 @@ AggView agg_view(const Sim* s)
     const AggState* st = static_cast<const AggState*>(s->agg);
     if (!st || !s->agg_ready) return AggView{0, nullptr, nullptr, nullptr, nullptr};
     return AggView{st->nagg, st->voff.p, st->verts.p, st->boff.p, st->inv.p};
+}
+
+int agg_rounds(Sim* s, int grid, int rows, int maxagg, int loads, const int** bround, const int** rstart)
+{
+    AggState* st = static_cast<AggState*>(s->agg);
+    if (!st || grid < 1 || rows < st->max_m || maxagg < 1 || loads < 3)
+        return set_error(CIPC_ERR_INVALID_ARG, "aggregate rounds: no aggregates or limits below the largest block");
+    if (st->rk_grid != grid || st->rk_rows != rows || st->rk_max != maxagg || st->rk_loads != loads) {
+        // The phase is latency-bound: a warp takes one item (a column slice of a
+        // dense product) per L2 round trip, a thread two rows of updates per round
+        // trip.  Cost of an aggregate in those units (x 1024 for 256-thread blocks
+        // of 8 warps): 128 per item, 10 per scalar row (its loads, the staging and
+        // the store of z).
+        const int nagg = st->nagg;
+        std::vector<long long> cost(nagg + 1, 0);
+        for (int g = 0; g < nagg; ++g) {
+            const int sv = st->h_voff[g + 1] - st->h_voff[g], m = 3 * sv;
+            const bool pk = sv > 1 && st->h_boff[g + 1] - st->h_boff[g] == 9LL * sv;
+            const int rg = (m + 31) / 32, C = std::max(1, loads / rg);
+            const long long items = pk ? 0 : (m + C - 1) / C;
+            cost[g + 1] = cost[g] + 128 * items + 10LL * m;
+        }
+        const long long T = cost[nagg];
+        std::vector<int> br(grid + 1), rs;
+        rs.reserve(nagg + 1);
+        int a = 0;
+        for (int b = 0; b < grid; ++b) {
+            br[b] = (int)rs.size();
+            // block b: the aggregates whose cost prefix lies in [T b / grid, T (b + 1) / grid)
+            const long long end = T * (b + 1) / grid;
+            int hi = a;
+            while (hi < nagg && (b + 1 == grid || cost[hi] < end)) ++hi;
+            for (int g = a; g < hi;) {
+                rs.push_back(g);
+                int nr = 0, cnt = 0;
+                while (g < hi && cnt < maxagg && nr + 3 * (st->h_voff[g + 1] - st->h_voff[g]) <= rows) {
+                    nr += 3 * (st->h_voff[g + 1] - st->h_voff[g]);
+                    ++cnt;
+                    ++g;
+                }
+            }
+            a = hi;
+        }
+        br[grid] = (int)rs.size();
+        rs.push_back(nagg);
+        cudaStreamSynchronize(s->stream);
+        if (st->bround.alloc(br.size()) != cudaSuccess || st->rstart.alloc(rs.size()) != cudaSuccess)
+            return set_error(CIPC_ERR_CUDA, "aggregate rounds");
+        cudaError_t e = cudaMemcpy(st->bround.p, br.data(), sizeof(int) * br.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(st->rstart.p, rs.data(), sizeof(int) * rs.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return set_cuda_error(e, "aggregate rounds upload");
+        st->rk_grid = grid;
+        st->rk_rows = rows;
+        st->rk_max = maxagg;
+        st->rk_loads = loads;
+    }
+    *bround = st->bround.p;
+    *rstart = st->rstart.p;
+    return CIPC_OK;
 }
 
 void agg_release(Sim* s)

@@ -82,6 +82,13 @@ struct AggView {
     const void* inv;        // inverses (float or double per precision), symmetric m x m, m = 3 x vertices
 };
 AggView agg_view(const Sim* s);
+// The solver's rounds of aggregates for a grid of `grid` blocks: block b owns a
+// contiguous range of aggregates of about equal cost (the solver's items, of
+// `loads` loads per lane, and rows), cut into rounds of at most `rows` scalar
+// rows and `maxagg` aggregates; rounds [bround[b], bround[b + 1]) of block b,
+// round q = aggregates [rstart[q], rstart[q + 1]).  Built on the host when the
+// grid or the limits change (device arrays owned by the aggregate state).
+int agg_rounds(Sim* s, int grid, int rows, int maxagg, int loads, const int** bround, const int** rstart);
 void agg_release(Sim* s);
 
 }  // namespace cipc

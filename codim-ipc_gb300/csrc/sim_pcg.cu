@@ -19,7 +19,7 @@
 //            stores), the matrix-free contact and friction parts are accumulated
 //            into q_c with atomics, and p_k^T H p_k is summed element by element.
 //   update   alpha = (r,z)/(p,Hp); x += alpha p; r -= alpha (q_e + q_c); q_c = 0;
-//            z = M^-1 r (per vertex, or per aggregate by one warp); (r,z), (r,r).
+//            z = M^-1 r (per vertex, or per aggregate by the block's warps); (r,z), (r,r).
 // Each phase ends with a grid-wide sum (grid_allreduce): per-block partials, a
 // release/acquire arrival counter, and a fixed-order sum of the partials read by
 // every block, so every block takes the same stop decision.  The atomics of the
@@ -54,8 +54,9 @@ struct PcgScalars {
     int pad;
     // arrivals (monotone: gridDim.x per reduction), on its own 128-byte line
     alignas(128) unsigned int arrive;
-    // with tracing on: block 0's time (ns) in apply, reduction 1, -, update,
-    // reduction 2, -, summed over iterations
+    // with tracing on: block 0's time (ns) in apply, reduction 1, the aggregate
+    // rows (part of update), update, reduction 2, the aggregate items (part of
+    // update), summed over iterations
     unsigned long long tphase[6];
 };
 
@@ -97,12 +98,15 @@ struct PcgArgs {
     const uint8_t* proj;
     const PT* pinv;
     // aggregate block Jacobi (nagg > 0): vertices of aggregate g at
-    // averts[avoff[g] .. avoff[g + 1]), its symmetric inverse block at ainv + aboff[g]
+    // averts[avoff[g] .. avoff[g + 1]), its symmetric inverse block at ainv + aboff[g];
+    // the blocks' rounds of aggregates (agg_phase)
     int nagg;
     const int* avoff;
     const int* averts;
     const long long* aboff;
     const PT* ainv;
+    const int* abround;
+    const int* arstart;
     const XT* b;
     XT* x;
     XT* r;
@@ -225,80 +229,231 @@ __device__ __forceinline__ bool grid_allreduce(const AT (&v)[N], double (&out)[N
     return true;
 }
 
-// Aggregate block Jacobi, one aggregate per warp (up to 32 vertices, lane v owns
-// vertex v): rfun(j) performs the phase's update of scalar row j and returns r_j,
-// the warp stages the aggregate's r in shared memory and forms z = B r row by row
-// (B symmetric: lane `row` reads column entries of consecutive rows, coalesced),
-// or, for a pack of isolated vertices, lane v applies vertex v's own 3x3 block;
-// z_j goes to zout[j].x.  Adds the lanes' shares of (r, z) and (r, r).
-constexpr int kAggRows = 96;
-template <typename VT, typename XT, typename PT, typename XT2, typename RF>
-__device__ __forceinline__ void agg_phase(const PcgArgs<VT, XT, PT>& a, XT2* zout, const RF& rfun, XT& rz, XT& rr)
+// Aggregate block Jacobi inside a phase.  Every block owns a contiguous range of
+// aggregates of about equal cost (inverse entries plus a share per vertex for the
+// row updates), cut on the host into rounds of at most AggTile::kStage scalar rows
+// and kAggRoundMax aggregates (rounds [abround[b], abround[b + 1]) of block b,
+// round q = aggregates [arstart[q], arstart[q + 1])).  Per round:
+//  (1) warp 0 tabulates the round's aggregates while all threads perform the
+//      phase's update of the round's scalar rows (rfun(j0, j1, two, r0, r1)
+//      updates row j0 and, if two, row j1, and returns their r) and stage r in
+//      shared memory;
+//  (2) the product of each dense inverse B (symmetric, so a column's entries are
+//      consecutive) with r is cut into items of C columns x all rows, lane = row
+//      (up to three row groups; C = kLoads / row groups, so every lane has kLoads
+//      loads in flight), dealt round-robin to the warps; item c of an aggregate
+//      stores its partial sums in shared slot c;
+//  (3) one thread per row sums its aggregate's slots in slot order (or, in a pack
+//      of isolated vertices, applies the vertex's own 3x3 block) and writes z_j to
+//      zout[j].x.
+// The lanes' shares of (r, z) and (r, r) are added into rz and rr.  The sums do
+// not depend on which warp takes an item, so z is the same in every run.
+template <typename XT>
+struct AggTile;
+template <>
+struct AggTile<float> {
+    static constexpr int kLoads = 48, kStage = 768, kSlots = 8;
+};
+template <>
+struct AggTile<double> {
+    static constexpr int kLoads = 18, kStage = 384, kSlots = 16;
+};
+constexpr int kAggRoundMax = 64;
+constexpr int kAggMaxRows = 96;  // 32 vertices
+// slots an aggregate of up to kAggMaxRows rows needs (its items)
+constexpr int agg_slots(int L)
 {
-    __shared__ XT rs[kPcgThreads / 32][kAggRows];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int nw = gridDim.x * (blockDim.x >> 5);
-    for (int g = blockIdx.x * (blockDim.x >> 5) + wib; g < a.nagg; g += nw) {
-        const int v0 = __ldg(a.avoff + g), sv = __ldg(a.avoff + g + 1) - v0, m = 3 * sv;
-        if (lane < sv) {
-            const int i = __ldg(a.averts + v0 + lane);
+    const int s3 = (kAggMaxRows + L / 3 - 1) / (L / 3), s2 = (64 + L / 2 - 1) / (L / 2), s1 = (32 + L - 1) / L;
+    return s3 > s2 ? (s3 > s1 ? s3 : s1) : (s2 > s1 ? s2 : s1);
+}
+static_assert(agg_slots(AggTile<float>::kLoads) <= AggTile<float>::kSlots, "FP32 item slots");
+static_assert(agg_slots(AggTile<double>::kLoads) <= AggTile<double>::kSlots, "FP64 item slots");
+static_assert(kAggMaxRows <= AggTile<float>::kStage && kAggMaxRows <= AggTile<double>::kStage, "round staging");
+
+struct AggEnt {
+    int m;        // scalar rows
+    int bo;       // offset of the inverse block
+    int rowbase;  // first row in the round's staging
+    int ibeg;     // first item (items of aggregate e: [ibeg(e), ibeg(e + 1)))
+    int pk;       // pack of isolated vertices (3x3 blocks)
+};
+
+template <typename XT>
+struct AggSmem {
+    XT rs[AggTile<XT>::kStage];
+    XT part[AggTile<XT>::kSlots][AggTile<XT>::kStage];
+    int jrow[AggTile<XT>::kStage];             // scalar row of each staged row
+    unsigned char rent[AggTile<XT>::kStage];   // its aggregate's table entry
+    AggEnt ent[kAggRoundMax + 1];
+    int nitems;
+    // the block's rounds [q0, q1); a block with one round keeps its table, rows
+    // and entries from one phase to the next (cached = that round, else -1)
+    int q0, q1, cached, ne, nrows;
+};
+
+// item: columns c0 .. c0 + C - 1 of B (m x m) times rsb, rows lane + 32 k; the
+// loads are all issued before the multiply-adds
+template <int RG, int C, typename XT, typename PT>
+__device__ __forceinline__ void agg_item(const PT* __restrict__ B, int m, int c0, int lane, const XT* rsb, XT* out)
+{
+    // one pointer walks the columns (m apart); the row groups are fixed offsets
+    PT b[RG][C];
+    const PT* p = B + (size_t)c0 * m + lane;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const XT r = rfun(3 * i + c);
-                rs[wib][3 * lane + c] = r;
-                rr += r * r;
-            }
+    for (int u = 0; u < C; ++u) {
+        const bool cu = c0 + u < m;
+#pragma unroll
+        for (int k = 0; k < RG; ++k) b[k][u] = (cu && lane + 32 * k < m) ? __ldg(p + 32 * k) : PT(0);
+        p += cu ? m : 0;
+    }
+    XT acc[RG];
+#pragma unroll
+    for (int k = 0; k < RG; ++k) acc[k] = 0;
+#pragma unroll
+    for (int u = 0; u < C; ++u) {
+        const XT rv = c0 + u < m ? rsb[c0 + u] : XT(0);
+#pragma unroll
+        for (int k = 0; k < RG; ++k) acc[k] += (XT)b[k][u] * rv;
+    }
+#pragma unroll
+    for (int k = 0; k < RG; ++k)
+        if (lane + 32 * k < m) out[lane + 32 * k] = acc[k];
+}
+
+// (tp: block 0's lap accumulators with tracing on, else null: [2] += time to the
+// end of step (1), [5] += time in step (2))
+template <typename VT, typename XT, typename PT, typename XT2, typename RF>
+__device__ __forceinline__ void agg_phase(const PcgArgs<VT, XT, PT>& a, AggSmem<XT>& sm, XT2* zout, const RF& rfun,
+                                          XT& rz, XT& rr, unsigned long long* tp)
+{
+    unsigned long long mark = tp && threadIdx.x == 0 ? gtimer() : 0;
+    auto lap = [&](int k) {
+        if (tp && threadIdx.x == 0) {
+            const unsigned long long t = gtimer();
+            tp[k] += t - mark;
+            mark = t;
         }
-        __syncwarp();
-        const long long bo = __ldg(a.aboff + g);
-        const PT* B = a.ainv + bo;
-        if (sv > 1 && __ldg(a.aboff + g + 1) - bo == 9LL * sv) {
-            // a pack of isolated vertices: each vertex's own 3x3 block
-            if (lane < sv) {
-                const int i = __ldg(a.averts + v0 + lane);
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const PT* Bc = B + 9 * lane + 3 * c;
-                    const XT z = (XT)__ldg(Bc) * rs[wib][3 * lane] + (XT)__ldg(Bc + 1) * rs[wib][3 * lane + 1] +
-                                 (XT)__ldg(Bc + 2) * rs[wib][3 * lane + 2];
-                    zout[3 * i + c].x = z;
-                    rz += rs[wib][3 * lane + c] * z;
+    };
+    using Tile = AggTile<XT>;
+    constexpr int L = Tile::kLoads;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int q0 = sm.q0, q1 = sm.q1;
+    for (int q = q0; q < q1; ++q) {
+        const bool reuse = sm.cached == q;
+        int ne, vb = 0, nrows;
+        if (reuse) {
+            ne = sm.ne;
+            nrows = sm.nrows;
+        } else {
+            const int ga = __ldg(a.arstart + q);
+            ne = __ldg(a.arstart + q + 1) - ga;
+            vb = __ldg(a.avoff + ga);
+            nrows = 3 * (__ldg(a.avoff + ga + ne) - vb);
+        }
+        if (!reuse && wib == 0) {
+            const int ga = __ldg(a.arstart + q);
+            int carry = 0;
+            for (int base = 0; base < ne; base += 32) {
+                const int e = base + lane;
+                int nc = 0;
+                if (e < ne) {
+                    const int g = ga + e;
+                    const int v0 = __ldg(a.avoff + g), sv = __ldg(a.avoff + g + 1) - v0, m = 3 * sv;
+                    const long long bo = __ldg(a.aboff + g), bsz = __ldg(a.aboff + g + 1) - bo;
+                    const int pk = sv > 1 && bsz == 9LL * sv;
+                    const int rg = (m + 31) >> 5, C = L / rg;
+                    nc = pk ? 0 : (m + C - 1) / C;
+                    sm.ent[e].m = m;
+                    sm.ent[e].bo = (int)bo;
+                    sm.ent[e].rowbase = 3 * (v0 - vb);
+                    sm.ent[e].pk = pk;
                 }
-            }
-            __syncwarp();
-            continue;
-        }
-        for (int row = lane; row < m; row += 32) {
-            // twelve independent loads in flight per step: the blocks are read
-            // from L2 and the loop is latency-bound otherwise
-            const PT* Bc = B + row;
-            XT z0 = 0, z1 = 0, z2 = 0, z3 = 0;
-            int c = 0;
-            for (; c + 12 <= m; c += 12) {
-                PT b[12];
+                int incl = nc;
 #pragma unroll
-                for (int u = 0; u < 12; ++u) b[u] = __ldg(Bc + (size_t)(c + u) * m);
-#pragma unroll
-                for (int u = 0; u < 12; u += 4) {
-                    z0 += (XT)b[u] * rs[wib][c + u];
-                    z1 += (XT)b[u + 1] * rs[wib][c + u + 1];
-                    z2 += (XT)b[u + 2] * rs[wib][c + u + 2];
-                    z3 += (XT)b[u + 3] * rs[wib][c + u + 3];
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += t;
                 }
+                if (e < ne) sm.ent[e].ibeg = carry + incl - nc;
+                carry += __shfl_sync(0xffffffffu, incl, 31);
             }
-            for (; c < m; c += 3) {
-                const PT b0 = __ldg(Bc + (size_t)c * m), b1 = __ldg(Bc + (size_t)(c + 1) * m),
-                         b2 = __ldg(Bc + (size_t)(c + 2) * m);
-                z0 += (XT)b0 * rs[wib][c];
-                z1 += (XT)b1 * rs[wib][c + 1];
-                z2 += (XT)b2 * rs[wib][c + 2];
+            if (lane == 0) {
+                sm.ent[ne].ibeg = carry;
+                sm.ent[ne].rowbase = nrows;
+                sm.nitems = carry;
             }
-            const XT z = (z0 + z1) + (z2 + z3);
-            const int i = __ldg(a.averts + v0 + row / 3);
-            zout[3 * i + row % 3].x = z;
-            rz += rs[wib][row] * z;
         }
-        __syncwarp();
+        // two rows per thread and step, both rows' loads issued before the stores
+        for (int lr = threadIdx.x; lr < nrows; lr += 2 * blockDim.x) {
+            const int lr1 = lr + blockDim.x;
+            const bool two = lr1 < nrows;
+            const int j0 = reuse ? sm.jrow[lr] : 3 * __ldg(a.averts + vb + lr / 3) + lr % 3;
+            const int j1 = !two ? j0 : (reuse ? sm.jrow[lr1] : 3 * __ldg(a.averts + vb + lr1 / 3) + lr1 % 3);
+            XT r0, r1;
+            rfun(j0, j1, two, r0, r1);
+            sm.rs[lr] = r0;
+            if (!reuse) sm.jrow[lr] = j0;
+            rr += r0 * r0;
+            if (two) {
+                sm.rs[lr1] = r1;
+                if (!reuse) sm.jrow[lr1] = j1;
+                rr += r1 * r1;
+            }
+        }
+        __syncthreads();
+        lap(2);
+        {
+            const int nit = sm.nitems;
+            int e = 0;
+            for (int it = wib; it < nit; it += nwarp) {
+                while (sm.ent[e + 1].ibeg <= it) ++e;
+                const AggEnt E = sm.ent[e];
+                const int c = it - E.ibeg, rg = (E.m + 31) >> 5;
+                const PT* B = a.ainv + E.bo;
+                const XT* rsb = sm.rs + E.rowbase;
+                XT* out = sm.part[c] + E.rowbase;
+                if (rg == 3) agg_item<3, L / 3>(B, E.m, c * (L / 3), lane, rsb, out);
+                else if (rg == 2) agg_item<2, L / 2>(B, E.m, c * (L / 2), lane, rsb, out);
+                else agg_item<1, L>(B, E.m, c * L, lane, rsb, out);
+            }
+        }
+        __syncthreads();
+        lap(5);
+        for (int lr = threadIdx.x; lr < nrows; lr += blockDim.x) {
+            // the row's aggregate: the last entry with rowbase <= lr
+            int lo = 0;
+            if (reuse) {
+                lo = sm.rent[lr];
+            } else {
+                int hi = ne - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (sm.ent[mid].rowbase <= lr) lo = mid;
+                    else hi = mid - 1;
+                }
+                sm.rent[lr] = (unsigned char)lo;
+            }
+            const AggEnt E = sm.ent[lo];
+            XT z;
+            if (E.pk) {
+                const int t = lr - E.rowbase, v = t / 3, c = t - 3 * v;
+                const PT* Bc = a.ainv + E.bo + 9 * v + 3 * c;
+                const XT* rv = sm.rs + E.rowbase + 3 * v;
+                z = (XT)__ldg(Bc) * rv[0] + (XT)__ldg(Bc + 1) * rv[1] + (XT)__ldg(Bc + 2) * rv[2];
+            } else {
+                const int nc = sm.ent[lo + 1].ibeg - E.ibeg;
+                z = 0;
+                for (int c = 0; c < nc; ++c) z += sm.part[c][lr];
+            }
+            zout[sm.jrow[lr]].x = z;
+            rz += sm.rs[lr] * z;
+        }
+        if (!reuse && q1 - q0 == 1 && threadIdx.x == 0) {
+            sm.cached = q;
+            sm.ne = ne;
+            sm.nrows = nrows;
+        }
+        __syncthreads();  // the next round rewrites the staging
     }
 }
 
@@ -472,28 +627,44 @@ __device__ __forceinline__ XT apply_phase(const PcgArgs<VT, XT, PT>& a, XT beta,
     return v;
 }
 
+// two blocks per SM (the grid's size, coresident_grid): 128 registers a thread,
+// which the aggregate phase's loads in flight use (against 80 at three blocks)
 template <typename VT, typename XT, typename PT>
-__global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_solve(PcgArgs<VT, XT, PT> a)
+__global__ void __launch_bounds__(kPcgThreads, 2) k_pcg_solve(PcgArgs<VT, XT, PT> a)
 {
     PcgScalars* d = a.d;
     unsigned int epoch = 0;
     const int ncon = a.nlist ? min(__ldg(a.nlist), a.ncon) : a.ncon;
     const int nfric = a.nlist ? min(__ldg(a.nlist + 1), a.nfric) : a.nfric;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+    // the aggregate phase's staging (dynamic: launched with it only when nagg > 0)
+    extern __shared__ __align__(16) unsigned char pcg_dyn_smem[];
+    AggSmem<XT>& agg_sm = *reinterpret_cast<AggSmem<XT>*>(pcg_dyn_smem);
     // r = b, x = 0, q_c = 0, z = M^-1 r
     double tot[2];
     if (a.nagg > 0) {
+        if (threadIdx.x == 0) {
+            agg_sm.q0 = __ldg(a.abround + blockIdx.x);
+            agg_sm.q1 = __ldg(a.abround + blockIdx.x + 1);
+            agg_sm.cached = -1;
+        }
+        __syncthreads();
         XT rz0 = 0, rr0 = 0;
         agg_phase(
-            a, a.zp[0],
-            [&](int j) {
-                const XT r = a.b[j];
-                a.r[j] = r;
-                a.x[j] = 0;
-                a.qc[j] = 0;
-                return r;
+            a, agg_sm, a.zp[0],
+            [&](int j0, int j1, bool two, XT& r0, XT& r1) {
+                r0 = a.b[j0];
+                r1 = a.b[j1];
+                a.r[j0] = r0;
+                a.x[j0] = 0;
+                a.qc[j0] = 0;
+                if (two) {
+                    a.r[j1] = r1;
+                    a.x[j1] = 0;
+                    a.qc[j1] = 0;
+                }
             },
-            rz0, rr0);
+            rz0, rr0, nullptr);
         const XT v0[2] = {rz0, rr0};
         double v[2];
         if (!grid_allreduce<2>(v0, v, d, epoch, a.wait_polls, a.part)) return;
@@ -528,12 +699,19 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
     if (!(bb == bb) || !(rz == rz)) done = 2;
     else if (!(bb > 0)) done = 1;
     const bool tr = a.trace && blockIdx.x == 0 && threadIdx.x == 0;
-    unsigned long long tp[6] = {0, 0, 0, 0, 0, 0}, t0 = tr ? gtimer() : 0;
+    // phase laps of block 0 (kept in shared memory: registers are the scarce
+    // resource of this kernel, and a spilled loop-carried value costs an L2 round
+    // trip per iteration once the streamed operands have evicted it from L1)
+    __shared__ unsigned long long tp[7];
+    if (tr) {
+        for (int q = 0; q < 6; ++q) tp[q] = 0;
+        tp[6] = gtimer();
+    }
     auto lap = [&](int k) {
         if (tr) {
             const unsigned long long t = gtimer();
-            tp[k] += t - t0;
-            t0 = t;
+            tp[k] += t - tp[6];
+            tp[6] = t;
         }
     };
     while (!done) {
@@ -559,23 +737,43 @@ __global__ void __launch_bounds__(kPcgThreads, sizeof(XT) == 4 ? 3 : 2) k_pcg_so
         XT rz_t = 0, rr_t = 0;
         if (a.nagg > 0)
             agg_phase(
-                a, zp_next,
-                [&](int j) {
-                    a.x[j] = ldcg(a.x + j) + alpha * ldcg(&zp_next[j].y);
-                    const XT r = ldcg(a.r + j) - alpha * (ldcg(a.qe + j) + ldcg(a.qc + j));
-                    a.r[j] = r;
-                    a.qc[j] = 0;
-                    return r;
+                a, agg_sm, zp_next,
+                [&](int j0, int j1, bool two, XT& r0, XT& r1) {
+                    const XT x0 = ldcg(a.x + j0), p0 = ldcg(&zp_next[j0].y), s0 = ldcg(a.r + j0),
+                             e0 = ldcg(a.qe + j0), c0 = ldcg(a.qc + j0);
+                    const XT x1 = ldcg(a.x + j1), p1 = ldcg(&zp_next[j1].y), s1 = ldcg(a.r + j1),
+                             e1 = ldcg(a.qe + j1), c1 = ldcg(a.qc + j1);
+                    a.x[j0] = x0 + alpha * p0;
+                    r0 = s0 - alpha * (e0 + c0);
+                    a.r[j0] = r0;
+                    a.qc[j0] = 0;
+                    r1 = s1 - alpha * (e1 + c1);
+                    if (two) {
+                        a.x[j1] = x1 + alpha * p1;
+                        a.r[j1] = r1;
+                        a.qc[j1] = 0;
+                    }
                 },
-                rz_t, rr_t);
+                rz_t, rr_t, tr ? tp : nullptr);
         else
         for (int i = gtid; i < a.nv; i += gstride) {
-            XT r[3], z[3];
+            // all loads of the vertex's three rows before its stores (the stores
+            // could alias them, so the loads would otherwise wait for each row)
+            XT r[3], z[3], xv[3], pv[3], rv[3], ev[3], cv[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const int j = 3 * i + c;
-                a.x[j] = ldcg(a.x + j) + alpha * ldcg(&zp_next[j].y);
-                r[c] = ldcg(a.r + j) - alpha * (ldcg(a.qe + j) + ldcg(a.qc + j));
+                xv[c] = ldcg(a.x + j);
+                pv[c] = ldcg(&zp_next[j].y);
+                rv[c] = ldcg(a.r + j);
+                ev[c] = ldcg(a.qe + j);
+                cv[c] = ldcg(a.qc + j);
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const int j = 3 * i + c;
+                a.x[j] = xv[c] + alpha * pv[c];
+                r[c] = rv[c] - alpha * (ev[c] + cv[c]);
                 a.r[j] = r[c];
                 a.qc[j] = 0;
             }
@@ -640,12 +838,19 @@ template <typename VT, typename XT, typename PT>
 int coresident_grid(int nv)
 {
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_solve<VT, XT, PT>, kPcgThreads, 0);
+    // (with the aggregate phase's shared staging, so both launches fit; the FP64
+    // staging is above the default 48 KB of dynamic shared memory)
+    cudaError_t e = cudaFuncSetAttribute(k_pcg_solve<VT, XT, PT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(AggSmem<XT>));
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_solve<VT, XT, PT>, kPcgThreads,
+                                                          sizeof(AggSmem<XT>));
     if (e != cudaSuccess || per_sm < 1) return 0;
     // blocks per SM trade apply-phase parallelism against the cost of the grid
     // reductions, which grows with the number of blocks: two per SM measured best
     // on the 200x200 cloth (FP32: 26 us per iteration against 30 with four and 35
-    // with one); CIPC_PCG_BLOCKS_PER_SM (1..occupancy) overrides
+    // with one, before the kernel's launch bounds fixed two);
+    // CIPC_PCG_BLOCKS_PER_SM (1..occupancy) overrides
     int want = 2;
     if (const char* env = std::getenv("CIPC_PCG_BLOCKS_PER_SM")) {
         const int b = std::atoi(env);
@@ -737,6 +942,8 @@ int solve(Sim* s, const XT* b, XT* x, double tol, int maxit, int* iters, double*
         a.averts = av.verts;
         a.aboff = av.boff;
         a.ainv = reinterpret_cast<const PT*>(av.inv);
+        rc = agg_rounds(s, g, AggTile<XT>::kStage, kAggRoundMax, AggTile<XT>::kLoads, &a.abround, &a.arstart);
+        if (rc) return rc;
     }
     if (s->folded) {
         a.clist = s->crest.p;
@@ -753,8 +960,8 @@ int solve(Sim* s, const XT* b, XT* x, double tol, int maxit, int* iters, double*
     void* args[] = {&a};
     if (e == cudaSuccess) e = cudaEventRecord(st->ev[0], str);
     if (e == cudaSuccess)
-        e = cudaLaunchCooperativeKernel((const void*)k_pcg_solve<VT, XT, PT>, dim3(g), dim3(kPcgThreads), args, 0,
-                                        str);
+        e = cudaLaunchCooperativeKernel((const void*)k_pcg_solve<VT, XT, PT>, dim3(g), dim3(kPcgThreads), args,
+                                        a.nagg > 0 ? sizeof(AggSmem<XT>) : 0, str);
     if (e == cudaSuccess) e = cudaEventRecord(st->ev[1], str);
     if (e == cudaSuccess) e = cudaMemcpyAsync(st->host, st->dsc.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, str);
     if (e == cudaSuccess) e = cudaStreamSynchronize(str);
@@ -768,9 +975,10 @@ int solve(Sim* s, const XT* b, XT* x, double tol, int maxit, int* iters, double*
         const double it = std::max(1, h->it);
         std::fprintf(stderr,
                      "cipc pcg: rel %.3e iters %d stop %d grid %d  us/iter: apply %.2f reduce %.2f update %.2f "
-                     "reduce %.2f\n",
+                     "reduce %.2f (aggregate rows %.2f items %.2f)\n",
                      *rel, h->it, h->done, g, h->tphase[0] * 1e-3 / it, h->tphase[1] * 1e-3 / it,
-                     h->tphase[3] * 1e-3 / it, h->tphase[4] * 1e-3 / it);
+                     h->tphase[3] * 1e-3 / it, h->tphase[4] * 1e-3 / it, h->tphase[2] * 1e-3 / it,
+                     h->tphase[5] * 1e-3 / it);
     }
     if (h->err) return set_error(CIPC_ERR_TIMEOUT, "PCG: a grid-wide wait gave up after %u polls", a.wait_polls);
     if (h->done == 2) return set_error(CIPC_ERR_NAN, "PCG produced NaN");
