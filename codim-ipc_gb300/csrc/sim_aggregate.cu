@@ -342,6 +342,9 @@ __global__ void __launch_bounds__(kInvThreads) k_agg_invert(const int* __restric
     __shared__ double dsc[3 * kAggMax];
     __shared__ GT piv;
     __shared__ int bad;
+    // rows to warps, columns to lanes: no index division in the O(m^3) loops (each
+    // entry is still updated by one thread with the same arithmetic)
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     // symmetric diagonal scaling (unit diagonal) before the elimination: the
     // contact blocks make the rows' scales differ by orders of magnitude
     for (int i = threadIdx.x; i < m; i += blockDim.x) {
@@ -349,10 +352,8 @@ __global__ void __launch_bounds__(kInvThreads) k_agg_invert(const int* __restric
         dsc[i] = d > 0 ? 1.0 / sqrt(d) : 1.0;
     }
     __syncthreads();
-    for (int q = threadIdx.x; q < m * m; q += blockDim.x) {
-        const int i = q / m, j = q - i * m;
-        S[q] = (GT)(Ab[q] * dsc[i] * dsc[j]);
-    }
+    for (int i = wid; i < m; i += nw)
+        for (int j = lane; j < m; j += 32) S[i * m + j] = (GT)(Ab[(size_t)i * m + j] * dsc[i] * dsc[j]);
     if (threadIdx.x == 0) bad = 0;
     for (int k = 0; k < m; ++k) {
         __syncthreads();
@@ -366,19 +367,18 @@ __global__ void __launch_bounds__(kInvThreads) k_agg_invert(const int* __restric
         const GT p = piv;
         for (int j = threadIdx.x; j < m; j += blockDim.x) S[k * m + j] = (j == k ? GT(1) : S[k * m + j]) * p;
         __syncthreads();
-        for (int q = threadIdx.x; q < m * m; q += blockDim.x) {
-            const int i = q / m, j = q - i * m;
+        for (int i = wid; i < m; i += nw) {
             if (i == k) continue;
-            S[q] = (j == k ? GT(0) : S[q]) - fcol[i] * S[k * m + j];
+            const GT f = fcol[i];
+            for (int j = lane; j < m; j += 32) S[i * m + j] = (j == k ? GT(0) : S[i * m + j]) - f * S[k * m + j];
         }
     }
     __syncthreads();
     PT* out = inv + boff[a];
     // symmetrise (the rounding of the elimination is not symmetric)
-    for (int q = threadIdx.x; q < m * m; q += blockDim.x) {
-        const int i = q / m, j = q - i * m;
-        out[q] = (PT)(0.5 * ((double)S[q] + (double)S[j * m + i]) * dsc[i] * dsc[j]);
-    }
+    for (int i = wid; i < m; i += nw)
+        for (int j = lane; j < m; j += 32)
+            out[i * m + j] = (PT)(0.5 * ((double)S[i * m + j] + (double)S[j * m + i]) * dsc[i] * dsc[j]);
     if (threadIdx.x == 0 && bad) atomicExch(flag, 1);
 }
 
