@@ -105,7 +105,10 @@ def test_codim_ccd_step_size_matches(cuda, trajectory):
         assert abs(ag - ao) <= 1e-12 * max(ao, 1e-300), (k, ag, ao)
 
 
-def test_codim_steps_match_direct_solve(cuda, orc):
+@pytest.mark.parametrize("precond", [F.PRECOND_BLOCK_JACOBI, F.PRECOND_AGGREGATE])
+def test_codim_steps_match_direct_solve(cuda, orc, precond):
+    """The aggregate preconditioner's rod aggregates and its pack of the isolated
+    particles (3x3 blocks only) change PCG iteration counts, not the solution."""
     X, T, codim, dbc = scene()
     sh = orc.Shell(X, T, **MAT, codim=codim)
     k2o, dhat2 = sh.init_oipc(DHAT)
@@ -115,7 +118,8 @@ def test_codim_steps_match_direct_solve(cuda, orc):
     assert np.allclose(k2o, k2g, rtol=1e-12) and dhat2 == dhat2g
     xo = X.copy()
     vo = np.zeros_like(X)
-    prm = F.make_params(DT, dhat2, XI, newton_tol=1e-7, pcg_tol=1e-12, max_newton_iters=400)
+    prm = F.make_params(DT, dhat2, XI, newton_tol=1e-7, pcg_tol=1e-12, max_newton_iters=400,
+                        preconditioner=precond)
     diag = np.linalg.norm(X.max(0) - X.min(0))
     for step in range(6):
         s.set_state(xo, vo)
@@ -127,3 +131,4 @@ def test_codim_steps_match_direct_solve(cuda, orc):
         assert stg.min_dist2 > 0 or stg.n_constraints == 0
         err = np.abs(xg - xo).max()
         assert err <= 1e-8 * diag, (step, err, sto, stg.as_dict())
+        assert stg.precond_fallbacks == 0  # the aggregate solves ran as aggregate solves
