@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "../../include/cipc.h"
+#include "agg_rounds.h"
 #include "cipc_util.h"
 #include "constraint_eval.cuh"
 #include "sim.h"
@@ -466,43 +467,8 @@ int agg_rounds(Sim* s, int grid, int rows, int maxagg, int loads, const int** br
     if (!st || grid < 1 || rows < st->max_m || maxagg < 1 || loads < 3)
         return set_error(CIPC_ERR_INVALID_ARG, "aggregate rounds: no aggregates or limits below the largest block");
     if (st->rk_grid != grid || st->rk_rows != rows || st->rk_max != maxagg || st->rk_loads != loads) {
-        // The phase is latency-bound: a warp takes one item (a column slice of a
-        // dense product) per L2 round trip, a thread two rows of updates per round
-        // trip.  Cost of an aggregate in those units (x 1024 for 256-thread blocks
-        // of 8 warps): 128 per item, 10 per scalar row (its loads, the staging and
-        // the store of z).
-        const int nagg = st->nagg;
-        std::vector<long long> cost(nagg + 1, 0);
-        for (int g = 0; g < nagg; ++g) {
-            const int sv = st->h_voff[g + 1] - st->h_voff[g], m = 3 * sv;
-            const bool pk = sv > 1 && st->h_boff[g + 1] - st->h_boff[g] == 9LL * sv;
-            const int rg = (m + 31) / 32, C = std::max(1, loads / rg);
-            const long long items = pk ? 0 : (m + C - 1) / C;
-            cost[g + 1] = cost[g] + 128 * items + 10LL * m;
-        }
-        const long long T = cost[nagg];
-        std::vector<int> br(grid + 1), rs;
-        rs.reserve(nagg + 1);
-        int a = 0;
-        for (int b = 0; b < grid; ++b) {
-            br[b] = (int)rs.size();
-            // block b: the aggregates whose cost prefix lies in [T b / grid, T (b + 1) / grid)
-            const long long end = T * (b + 1) / grid;
-            int hi = a;
-            while (hi < nagg && (b + 1 == grid || cost[hi] < end)) ++hi;
-            for (int g = a; g < hi;) {
-                rs.push_back(g);
-                int nr = 0, cnt = 0;
-                while (g < hi && cnt < maxagg && nr + 3 * (st->h_voff[g + 1] - st->h_voff[g]) <= rows) {
-                    nr += 3 * (st->h_voff[g + 1] - st->h_voff[g]);
-                    ++cnt;
-                    ++g;
-                }
-            }
-            a = hi;
-        }
-        br[grid] = (int)rs.size();
-        rs.push_back(nagg);
+        std::vector<int> br, rs;
+        agg_partition(st->h_voff, st->h_boff, grid, rows, maxagg, loads, br, rs);
         cudaStreamSynchronize(s->stream);
         if (st->bround.alloc(br.size()) != cudaSuccess || st->rstart.alloc(rs.size()) != cudaSuccess)
             return set_error(CIPC_ERR_CUDA, "aggregate rounds");

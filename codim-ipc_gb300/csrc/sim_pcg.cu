@@ -35,6 +35,7 @@
 #include <cstring>
 
 #include "../../include/cipc.h"
+#include "agg_rounds.h"
 #include "cipc_util.h"
 #include "constraint_eval.cuh"
 #include "sim.h"
@@ -361,8 +362,7 @@ __device__ __forceinline__ void agg_phase(const PcgArgs<VT, XT, PT>& a, AggSmem<
                     const int v0 = __ldg(a.avoff + g), sv = __ldg(a.avoff + g + 1) - v0, m = 3 * sv;
                     const long long bo = __ldg(a.aboff + g), bsz = __ldg(a.aboff + g + 1) - bo;
                     const int pk = sv > 1 && bsz == 9LL * sv;
-                    const int rg = (m + 31) >> 5, C = L / rg;
-                    nc = pk ? 0 : (m + C - 1) / C;
+                    nc = agg_items(m, pk, L);
                     sm.ent[e].m = m;
                     sm.ent[e].bo = (int)bo;
                     sm.ent[e].rowbase = 3 * (v0 - vb);
