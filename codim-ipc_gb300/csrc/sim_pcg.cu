@@ -231,10 +231,10 @@ __device__ __forceinline__ bool grid_allreduce(const AT (&v)[N], double (&out)[N
 }
 
 // Aggregate block Jacobi inside a phase.  Every block owns a contiguous range of
-// aggregates of about equal cost (inverse entries plus a share per vertex for the
-// row updates), cut on the host into rounds of at most AggTile::kStage scalar rows
-// and kAggRoundMax aggregates (rounds [abround[b], abround[b + 1]) of block b,
-// round q = aggregates [arstart[q], arstart[q + 1])).  Per round:
+// aggregates of about equal cost (the phase's column items and rows: agg_partition
+// in agg_rounds.h), cut on the host into rounds of at most AggTile::kStage scalar
+// rows and kAggRoundMax aggregates (rounds [abround[b], abround[b + 1]) of block
+// b, round q = aggregates [arstart[q], arstart[q + 1])).  Per round:
 //  (1) warp 0 tabulates the round's aggregates while all threads perform the
 //      phase's update of the round's scalar rows (rfun(j0, j1, two, r0, r1)
 //      updates row j0 and, if two, row j1, and returns their r) and stage r in
@@ -270,6 +270,8 @@ constexpr int agg_slots(int L)
 static_assert(agg_slots(AggTile<float>::kLoads) <= AggTile<float>::kSlots, "FP32 item slots");
 static_assert(agg_slots(AggTile<double>::kLoads) <= AggTile<double>::kSlots, "FP64 item slots");
 static_assert(kAggMaxRows <= AggTile<float>::kStage && kAggMaxRows <= AggTile<double>::kStage, "round staging");
+// the item widths agg_phase dispatches on (L / row groups) are agg_cols's
+static_assert(AggTile<float>::kLoads >= 3 && AggTile<double>::kLoads >= 3, "item width");
 
 struct AggEnt {
     int m;        // scalar rows
